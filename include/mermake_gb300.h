@@ -1,0 +1,154 @@
+/*
+ * mermake_gb300 -- C ABI of the GB300 (sm_103a) implementation of MERMAKE's
+ * per-FOV image path.
+ *
+ * Every entry point takes plain device pointers, element strides and sizes,
+ * and a cudaStream_t passed as void* (NULL = legacy default stream); work is
+ * enqueued on that stream.  Entry points that must report a count to the
+ * host (maxima, spots) synchronise that stream once, at the end.  All device
+ * buffers are owned by the caller; an mm_ctx owns only reusable scratch
+ * (spectrum/tile workspaces, candidate lists, counters), grows it on demand
+ * and frees it in mm_ctx_destroy.  An mm_ctx may be used by one host thread
+ * at a time.  FFT plans (twiddle tables) are cached per device for the life
+ * of the process; the first call at a new length uploads them synchronously,
+ * so make it before any stream capture.
+ *
+ * Return value: MM_OK or an error code; mm_last_error() gives the message of
+ * the calling thread's last failure.  Layouts follow the reference: volumes
+ * are (z, x, y) with y contiguous; Xh rows are 8 float32
+ * [zc, xc, yc, background, a, habs, hn, h].
+ *
+ * Each declaration cites the reference interface it replaces (paths inside
+ * the deprekate/MERMAKE v0.0.74 tree).
+ */
+#ifndef MERMAKE_GB300_H
+#define MERMAKE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    MM_OK = 0,
+    MM_EINVAL = 1,     /* bad argument: ValueError / TypeError / IndexError in the reference */
+    MM_ENOMEM = 2,     /* device allocation of scratch failed */
+    MM_EOVERFLOW = 3,  /* output capacity too small; *count holds the exact count, retry */
+    MM_ETIMEOUT = 4,   /* a bounded device-side wait gave up */
+    MM_EDEVICE = 5     /* CUDA runtime error */
+};
+
+/* element types of image / raw operands */
+enum { MM_DTYPE_F32 = 0, MM_DTYPE_U16 = 1 };
+
+typedef struct mm_ctx mm_ctx;
+
+/* Version of this ABI (bumped on incompatible changes). */
+int mm_abi_version(void);
+/* Message of the calling thread's last error ("" if none). */
+const char *mm_last_error(void);
+/* Scratch owner for the calls below (no reference counterpart: it replaces
+ * CuPy's memory pool and the per-call free_all_blocks, mermake/maxima.py:96). */
+int mm_ctx_create(mm_ctx **out);
+int mm_ctx_destroy(mm_ctx *ctx);
+
+/* fill.reflect (mermake/fill.py:54-111, kernel `mirror` fill.py:6-52), in place.
+ * mode 0 = "out" (a[j] = a[2i-j] for j > i), 1 = "in" (for j < i).
+ * shape/strides are host arrays of ndim int64 (strides in elements). */
+int mm_reflect_f32(float *arr, int ndim, const int64_t *shape, const int64_t *strides, int axis, int i,
+                   int mode, void *stream);
+
+/* blur.box_1d (mermake/blur.py:157-188, kernel box_1d blur.cu:1-52): mean over
+ * [c-delta, c+delta] clipped to the axis.  A 2-D image is (1, x, y).
+ * in_strides/out_strides: host int64[3] (elements). */
+int mm_box_1d_f32(const float *in, const int64_t *in_strides, float *out, const int64_t *out_strides,
+                  int size_z, int size_x, int size_y, int delta, int axis, void *stream);
+
+/* math.subtract_clamp (mode 0, mermake/math.py:4-17) and math.subtract_reflect
+ * (mode 1, mermake/math.py:20-33) on uint16 arrays of any rank <= 8. */
+int mm_subtract_u16(const uint16_t *x, const int64_t *x_strides, const uint16_t *y, const int64_t *y_strides,
+                    uint16_t *z, const int64_t *z_strides, int ndim, const int64_t *shape, int mode,
+                    void *stream);
+
+/* Deconvolver.__init__ for one PSF (mermake/deconvolver.py:48-75 with
+ * center_psf 238-270 and laplacian_3d 24-36): writes the Wiener spectrum
+ * conj(H)/(|H|^2 + beta |L|^2), pre-divided by Zp*P*P, as the half spectrum
+ * W[Zp][P][P/2+1] of complex64 (float2), Zp = tile_height + 2*zpad,
+ * P = tile_size + 2*overlap.  psf: float32 (pz, px, py), device. */
+int mm_wiener_spectrum(mm_ctx *ctx, const float *psf, int pz, int px, int py, int tile_height, int tile_size,
+                       int zpad, int overlap, float beta, void *W, void *stream);
+
+/* Deconvolver.tile_wise / apply (mermake/deconvolver.py:98-184) for tiles
+ * [tile_begin, tile_begin + tile_count) of the x-major tile grid of a
+ * (Z, X, Y) channel, uint16 or float32 (image_dtype; strides isz, isx, 1).  flat: float32 (X, Y) with row stride fsx, or NULL.
+ * W: npsf spectra as made by mm_wiener_spectrum (tile i uses spectrum i when
+ * npsf > 1).  blur_radius < 0: no background subtraction.
+ * Outputs (any may be NULL):
+ *   res_out    (tile_count, Z, P, P) float32: tile_res after blur subtraction;
+ *              the yielded view is [:, :xend, :yend]
+ *   raw_out    (tile_count, Z, P, P) float32: the raw view tile_pad[zpad:-zpad]
+ *              with the flat multiplied back (deconvolver.py:165-170)
+ *   stitch_out (Z, X, Y) float32 with strides (osz, osx, 1): tile centres
+ *              written as Deconvolver.apply does (deconvolver.py:179-183). */
+int mm_deconv_tiles(mm_ctx *ctx, const void *image, int image_dtype, int Z, int X, int Y, int64_t isz, int64_t isx,
+                    const float *flat, int64_t fsx, const void *W, int npsf, int tile_size, int zpad,
+                    int overlap, int tile_begin, int tile_count, int blur_radius, float *res_out, float *raw_out,
+                    float *stitch_out, int64_t osz, int64_t osx, void *stream);
+
+/* find_local_maxima (mermake/maxima.py:17-98; kernels local_maxima_count,
+ * local_maxima, delta_fit_cross_corr in mermake/maxima.cu) on one (Z, X, Y)
+ * float32 volume with strides (isz, isx, 1).  raw: same shape, raw_dtype 0 =
+ * float32 (MM_DTYPE_F32), 1 = uint16 (MM_DTYPE_U16), strides (rsz, rsx, 1).  norm_div != 0 reads the image
+ * as v / norm_div (then negated if negate), bit-identical to dividing the
+ * volume first (mermake/__main__.py:222-224).  Writes min(count, out_cap) rows
+ * to out and the count to *count (host); MM_EOVERFLOW if count > out_cap.
+ * delta > 5 -> MM_EINVAL (the reference raises TypeError). */
+int mm_find_local_maxima(mm_ctx *ctx, const float *image, int Z, int X, int Y, int64_t isz, int64_t isx,
+                         const void *raw, int raw_dtype, int64_t rsz, int64_t rsx, float threshold, int delta,
+                         int delta_fit, float sigmaZ, float sigmaXY, float norm_div, int negate, float *out,
+                         uint32_t out_cap, uint32_t *count, void *stream);
+
+/* One hyb colour (mermake/__main__.py:242-265): tile_wise over every tile,
+ * find_local_maxima on each yielded tile with its raw view, keep rows with
+ * overlap <= xc, yc < extent - overlap, shift by the tile origin, concatenate.
+ * Tiles run `batch` at a time.  Rows are appended to out (row order is not
+ * specified, as in the reference); *count = total rows; MM_EOVERFLOW if it
+ * exceeds out_cap. */
+int mm_hyb_spots(mm_ctx *ctx, const uint16_t *image, int Z, int X, int Y, int64_t isz, int64_t isx,
+                 const float *flat, int64_t fsx, const void *W, int npsf, int tile_size, int zpad, int overlap,
+                 int blur_radius, float threshold, int delta, int delta_fit, float sigmaZ, float sigmaXY,
+                 int batch, float *out, uint32_t out_cap, uint32_t *count, void *stream);
+
+/* The DAPI block (mermake/__main__.py:215-225): Deconvolver.apply into `buffer`
+ * (Z, X, Y) float32, divide by the RMS, find_local_maxima (+), negate,
+ * find_local_maxima (-), both with the uint16 channel as raw.  The division
+ * and negation are applied on read; `buffer` keeps the un-normalised result.
+ * *rms receives the divisor used (float). */
+int mm_dapi_spots(mm_ctx *ctx, const uint16_t *image, int Z, int X, int Y, int64_t isz, int64_t isx,
+                  const float *flat, int64_t fsx, const void *W, int npsf, int tile_size, int zpad, int overlap,
+                  int blur_radius, float threshold, int delta, int delta_fit, float sigmaZ, float sigmaXY,
+                  int batch, float *buffer, float *out_plus, uint32_t cap_plus, uint32_t *count_plus,
+                  float *out_minus, uint32_t cap_minus, uint32_t *count_minus, float *rms, void *stream);
+
+/* Tile layout of Deconvolver.tiled / tile_wise (mermake/deconvolver.py:117-148,
+ * 186-206), host only (no device work).  tile < 0 returns the number of tiles.
+ * desc (13 int32): x, y, x0, y0, xd, yd, xstart, ystart, xend, yend, psf index,
+ * P, Zp.  map_z (Zp), map_x (P), map_y (P): for each padded index, the source
+ * index inside the tile after placement and the reference's reflect calls, or
+ * -1 where the padded tile holds zero.  Any output may be NULL. */
+int mm_tile_geometry(int Z, int X, int Y, int tile_size, int zpad, int overlap, int npsf, int tile, int32_t *desc,
+                     int32_t *map_z, int32_t *map_x, int32_t *map_y);
+
+/* Engine diagnostic, no reference counterpart (the reference calls cuFFT via
+ * cp.fft.fftn/ifftn, mermake/deconvolver.py:155-157): in-place unnormalised
+ * complex64 DFT of nlines lines of length n stored element-major
+ * (element e of line l at data[e*nlines + l]); inverse uses exp(+i...). */
+int mm_fft_c2c(void *data, int n, int nlines, int inverse, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MERMAKE_GB300_H */

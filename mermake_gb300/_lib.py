@@ -1,0 +1,135 @@
+"""ctypes binding of ``libmermake_gb300.so`` (the C ABI in include/mermake_gb300.h).
+
+The library is the only compute path: if it is missing, or no CUDA device is
+present, every entry point raises instead of falling back to another
+implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import torch
+
+from . import _build
+
+MM_OK, MM_EINVAL, MM_ENOMEM, MM_EOVERFLOW, MM_ETIMEOUT, MM_EDEVICE = range(6)
+
+_lock = threading.Lock()
+_lib = None
+_ctx = {}
+
+
+class MermakeError(RuntimeError):
+    """A CUDA-side failure reported by the library (MM_EDEVICE / MM_ETIMEOUT)."""
+
+
+class Overflow(Exception):
+    def __init__(self, count):
+        super().__init__(count)
+        self.count = count
+
+
+_vp = C.c_void_p
+_i32 = C.c_int
+_i64 = C.c_int64
+_u32 = C.c_uint32
+_f32 = C.c_float
+_pi64 = C.POINTER(C.c_int64)
+_pu32 = C.POINTER(C.c_uint32)
+_pf32 = C.POINTER(C.c_float)
+
+_SIGS = {
+    "mm_abi_version": ([], _i32),
+    "mm_last_error": ([], C.c_char_p),
+    "mm_ctx_create": ([C.POINTER(_vp)], _i32),
+    "mm_ctx_destroy": ([_vp], _i32),
+    "mm_reflect_f32": ([_vp, _i32, _pi64, _pi64, _i32, _i32, _i32, _vp], _i32),
+    "mm_box_1d_f32": ([_vp, _pi64, _vp, _pi64, _i32, _i32, _i32, _i32, _i32, _vp], _i32),
+    "mm_subtract_u16": ([_vp, _pi64, _vp, _pi64, _vp, _pi64, _i32, _pi64, _i32, _vp], _i32),
+    "mm_wiener_spectrum": ([_vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _i32, _f32, _vp, _vp], _i32),
+    "mm_deconv_tiles": ([_vp, _vp, _i32, _i32, _i32, _i32, _i64, _i64, _vp, _i64, _vp] + [_i32] * 7
+                        + [_vp, _vp, _vp, _i64, _i64, _vp], _i32),
+    "mm_find_local_maxima": ([_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i32, _i64, _i64, _f32, _i32, _i32,
+                              _f32, _f32, _f32, _i32, _vp, _u32, _pu32, _vp], _i32),
+    "mm_hyb_spots": ([_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i64, _vp, _i32, _i32, _i32, _i32, _i32, _f32,
+                      _i32, _i32, _f32, _f32, _i32, _vp, _u32, _pu32, _vp], _i32),
+    "mm_dapi_spots": ([_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i64, _vp, _i32, _i32, _i32, _i32, _i32, _f32,
+                       _i32, _i32, _f32, _f32, _i32, _vp, _vp, _u32, _pu32, _vp, _u32, _pu32, _pf32, _vp], _i32),
+    "mm_tile_geometry": ([_i32] * 8 + [_vp] * 4, _i32),
+    "mm_fft_c2c": ([_vp, _i32, _i32, _i32, _vp], _i32),
+}
+
+
+def declared_symbols():
+    """Names of the entry points bound here (checked against include/*.h by tests)."""
+    return sorted(_SIGS)
+
+
+def load(require_gpu=True):
+    """Loads (building first if needed) the shared library."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            path = _build.LIB
+            if not os.path.exists(path):
+                path = _build.build()
+            lib = C.CDLL(path)
+            for name, (args, res) in _SIGS.items():
+                fn = getattr(lib, name)
+                fn.argtypes = args
+                fn.restype = res
+            _lib = lib
+    if require_gpu and not torch.cuda.is_available():
+        raise MermakeError("mermake_gb300 needs a CUDA device; none is visible")
+    return _lib
+
+
+def lib():
+    return load(True)
+
+
+def ctx(device=None):
+    """The process-wide mm_ctx of a device (scratch owner)."""
+    L = lib()
+    dev = torch.cuda.current_device() if device is None else int(device)
+    with _lock:
+        c = _ctx.get(dev)
+        if c is None:
+            with torch.cuda.device(dev):
+                p = _vp()
+                check(L.mm_ctx_create(C.byref(p)))
+            c = _ctx[dev] = p
+    return c
+
+
+def last_error():
+    return (_lib.mm_last_error() or b"").decode(errors="replace") if _lib else ""
+
+
+def check(rc, exc=ValueError):
+    if rc == MM_OK:
+        return
+    msg = last_error()
+    if rc == MM_EINVAL:
+        raise exc(msg)
+    if rc == MM_ENOMEM:
+        raise MemoryError(msg)
+    if rc == MM_ETIMEOUT:
+        raise MermakeError("device wait timed out: " + msg)
+    raise MermakeError(msg or "mermake_gb300 error %d" % rc)
+
+
+def stream_ptr(stream=None):
+    s = torch.cuda.current_stream() if stream is None else stream
+    return _vp(s.cuda_stream)
+
+
+def i64arr(vals):
+    a = (C.c_int64 * len(vals))(*[int(v) for v in vals])
+    return a
+
+
+def ptr(t):
+    return _vp(t.data_ptr()) if t is not None else _vp(0)

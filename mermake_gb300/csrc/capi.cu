@@ -1,0 +1,422 @@
+// C ABI entry points (include/mermake_gb300.h): context, scratch, and the
+// drivers that chain the kernels of deconv.cu / wiener.cu / maxima.cu.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "deconv.cuh"
+
+namespace {
+thread_local char g_err[1024] = "";
+
+enum Slot { WS_SPEC = 0, WS_RES, WS_TMP, WS_VOL, WS_CAND, WS_SMALL, WS_N };
+}  // namespace
+
+void mm_set_error(const char *fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+struct mm_ctx {
+    std::mutex mu;
+    void *ws[WS_N] = {};
+    size_t ws_bytes[WS_N] = {};
+    unsigned *h_counters = nullptr;  // pinned: [0] candidates, [1] rows, [2] rows (2nd set)
+    int device = 0;
+};
+
+namespace {
+
+int ws_get(mm_ctx *c, Slot s, size_t bytes, void **out) {
+    if (bytes == 0) bytes = 16;
+    if (c->ws_bytes[s] < bytes) {
+        if (c->ws[s]) {
+            MM_CUDA_TRY(cudaDeviceSynchronize());
+            cudaFree(c->ws[s]);
+            c->ws[s] = nullptr;
+            c->ws_bytes[s] = 0;
+        }
+        // grow with headroom so that slowly growing requests do not thrash
+        size_t want = bytes + bytes / 8;
+        cudaError_t e = cudaMalloc(&c->ws[s], want);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            e = cudaMalloc(&c->ws[s], bytes);
+            want = bytes;
+        }
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            c->ws[s] = nullptr;
+            mm_set_error("cudaMalloc of %zu bytes of scratch failed: %s", bytes, cudaGetErrorString(e));
+            return MM_ENOMEM;
+        }
+        c->ws_bytes[s] = want;
+    }
+    *out = c->ws[s];
+    return MM_OK;
+}
+
+// small device scratch: counters and reduction cells
+struct Small {
+    unsigned cand;       // candidate count
+    unsigned rows;       // kept rows (set 1)
+    unsigned rows2;      // kept rows (set 2)
+    unsigned overflow;   // largest candidate count that did not fit
+    double sumsq;
+    float div;
+    float pad_;
+};
+
+int small_get(mm_ctx *c, Small **out) {
+    void *p;
+    int rc = ws_get(c, WS_SMALL, sizeof(Small), &p);
+    *out = (Small *)p;
+    return rc;
+}
+
+int fill_geom(TileGeom &g, int Z, int X, int Y, long long isz, long long isx, long long fsx, int ts, int zpad,
+              int ov, int npsf) {
+    MM_REQUIRE(Z > 0 && X > 0 && Y > 0, "empty channel (%d, %d, %d)", Z, X, Y);
+    MM_REQUIRE(Z < 65536 && X < 65536 && Y < 65536, "channel dimensions must be < 65536");
+    MM_REQUIRE(ts > 0, "tile_size must be positive");
+    MM_REQUIRE(ov >= 0, "overlap must be >= 0");
+    MM_REQUIRE(zpad >= 1, "zpad must be >= 1 (the reference's [zpad:-zpad] crop is empty for zpad = 0)");
+    MM_REQUIRE(npsf >= 1, "need at least one Wiener spectrum");
+    g.Z = Z; g.X = X; g.Y = Y;
+    g.isz = isz; g.isx = isx; g.fsx = fsx;
+    g.ts = ts; g.ov = ov; g.zpad = zpad;
+    g.P = ts + 2 * ov;
+    g.H = g.P / 2 + 1;
+    g.Zp = Z + 2 * zpad;
+    MM_REQUIRE(g.P <= MM_FFT_MAXN && g.Zp <= MM_FFT_MAXN, "padded tile (%d, %d) exceeds the FFT length limit %d",
+               g.Zp, g.P, MM_FFT_MAXN);
+    g.ny = (Y + ts - 1) / ts;
+    g.t0 = 0; g.nt = 0;
+    g.npsf = npsf;
+    return MM_OK;
+}
+
+int ntiles_of(const TileGeom &g) {
+    int nx = (g.X + g.ts - 1) / g.ts;
+    int n = nx * g.ny;
+    // zip(tiles, psf_ffts) truncates when several spectra are given (deconvolver.py:110, 116)
+    if (g.npsf > 1 && g.npsf < n) n = g.npsf;
+    return n;
+}
+
+// tile_wise core for tiles [g.t0, g.t0 + g.nt)
+int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *flat, const float2 *W, int blur_radius,
+              float *res_out, float *raw_out, float *stitch, long long osz, long long osx, cudaStream_t st) {
+    const long long plane_c = (long long)g.P * g.H;
+    const long long tile_c = (long long)g.Z * plane_c;
+    const long long tile_r = (long long)g.Z * g.P * g.P;
+    void *spec, *res, *tmp = nullptr;
+    int rc;
+    if ((rc = ws_get(c, WS_SPEC, sizeof(float2) * tile_c * g.nt, &spec))) return rc;
+    res = res_out;
+    if (!res && (rc = ws_get(c, WS_RES, sizeof(float) * tile_r * g.nt, &res))) return rc;
+    if (blur_radius >= 0 && (rc = ws_get(c, WS_TMP, sizeof(float) * tile_r * g.nt, &tmp))) return rc;
+    float2 *S = (float2 *)spec;
+    const long long wstride = (long long)g.Zp * plane_c;
+    if ((rc = mm_launch_rows_fwd_img(g, image, dtype, flat, S, st))) return rc;
+    if ((rc = mm_launch_cols(S, g.P, g.H, g.H, plane_c, g.nt * g.Z, false, st))) return rc;
+    if ((rc = mm_launch_zpass(g, S, W, wstride, st))) return rc;
+    if ((rc = mm_launch_cols(S, g.P, g.H, g.H, plane_c, g.nt * g.Z, true, st))) return rc;
+    if ((rc = mm_launch_rows_inv(S, g.nt * g.Z * g.P, g.P, g.H, (float *)res, st))) return rc;
+    const int delta = blur_radius >= 0 ? blur_radius / 2 : -1;
+    if (delta >= 0 && (rc = mm_launch_blur_y((float *)res, (float *)tmp, g.nt * g.Z * g.P, g.P, delta, st)))
+        return rc;
+    if (delta >= 0 || stitch) {
+        if ((rc = mm_launch_blur_x_sub(g, (float *)res, (float *)tmp, delta, (float *)res, stitch, osz, osx, st)))
+            return rc;
+    }
+    if (raw_out && (rc = mm_launch_make_raw(g, image, dtype, flat, raw_out, st))) return rc;
+    return MM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mm_abi_version(void) { return 1; }
+
+const char *mm_last_error(void) { return g_err; }
+
+int mm_ctx_create(mm_ctx **out) {
+    MM_REQUIRE(out != nullptr, "null output pointer");
+    mm_ctx *c = new mm_ctx();
+    MM_CUDA_TRY(cudaGetDevice(&c->device));
+    if (cudaMallocHost(&c->h_counters, 16 * sizeof(unsigned)) != cudaSuccess) {
+        cudaGetLastError();
+        delete c;
+        mm_set_error("cudaMallocHost for counters failed");
+        return MM_ENOMEM;
+    }
+    int rc = mm_maxima_ensure_init(0);
+    if (rc) {
+        cudaFreeHost(c->h_counters);
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return MM_OK;
+}
+
+int mm_ctx_destroy(mm_ctx *c) {
+    if (!c) return MM_OK;
+    cudaDeviceSynchronize();
+    for (int s = 0; s < WS_N; ++s)
+        if (c->ws[s]) cudaFree(c->ws[s]);
+    if (c->h_counters) cudaFreeHost(c->h_counters);
+    delete c;
+    return MM_OK;
+}
+
+int mm_wiener_spectrum(mm_ctx *c, const float *psf, int pz, int px, int py, int tile_height, int tile_size,
+                       int zpad, int overlap, float beta, void *W, void *stream) {
+    MM_REQUIRE(c && psf && W, "null argument");
+    MM_REQUIRE(pz > 0 && px > 0 && py > 0, "empty PSF");
+    MM_REQUIRE(tile_height > 0 && tile_size > 0 && zpad >= 0 && overlap >= 0, "bad tile geometry");
+    std::lock_guard<std::mutex> lock(c->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    const int nz = tile_height + 2 * zpad, nx = tile_size + 2 * overlap;
+    MM_REQUIRE(nz <= MM_FFT_MAXN && nx <= MM_FFT_MAXN, "padded PSF exceeds the FFT length limit");
+    const int H = nx / 2 + 1;
+    void *vol, *spec;
+    Small *sm;
+    int rc;
+    if ((rc = ws_get(c, WS_VOL, sizeof(float) * (size_t)nz * nx * nx, &vol))) return rc;
+    if ((rc = ws_get(c, WS_SPEC, sizeof(float2) * (size_t)nz * nx * H, &spec))) return rc;
+    if ((rc = small_get(c, &sm))) return rc;
+    return mm_wiener_build_impl(psf, pz, px, py, tile_height, tile_size, zpad, overlap, beta, (float2 *)W,
+                                (float *)vol, (float2 *)spec, &sm->sumsq, st);
+}
+
+int mm_deconv_tiles(mm_ctx *c, const void *image, int image_dtype, int Z, int X, int Y, int64_t isz, int64_t isx,
+                    const float *flat, int64_t fsx, const void *W, int npsf, int tile_size, int zpad, int overlap,
+                    int tile_begin, int tile_count, int blur_radius, float *res_out, float *raw_out,
+                    float *stitch_out, int64_t osz, int64_t osx, void *stream) {
+    MM_REQUIRE(c && image && W, "null argument");
+    TileGeom g;
+    int rc = fill_geom(g, Z, X, Y, isz, isx, fsx, tile_size, zpad, overlap, npsf);
+    if (rc) return rc;
+    const int nt = ntiles_of(g);
+    MM_REQUIRE(tile_begin >= 0 && tile_count >= 0 && tile_begin + tile_count <= nt,
+               "tiles [%d, %d) outside the %d tiles of the channel", tile_begin, tile_begin + tile_count, nt);
+    MM_REQUIRE(!stitch_out || overlap >= 1, "stitching needs overlap >= 1");
+    MM_REQUIRE(image_dtype == MM_DTYPE_U16 || image_dtype == MM_DTYPE_F32, "image_dtype must be uint16 or float32");
+    if (tile_count == 0) return MM_OK;
+    g.t0 = tile_begin;
+    g.nt = tile_count;
+    std::lock_guard<std::mutex> lock(c->mu);
+    return run_tiles(c, g, image, image_dtype, flat, (const float2 *)W, blur_radius, res_out, raw_out, stitch_out, osz, osx,
+                     (cudaStream_t)stream);
+}
+
+int mm_find_local_maxima(mm_ctx *c, const float *image, int Z, int X, int Y, int64_t isz, int64_t isx,
+                         const void *raw, int raw_dtype, int64_t rsz, int64_t rsx, float threshold, int delta,
+                         int delta_fit, float sigmaZ, float sigmaXY, float norm_div, int negate, float *out,
+                         uint32_t out_cap, uint32_t *count, void *stream) {
+    MM_REQUIRE(c && image && raw && count, "null argument");
+    MM_REQUIRE(delta <= 5, "Delta must be an less than or equal to 5 due to MAX_KERNEL_POINTS");
+    MM_REQUIRE(delta >= 0 && delta_fit >= 0, "negative delta");
+    MM_REQUIRE(raw_dtype == 0 || raw_dtype == 1, "raw_dtype must be 0 (float32) or 1 (uint16)");
+    MM_REQUIRE(Z < 65536 && X < 65536 && Y < 65536, "dimensions must be < 65536");
+    *count = 0;
+    if ((long long)Z * X * Y == 0) return MM_OK;
+    std::lock_guard<std::mutex> lock(c->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    Small *sm;
+    int rc;
+    if ((rc = small_get(c, &sm))) return rc;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        size_t cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
+        if (cap < 65536) cap = 65536;
+        void *cand;
+        if ((rc = ws_get(c, WS_CAND, cap * sizeof(uint2), &cand))) return rc;
+        cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
+        MaximaArgs a = {};
+        a.img = image; a.isz = isz; a.isx = isx; a.ivol = 0;
+        a.Z = Z; a.X = X; a.Y = Y; a.nvol = 1;
+        a.tiles = nullptr;
+        a.raw_kind = raw_dtype; a.raw = raw; a.rsz = rsz; a.rsx = rsx; a.rvol = 0;
+        a.th = threshold; a.delta = delta; a.delta_fit = delta_fit;
+        a.sigmaZ = sigmaZ; a.sigmaXY = sigmaXY;
+        a.div = norm_div; a.divp = nullptr; a.neg = negate; a.keep_filter = 0;
+        if ((rc = mm_launch_maxima_fit(a, (uint2 *)cand, (unsigned)cap, &sm->cand, out, out_cap, nullptr, 0, st)))
+            return rc;
+        MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters, &sm->cand, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        MM_CUDA_TRY(cudaStreamSynchronize(st));
+        unsigned n = c->h_counters[0];
+        if (n <= cap) {
+            *count = n;
+            return n > out_cap ? MM_EOVERFLOW : MM_OK;
+        }
+        if ((rc = ws_get(c, WS_CAND, (size_t)n * sizeof(uint2), &cand))) return rc;
+    }
+    mm_set_error("candidate list did not converge");
+    return MM_EDEVICE;
+}
+
+int mm_hyb_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t isz, int64_t isx,
+                 const float *flat, int64_t fsx, const void *W, int npsf, int tile_size, int zpad, int overlap,
+                 int blur_radius, float threshold, int delta, int delta_fit, float sigmaZ, float sigmaXY, int batch,
+                 float *out, uint32_t out_cap, uint32_t *count, void *stream) {
+    MM_REQUIRE(c && image && W && count, "null argument");
+    MM_REQUIRE(delta <= 5, "Delta must be an less than or equal to 5 due to MAX_KERNEL_POINTS");
+    MM_REQUIRE(delta >= 0 && delta_fit >= 0, "negative delta");
+    TileGeom g;
+    int rc = fill_geom(g, Z, X, Y, isz, isx, fsx, tile_size, zpad, overlap, npsf);
+    if (rc) return rc;
+    const int nt = ntiles_of(g);
+    if (batch <= 0) batch = nt;
+    std::lock_guard<std::mutex> lock(c->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    Small *sm;
+    if ((rc = small_get(c, &sm))) return rc;
+    *count = 0;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        size_t cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
+        if (cap < (1u << 20)) cap = 1u << 20;
+        void *cand;
+        if ((rc = ws_get(c, WS_CAND, cap * sizeof(uint2), &cand))) return rc;
+        cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
+        MM_CUDA_TRY(cudaMemsetAsync(&sm->overflow, 0, sizeof(unsigned), st));
+        for (int t0 = 0; t0 < nt; t0 += batch) {
+            TileGeom gb = g;
+            gb.t0 = t0;
+            gb.nt = (t0 + batch <= nt) ? batch : nt - t0;
+            if ((rc = run_tiles(c, gb, image, MM_DTYPE_U16, flat, (const float2 *)W, blur_radius, nullptr, nullptr,
+                                nullptr, 0, 0, st)))
+                return rc;
+            MaximaArgs a = {};
+            a.img = (const float *)c->ws[WS_RES];
+            a.isz = (long long)g.P * g.P; a.isx = g.P; a.ivol = (long long)g.Z * g.P * g.P;
+            a.Z = Z; a.X = 0; a.Y = 0; a.nvol = gb.nt;
+            a.tiles = &gb;
+            a.raw_kind = 2; a.chan = image; a.flat = flat;
+            a.th = threshold; a.delta = delta; a.delta_fit = delta_fit;
+            a.sigmaZ = sigmaZ; a.sigmaXY = sigmaXY;
+            a.div = 0.f; a.divp = nullptr; a.neg = 0; a.keep_filter = 1;
+            if ((rc = mm_launch_maxima_fit(a, (uint2 *)cand, (unsigned)cap, &sm->cand, out, out_cap, &sm->rows,
+                                           t0 == 0, st)))
+                return rc;
+            if ((rc = mm_launch_note_overflow(&sm->cand, (unsigned)cap, &sm->overflow, st))) return rc;
+        }
+        MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters, &sm->rows, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters + 2, &sm->overflow, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        MM_CUDA_TRY(cudaStreamSynchronize(st));
+        unsigned over = c->h_counters[2];
+        if (over == 0) {
+            *count = c->h_counters[0];
+            return *count > out_cap ? MM_EOVERFLOW : MM_OK;
+        }
+        if ((rc = ws_get(c, WS_CAND, (size_t)over * sizeof(uint2), &cand))) return rc;
+    }
+    mm_set_error("candidate list did not converge");
+    return MM_EDEVICE;
+}
+
+int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t isz, int64_t isx,
+                  const float *flat, int64_t fsx, const void *W, int npsf, int tile_size, int zpad, int overlap,
+                  int blur_radius, float threshold, int delta, int delta_fit, float sigmaZ, float sigmaXY,
+                  int batch, float *buffer, float *out_plus, uint32_t cap_plus, uint32_t *count_plus,
+                  float *out_minus, uint32_t cap_minus, uint32_t *count_minus, float *rms, void *stream) {
+    MM_REQUIRE(c && image && W && buffer && count_plus && count_minus, "null argument");
+    MM_REQUIRE(delta <= 5, "Delta must be an less than or equal to 5 due to MAX_KERNEL_POINTS");
+    MM_REQUIRE(delta >= 0 && delta_fit >= 0, "negative delta");
+    MM_REQUIRE(overlap >= 1, "stitching needs overlap >= 1");
+    TileGeom g;
+    int rc = fill_geom(g, Z, X, Y, isz, isx, fsx, tile_size, zpad, overlap, npsf);
+    if (rc) return rc;
+    const int nt = ntiles_of(g);
+    if (batch <= 0) batch = nt;
+    std::lock_guard<std::mutex> lock(c->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    Small *sm;
+    if ((rc = small_get(c, &sm))) return rc;
+    const long long N = (long long)Z * X * Y;
+    MM_CUDA_TRY(cudaMemsetAsync(buffer, 0, sizeof(float) * N, st));
+    for (int t0 = 0; t0 < nt; t0 += batch) {
+        TileGeom gb = g;
+        gb.t0 = t0;
+        gb.nt = (t0 + batch <= nt) ? batch : nt - t0;
+        if ((rc = run_tiles(c, gb, image, MM_DTYPE_U16, flat, (const float2 *)W, blur_radius, nullptr, nullptr, buffer,
+                            (long long)X * Y, Y, st)))
+            return rc;
+    }
+    if ((rc = mm_launch_sumsq(buffer, N, &sm->sumsq, st))) return rc;
+    if ((rc = mm_launch_rms_div(&sm->sumsq, N, &sm->div, st))) return rc;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        size_t cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
+        if (cap < (1u << 20)) cap = 1u << 20;
+        void *cand;
+        if ((rc = ws_get(c, WS_CAND, cap * sizeof(uint2), &cand))) return rc;
+        cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
+        MM_CUDA_TRY(cudaMemsetAsync(&sm->overflow, 0, sizeof(unsigned), st));
+        for (int sign = 0; sign < 2; ++sign) {
+            MaximaArgs a = {};
+            a.img = buffer; a.isz = (long long)X * Y; a.isx = Y; a.ivol = 0;
+            a.Z = Z; a.X = X; a.Y = Y; a.nvol = 1;
+            a.tiles = nullptr;
+            a.raw_kind = 1; a.raw = image; a.rsz = isz; a.rsx = isx; a.rvol = 0;
+            a.th = threshold; a.delta = delta; a.delta_fit = delta_fit;
+            a.sigmaZ = sigmaZ; a.sigmaXY = sigmaXY;
+            a.div = 0.f; a.divp = &sm->div; a.neg = sign; a.keep_filter = 0;
+            float *o = sign ? out_minus : out_plus;
+            unsigned oc = sign ? cap_minus : cap_plus;
+            if ((rc = mm_launch_maxima_fit(a, (uint2 *)cand, (unsigned)cap, &sm->cand, o, oc, nullptr, 0, st)))
+                return rc;
+            unsigned *dst = sign ? &sm->rows2 : &sm->rows;
+            MM_CUDA_TRY(cudaMemcpyAsync(dst, &sm->cand, sizeof(unsigned), cudaMemcpyDeviceToDevice, st));
+            if ((rc = mm_launch_note_overflow(&sm->cand, (unsigned)cap, &sm->overflow, st))) return rc;
+        }
+        MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters, &sm->rows, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        float hdiv = 0.f;
+        MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters + 4, &sm->div, sizeof(float), cudaMemcpyDeviceToHost, st));
+        MM_CUDA_TRY(cudaStreamSynchronize(st));
+        memcpy(&hdiv, c->h_counters + 4, sizeof(float));
+        if (rms) *rms = hdiv;
+        if (c->h_counters[2] == 0) {
+            *count_plus = c->h_counters[0];
+            *count_minus = c->h_counters[1];
+            return (*count_plus > cap_plus || *count_minus > cap_minus) ? MM_EOVERFLOW : MM_OK;
+        }
+        if ((rc = ws_get(c, WS_CAND, (size_t)c->h_counters[2] * sizeof(uint2), &cand))) return rc;
+    }
+    mm_set_error("candidate list did not converge");
+    return MM_EDEVICE;
+}
+
+}  // extern "C"
+
+extern "C" int mm_tile_geometry(int Z, int X, int Y, int tile_size, int zpad, int overlap, int npsf, int tile,
+                                int32_t *desc, int32_t *map_z, int32_t *map_x, int32_t *map_y) {
+    TileGeom g;
+    int rc = fill_geom(g, Z, X, Y, 0, 0, 0, tile_size, zpad, overlap, npsf);
+    if (rc) return rc;
+    const int nt = ntiles_of(g);
+    if (tile < 0) return nt;  // query: number of tiles
+    MM_REQUIRE(tile < nt, "tile %d outside the %d tiles of the channel", tile, nt);
+    TileDesc d = mm_tile_desc(g, tile);
+    if (desc) {
+        int32_t v[13] = {d.x, d.y, d.x0, d.y0, d.xd, d.yd, d.xs, d.ys, d.xend, d.yend, d.psf, g.P, g.Zp};
+        memcpy(desc, v, sizeof(v));
+    }
+    if (map_z)
+        for (int j = 0; j < g.Zp; ++j) map_z[j] = mm_map_z(j, g.Z, g.zpad, g.Zp);
+    if (map_x)
+        for (int j = 0; j < g.P; ++j) map_x[j] = mm_map_xy(j, d.x == 0, d.xd, g.P, g.ov);
+    if (map_y)
+        for (int j = 0; j < g.P; ++j) map_y[j] = mm_map_xy(j, d.y == 0, d.yd, g.P, g.ov);
+    return MM_OK;
+}
+
+extern "C" int mm_fft_c2c(void *data, int n, int nlines, int inverse, void *stream) {
+    MM_REQUIRE(data && n >= 1 && nlines >= 1, "bad FFT arguments");
+    return mm_launch_cols((float2 *)data, n, nlines, nlines, 0, 1, inverse != 0, (cudaStream_t)stream);
+}

@@ -1,0 +1,130 @@
+// Tile geometry shared by the deconvolution kernels and their host launchers.
+#pragma once
+#include "fft.cuh"
+
+// One launch works on tiles [t0, t0 + nt) of a channel's tile grid
+// (deconvolver.py:186-206: origins x-major, step tile_size).
+struct TileGeom {
+    int Z, X, Y;          // channel shape (deconvolver.py:178)
+    long long isz, isx;   // u16 image strides in elements (y stride 1)
+    long long fsx;        // flat-field row stride (y stride 1)
+    int ts, ov, zpad;     // tile_size, overlap, zpad
+    int P, H, Zp;         // padded tile edge, half spectrum length, padded depth
+    int ny;               // tiles along y
+    int t0, nt;           // first tile and tile count of this launch
+    int npsf;             // number of Wiener spectra (1 = shared)
+};
+
+struct TileDesc {
+    int x, y;        // tile origin
+    int x0, y0;      // first input row / column (max(x - ov, 0))
+    int xd, yd;      // input extent
+    int xs, ys;      // placement offset inside the padded tile (ov on the first row/col)
+    int xend, yend;  // yielded extent (deconvolver.py:120-144)
+    int psf;         // spectrum index
+};
+
+__device__ __host__ inline TileDesc mm_tile_desc(const TileGeom &g, int ti) {
+    TileDesc d;
+    int ix = ti / g.ny, iy = ti % g.ny;
+    d.x = ix * g.ts;
+    d.y = iy * g.ts;
+    d.x0 = d.x - g.ov > 0 ? d.x - g.ov : 0;
+    d.y0 = d.y - g.ov > 0 ? d.y - g.ov : 0;
+    int x1 = d.x + g.ts + g.ov < g.X ? d.x + g.ts + g.ov : g.X;
+    int y1 = d.y + g.ts + g.ov < g.Y ? d.y + g.ts + g.ov : g.Y;
+    d.xd = x1 - d.x0;
+    d.yd = y1 - d.y0;
+    d.xs = d.x == 0 ? g.ov : 0;
+    d.ys = d.y == 0 ? g.ov : 0;
+    d.xend = d.xd + ((d.x == 0 || d.xd < g.P) ? g.ov : 0);
+    d.yend = d.yd + ((d.y == 0 || d.yd < g.P) ? g.ov : 0);
+    d.psf = g.npsf == 1 ? 0 : ti;
+    return d;
+}
+
+// Padded index -> source index inside the tile, or -1 for a zero.  Restates
+// the placement and the reflect calls of deconvolver.py:123-148 (fill.py
+// mirror semantics) as a per-axis gather: every mirror copies whole
+// hyperplanes, so the padded tile is tile[mz[z], mx[x], my[y]] (zero where any
+// index is -1).
+__device__ __host__ inline int mm_map_xy(int j, bool first, int d, int P, int ov) {
+    if (first) {  // placed at ov, reflect 'in' about ov (deconvolver.py:132-134)
+        int q = j;
+        if (j < ov) {
+            int src = 2 * ov - j;
+            if (src < P) q = src;
+        }
+        return (q >= ov && q < ov + d) ? q - ov : -1;
+    }
+    if (d < P) {  // placed at 0, reflect 'out' about d-1 (deconvolver.py:135-137)
+        if (j < d) return j;
+        int src = 2 * (d - 1) - j;
+        return src >= 0 ? src : -1;
+    }
+    return j;
+}
+
+__device__ __host__ inline int mm_map_z0(int q, int Z, int zpad) {
+    return (q >= zpad && q < zpad + Z) ? q - zpad : -1;
+}
+
+// z: placed at zpad; reflect 'in' about zpad, then 'out' about zpad+Z-1
+// (deconvolver.py:145-148).
+__device__ __host__ inline int mm_map_z(int j, int Z, int zpad, int Zp) {
+    int i2 = zpad + Z - 1;
+    int q = j;
+    if (j > i2) {
+        int src = 2 * i2 - j;
+        if (src >= 0) q = src;
+    }
+    if (q < zpad) {
+        int src = 2 * zpad - q;
+        if (src < Zp) return mm_map_z0(src, Z, zpad);
+    }
+    return mm_map_z0(q, Z, zpad);
+}
+
+// host launchers (deconv.cu)
+int mm_launch_rows_fwd_img(const TileGeom &g, const void *img, int dtype, const float *flat, float2 *S,
+                           cudaStream_t st);
+int mm_launch_rows_fwd_f32(const float *vol, int nrows, int P, float2 *S, cudaStream_t st);
+int mm_launch_cols(float2 *S, int n, long long se, int nlines, long long plane_stride, int nplanes,
+                   bool inv, cudaStream_t st);
+int mm_launch_zpass(const TileGeom &g, float2 *S, const float2 *W, long long wstride, cudaStream_t st);
+int mm_launch_zfwd(float2 *S, int Zp, int plane, cudaStream_t st);
+int mm_launch_rows_inv(const float2 *S, int nrows, int P, int H, float *out, cudaStream_t st);
+int mm_launch_blur_y(const float *in, float *out, int nrows, int P, int delta, cudaStream_t st);
+int mm_launch_blur_x_sub(const TileGeom &g, const float *res, const float *tmp, int delta,
+                         float *res_out, float *stitch, long long osz, long long osx, cudaStream_t st);
+int mm_launch_make_raw(const TileGeom &g, const void *img, int dtype, const float *flat, float *raw,
+                       cudaStream_t st);
+
+// maxima + fit (maxima.cu)
+struct MaximaArgs {
+    const float *img;
+    long long isz, isx, ivol;   // image strides (y stride 1), per-volume stride
+    int Z, X, Y, nvol;          // dense dims (X, Y ignored in tile mode)
+    const TileGeom *tiles;      // tile mode: dims and raw view from the tile geometry
+    int raw_kind;               // 0 f32 array, 1 u16 array, 2 tile raw view (u16 chan), 3 (f32 chan)
+    const void *raw;
+    long long rsz, rsx, rvol;
+    const void *chan;
+    const float *flat;
+    float th;
+    int delta, delta_fit;
+    float sigmaZ, sigmaXY;
+    float div;                  // 0: none, else v -> v / div
+    const float *divp;          // device divisor, overrides div when set
+    int neg;                    // v -> -v after the division
+    int keep_filter;            // tile mode: keep-filter + origin offset, rows appended
+};
+int mm_maxima_ensure_init(cudaStream_t st);
+int mm_launch_maxima_fit(const MaximaArgs &a, uint2 *cand, unsigned cand_cap, unsigned *ncand, float *out,
+                         unsigned out_cap, unsigned *out_count, int zero_out_count, cudaStream_t st);
+int mm_launch_note_overflow(const unsigned *ncand, unsigned cap, unsigned *overflow, cudaStream_t st);
+int mm_launch_sumsq(const float *x, long long n, double *out, cudaStream_t st);
+int mm_launch_rms_div(const double *sumsq, long long n, float *div, cudaStream_t st);
+int mm_wiener_build_impl(const float *psf, int pz, int px, int py, int tile_height, int tile_size, int zpad,
+                         int overlap, float beta, float2 *W, float *vol, float2 *S, double *dsum,
+                         cudaStream_t st);

@@ -1,0 +1,87 @@
+// Host side of the FFT engine: factorisation and twiddle tables, cached per
+// (device, length) for the life of the process.
+#include <math.h>
+#include <stdlib.h>
+
+#include <map>
+#include <mutex>
+#include <utility>
+#include <vector>
+
+#include "fft.cuh"
+
+namespace {
+std::mutex g_mu;
+std::map<std::pair<int, int>, FftPlan> g_plans;
+
+void factor(int n, std::vector<int> &generic, std::vector<int> &small) {
+    while (n % 4 == 0) { small.push_back(4); n /= 4; }
+    while (n % 2 == 0) { small.push_back(2); n /= 2; }
+    for (int p : {3, 5, 7})
+        while (n % p == 0) { small.push_back(p); n /= p; }
+    for (int p = 11; (long)p * p <= n; p += 2)
+        while (n % p == 0) { generic.push_back(p); n /= p; }
+    if (n > 1) generic.push_back(n);
+}
+}  // namespace
+
+int mm_fft_plan_get(int n, FftPlan *out) {
+    if (n < 1 || n > MM_FFT_MAXN) {
+        mm_set_error("FFT length %d outside [1, %d]", n, MM_FFT_MAXN);
+        return MM_EINVAL;
+    }
+    int dev = 0;
+    MM_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(g_mu);
+    auto it = g_plans.find({dev, n});
+    if (it != g_plans.end()) {
+        *out = it->second;
+        return MM_OK;
+    }
+    std::vector<int> generic, small;
+    factor(n, generic, small);
+    FftPlan P = {};
+    P.n = n;
+    std::vector<float2> tab;
+    int Ns = 1;
+    // generic (large prime) stages first: at Ns == 1 they need no twiddles
+    for (int R : generic) {
+        P.rad[P.nst] = R;
+        P.ns[P.nst] = Ns;
+        P.ptab[P.nst] = (int)tab.size();
+        for (int m = 0; m < R; ++m) {
+            double a = -2.0 * M_PI * (double)m / (double)R;
+            tab.push_back(make_float2((float)cos(a), (float)sin(a)));
+        }
+        Ns *= R;
+        P.nst++;
+    }
+    for (int R : small) {
+        P.rad[P.nst] = R;
+        P.ns[P.nst] = Ns;
+        P.ptab[P.nst] = -1;
+        Ns *= R;
+        P.nst++;
+    }
+    if (P.nst > MM_FFT_MAXST) {
+        mm_set_error("FFT length %d needs too many stages", n);
+        return MM_EINVAL;
+    }
+    std::vector<float2> tw(n);
+    for (int m = 0; m < n; ++m) {
+        double a = -2.0 * M_PI * (double)m / (double)n;
+        tw[m] = make_float2((float)cos(a), (float)sin(a));
+    }
+    if (tab.empty()) tab.push_back(make_float2(1.f, 0.f));
+    P.ntab = (int)tab.size();
+    float2 *d_tw = nullptr, *d_tab = nullptr;
+    MM_CUDA_TRY(cudaMalloc(&d_tw, sizeof(float2) * n));
+    MM_CUDA_TRY(cudaMalloc(&d_tab, sizeof(float2) * tab.size()));
+    MM_CUDA_TRY(cudaMemcpy(d_tw, tw.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+    MM_CUDA_TRY(cudaMemcpy(d_tab, tab.data(), sizeof(float2) * tab.size(), cudaMemcpyHostToDevice));
+    P.tw = d_tw;
+    P.tab = d_tab;
+    g_plans[{dev, n}] = P;
+    *out = P;
+    return MM_OK;
+}

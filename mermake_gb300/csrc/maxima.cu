@@ -1,0 +1,322 @@
+// 3-D local maxima and per-spot fit (restating mermake/maxima.cu and
+// mermake/maxima.py:17-98, plus the hyb keep-filter of mermake/__main__.py:254-261).
+//
+// k_maxima   one thread per voxel: v > threshold (strict) and no neighbour in
+//            the sphere 0 < |d|^2 <= delta^2 is larger (ties keep both);
+//            neighbours reflect once about the first/last sample
+//            (maxima.cu:19, 25-62).  A neighbour that is still outside after
+//            the reflection (a dimension shorter than delta) is skipped; the
+//            reference kernel reads out of bounds there.  Maxima are compacted
+//            with one atomic per warp (ballot + popc) into a candidate list;
+//            the count/collect double pass of the reference becomes one pass.
+//            The image may be read through v -> v / div (IEEE, round to nearest)
+//            -> -v, which reproduces the DAPI normalisation (v / rms, then
+//            negated for minima, __main__.py:219-225) bit for bit without
+//            writing the normalised volume.
+// k_fit      one warp per spot: gathers the sphere |d|^2 <= delta_fit^2 in the
+//            reference's (dz, dx, dy) order (first 600 in-range samples,
+//            maxima.cu:148, 190-232) and forms every output of
+//            delta_fit_cross_corr from double-precision moment sums:
+//              bg = min v;  centroid = sum (c+d)(v-bg) / sum (v-bg)  (fallback c);
+//              hn = cov(v, G) / (std'(v) std(G));  a = cov(raw, G) / (std'(raw) std(G))
+//            with std' = std, or 1 where std == 0 (maxima.cu:233-341).  std(G) == 0
+//            (delta_fit = 0) gives NaN for hn and a, as in the reference.
+//            In tile mode the row is kept only if overlap <= xc < xend-overlap and
+//            the same for yc, then shifted by the tile origin (__main__.py:256-260).
+#include "deconv.cuh"
+
+namespace {
+
+constexpr int kMaxDelta = 5;
+constexpr int kSphereCap = 515;
+__device__ char4 g_sphere[kMaxDelta + 1][kSphereCap];  // neighbour offsets, nearest first
+__device__ int g_sphere_n[kMaxDelta + 1];
+__device__ int g_sphere_ready;
+
+__global__ void k_init_sphere() {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int d = 0; d <= kMaxDelta; ++d) {
+        int n = 0;
+        for (int r2 = 1; r2 <= d * d; ++r2)
+            for (int dz = -d; dz <= d; ++dz)
+                for (int dx = -d; dx <= d; ++dx)
+                    for (int dy = -d; dy <= d; ++dy)
+                        if (dz * dz + dx * dx + dy * dy == r2) g_sphere[d][n++] = make_char4(dz, dx, dy, 0);
+        g_sphere_n[d] = n;
+    }
+    g_sphere_ready = 1;
+}
+
+struct Xform {
+    float div;           // 0: none
+    int neg;
+    const float *divp;   // device divisor (overrides div when set)
+};
+__device__ __forceinline__ Xform xf_resolve(Xform t) {
+    if (t.divp) t.div = *t.divp;
+    return t;
+}
+__device__ __forceinline__ float xf(float v, Xform t) {
+    if (t.div != 0.f) v = __fdiv_rn(v, t.div);
+    return t.neg ? -v : v;
+}
+
+__device__ __forceinline__ int refl(int i, int n) { return i < 0 ? -i : (i >= n ? 2 * n - i - 2 : i); }
+
+// A set of volumes: either one dense volume, or the yielded views of a tile batch.
+struct Vols {
+    const float *img;
+    long long isz, isx, ivol;  // strides (y stride 1) and per-volume stride
+    int Z, X, Y;               // single-volume dims
+    int tiles;                 // 1: dims and raw from the tile geometry
+    TileGeom g;
+    int raw_kind;              // 0: f32 array, 1: u16 array, 2/3: tile raw view of a u16/f32 channel
+    const void *raw;
+    long long rsz, rsx, rvol;
+    const void *chan;
+    const float *flat;
+};
+
+__device__ __forceinline__ void vol_dims(const Vols &V, int vi, int &X, int &Y, TileDesc &d) {
+    if (V.tiles) {
+        d = mm_tile_desc(V.g, V.g.t0 + vi);
+        X = d.xend;
+        Y = d.yend;
+    } else {
+        X = V.X;
+        Y = V.Y;
+    }
+}
+
+__device__ __forceinline__ float raw_at(const Vols &V, int vi, const TileDesc &d, int z, int x, int y) {
+    if (V.raw_kind == 0)
+        return static_cast<const float *>(V.raw)[vi * V.rvol + z * V.rsz + x * V.rsx + y];
+    if (V.raw_kind == 1)
+        return (float)static_cast<const uint16_t *>(V.raw)[vi * V.rvol + z * V.rsz + x * V.rsx + y];
+    // tile_pad[zpad + z, x, y] after the flat is multiplied back (deconvolver.py:165-170)
+    const TileGeom &g = V.g;
+    int sx = mm_map_xy(x, d.x == 0, d.xd, g.P, g.ov);
+    int sy = mm_map_xy(y, d.y == 0, d.yd, g.P, g.ov);
+    if (sx < 0 || sy < 0) return 0.f;
+    int gx = d.x0 + sx, gy = d.y0 + sy;
+    const long long ci = z * g.isz + gx * g.isx + gy;
+    float v = V.raw_kind == 2 ? (float)static_cast<const uint16_t *>(V.chan)[ci] : static_cast<const float *>(V.chan)[ci];
+    if (V.flat) {
+        float f = V.flat[gx * g.fsx + gy];
+        v = __fdiv_rn(v, f);
+        if (x >= d.xs && x < d.xs + d.xd && y >= d.ys && y < d.ys + d.yd) v = __fmul_rn(v, f);
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(256)
+k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigned cap,
+         unsigned *__restrict__ count) {
+    t = xf_resolve(t);
+    const int vi = blockIdx.y;
+    int X, Y;
+    TileDesc d;
+    vol_dims(V, vi, X, Y, d);
+    const int Z = V.Z;
+    const long long total = (long long)Z * X * Y;
+    const float *img = V.img + vi * V.ivol;
+    const int nn = g_sphere_n[delta];
+    const char4 *sph = g_sphere[delta];
+    const unsigned lane = threadIdx.x & 31;
+    for (long long base = (long long)blockIdx.x * blockDim.x; base < total; base += (long long)gridDim.x * blockDim.x) {
+        long long i = base + threadIdx.x;
+        bool is_max = false;
+        int z = 0, x = 0, y = 0;
+        if (i < total) {
+            z = (int)(i / ((long long)X * Y));
+            x = (int)((i / Y) % X);
+            y = (int)(i % Y);
+            float v = xf(img[z * V.isz + x * V.isx + y], t);
+            if (!(v <= th)) {  // maxima.cu:19 (a NaN threshold admits every voxel)
+                is_max = true;
+                for (int k = 0; k < nn; ++k) {
+                    char4 o = sph[k];
+                    int nz = refl(z + o.x, Z), nx = refl(x + o.y, X), ny = refl(y + o.z, Y);
+                    if (nz < 0 || nz >= Z || nx < 0 || nx >= X || ny < 0 || ny >= Y) continue;
+                    if (v < xf(img[nz * V.isz + nx * V.isx + ny], t)) {
+                        is_max = false;
+                        break;
+                    }
+                }
+            }
+        }
+        unsigned m = __ballot_sync(0xffffffffu, is_max);
+        if (m) {
+            unsigned slot = 0;
+            int leader = __ffs(m) - 1;
+            if ((int)lane == leader) slot = atomicAdd(count, __popc(m));
+            slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(m & ((1u << lane) - 1));
+            if (is_max && slot < cap)
+                cand[slot] = make_uint2((unsigned)z | ((unsigned)x << 16), (unsigned)y | ((unsigned)vi << 16));
+        }
+    }
+}
+
+__device__ __forceinline__ double wsum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(256)
+k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand, unsigned cap, int delta_fit,
+      float sigmaZ, float sigmaXY, Xform t, float *__restrict__ out, unsigned out_cap,
+      unsigned *__restrict__ out_count, int keep_filter) {
+    t = xf_resolve(t);
+    const unsigned lane = threadIdx.x & 31;
+    const unsigned nc = min(*ncand, cap);
+    const int side = 2 * delta_fit + 1;
+    const int cube = side * side * side;
+    const int df2 = delta_fit * delta_fit;
+    for (unsigned s = (blockIdx.x * blockDim.x + threadIdx.x) / 32; s < nc; s += gridDim.x * blockDim.x / 32) {
+        uint2 c = cand[s];
+        const int z0 = c.x & 0xffff, x0 = c.x >> 16, y0 = c.y & 0xffff, vi = c.y >> 16;
+        int X, Y;
+        TileDesc d;
+        vol_dims(V, vi, X, Y, d);
+        const int Z = V.Z;
+        const float *img = V.img + vi * V.ivol;
+        double n = 0, sv = 0, svv = 0, sg = 0, sgg = 0, svg = 0, sr = 0, srr = 0, srg = 0;
+        double sdz = 0, sdx = 0, sdy = 0, svdz = 0, svdx = 0, svdy = 0;
+        float vmin = 1e20f;
+        int taken = 0;  // in-range samples before this chunk (cap 600, maxima.cu:194)
+        for (int c0 = 0; c0 < cube && taken < 600; c0 += 32) {
+            int ci = c0 + (int)lane;
+            int dz = 0, dx = 0, dy = 0;
+            bool ok = false;
+            int zz = 0, xx = 0, yy = 0;
+            if (ci < cube) {
+                dz = ci / (side * side) - delta_fit;
+                dx = (ci / side) % side - delta_fit;
+                dy = ci % side - delta_fit;
+                if (dz * dz + dx * dx + dy * dy <= df2) {
+                    zz = refl(z0 + dz, Z);
+                    xx = refl(x0 + dx, X);
+                    yy = refl(y0 + dy, Y);
+                    ok = zz >= 0 && zz < Z && xx >= 0 && xx < X && yy >= 0 && yy < Y;
+                }
+            }
+            unsigned m = __ballot_sync(0xffffffffu, ok);
+            int rank = taken + __popc(m & ((1u << lane) - 1));
+            taken += __popc(m);
+            if (ok && rank < 600) {
+                float v = xf(img[zz * V.isz + xx * V.isx + yy], t);
+                float r = raw_at(V, vi, d, zz, xx, yy);
+                float g = expf(-(dz * dz / (2 * sigmaZ * sigmaZ) + dx * dx / (2 * sigmaXY * sigmaXY) +
+                                 dy * dy / (2 * sigmaXY * sigmaXY)));
+                double dv = v, dr = r, dg = g;
+                n += 1;
+                sv += dv; svv += dv * dv;
+                sg += dg; sgg += dg * dg; svg += dv * dg;
+                sr += dr; srr += dr * dr; srg += dr * dg;
+                sdz += dz; sdx += dx; sdy += dy;
+                svdz += dv * dz; svdx += dv * dx; svdy += dv * dy;
+                vmin = fminf(vmin, v);
+            }
+        }
+        n = wsum(n); sv = wsum(sv); svv = wsum(svv); sg = wsum(sg); sgg = wsum(sgg); svg = wsum(svg);
+        sr = wsum(sr); srr = wsum(srr); srg = wsum(srg);
+        sdz = wsum(sdz); sdx = wsum(sdx); sdy = wsum(sdy);
+        svdz = wsum(svdz); svdx = wsum(svdx); svdy = wsum(svdy);
+        for (int o = 16; o > 0; o >>= 1) vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
+        if (lane != 0 || n == 0) continue;
+        const double bg = vmin;
+        const double mg = sg / n, mv = sv / n, mr = sr / n;
+        const double varg = fmax(sgg / n - mg * mg, 0.0);
+        const double varv = fmax(svv / n - mv * mv, 0.0);
+        const double varr = fmax(srr / n - mr * mr, 0.0);
+        const double stdg = sqrt(varg);
+        double stdv = sqrt(varv), stdr = sqrt(varr);
+        if (!(stdv > 0)) stdv = 1.0;
+        if (!(stdr > 0)) stdr = 1.0;
+        const double hn = (svg / n - mv * mg) / (stdv * stdg);
+        const double a = (srg / n - mr * mg) / (stdr * stdg);
+        // sum (c + d)(v - bg) = c * sum(v - bg) + sum d v - bg sum d
+        const double sw = sv - n * bg;
+        double zc, xc, yc;
+        if (sw > 0) {
+            zc = (z0 * sw + svdz - bg * sdz) / sw;
+            xc = (x0 * sw + svdx - bg * sdx) / sw;
+            yc = (y0 * sw + svdy - bg * sdy) / sw;
+        } else {
+            zc = z0; xc = x0; yc = y0;
+        }
+        float row[8];
+        row[0] = (float)zc; row[1] = (float)xc; row[2] = (float)yc; row[3] = vmin;
+        row[4] = (float)a;
+        row[5] = raw_at(V, vi, d, z0, x0, y0);
+        row[6] = (float)hn;
+        row[7] = xf(img[z0 * V.isz + x0 * V.isx + y0], t);
+        unsigned o;
+        if (keep_filter) {
+            const int ov = V.g.ov;
+            if (!(row[1] >= ov && row[2] >= ov && row[1] < (float)(X - ov) && row[2] < (float)(Y - ov))) continue;
+            row[1] += (float)(d.x - ov);
+            row[2] += (float)(d.y - ov);
+            o = atomicAdd(out_count, 1u);
+        } else {
+            o = s;
+        }
+        if (o < out_cap)
+            for (int k = 0; k < 8; ++k) out[(long long)o * 8 + k] = row[k];
+    }
+}
+
+__global__ void k_note_overflow(const unsigned *__restrict__ ncand, unsigned cap, unsigned *__restrict__ overflow) {
+    unsigned n = *ncand;
+    if (n > cap) atomicMax(overflow, n);
+}
+
+}  // namespace
+
+int mm_launch_note_overflow(const unsigned *ncand, unsigned cap, unsigned *overflow, cudaStream_t st) {
+    k_note_overflow<<<1, 1, 0, st>>>(ncand, cap, overflow);
+    MM_CHECK_LAUNCH();
+    return MM_OK;
+}
+
+int mm_maxima_ensure_init(cudaStream_t st) {
+    static int done_dev[64] = {0};
+    int dev = 0;
+    MM_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 64 && done_dev[dev]) return MM_OK;
+    k_init_sphere<<<1, 1, 0, st>>>();
+    MM_CHECK_LAUNCH();
+    MM_CUDA_TRY(cudaStreamSynchronize(st));
+    if (dev < 64) done_dev[dev] = 1;
+    return MM_OK;
+}
+
+
+
+// Launches maxima + fit.  cand/ncand: scratch list and its device counter;
+// out/out_count: rows and their device counter (keep mode) -- counters are
+// zeroed here.
+int mm_launch_maxima_fit(const MaximaArgs &a, uint2 *cand, unsigned cand_cap, unsigned *ncand, float *out,
+                         unsigned out_cap, unsigned *out_count, int zero_out_count, cudaStream_t st) {
+    Vols V = {};
+    V.img = a.img; V.isz = a.isz; V.isx = a.isx; V.ivol = a.ivol;
+    V.Z = a.Z; V.X = a.X; V.Y = a.Y;
+    V.tiles = a.tiles != nullptr;
+    if (a.tiles) V.g = *a.tiles;
+    V.raw_kind = a.raw_kind; V.raw = a.raw; V.rsz = a.rsz; V.rsx = a.rsx; V.rvol = a.rvol;
+    V.chan = a.chan; V.flat = a.flat;
+    Xform t = {a.div, a.neg, a.divp};
+    MM_CUDA_TRY(cudaMemsetAsync(ncand, 0, sizeof(unsigned), st));
+    if (out_count && zero_out_count) MM_CUDA_TRY(cudaMemsetAsync(out_count, 0, sizeof(unsigned), st));
+    long long per = (long long)a.Z * (a.tiles ? (long long)a.tiles->P * a.tiles->P : (long long)a.X * a.Y);
+    int gx = (int)((per + 255) / 256);
+    if (gx > 152 * 16) gx = 152 * 16;
+    if (gx < 1) gx = 1;
+    dim3 grid(gx, a.nvol);
+    k_maxima<<<grid, 256, 0, st>>>(V, a.th, a.delta, t, cand, cand_cap, ncand);
+    MM_CHECK_LAUNCH();
+    k_fit<<<152 * 8, 256, 0, st>>>(V, cand, ncand, cand_cap, a.delta_fit, a.sigmaZ, a.sigmaXY, t, out, out_cap,
+                                   out_count, a.keep_filter);
+    MM_CHECK_LAUNCH();
+    return MM_OK;
+}

@@ -1,0 +1,51 @@
+// Shared definitions for the mermake_gb300 CUDA library (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/mermake_gb300.h"
+
+#define MM_CUDA_TRY(expr)                                                   \
+    do {                                                                    \
+        cudaError_t _e = (expr);                                            \
+        if (_e != cudaSuccess) {                                            \
+            mm_set_error("%s:%d %s: %s", __FILE__, __LINE__, #expr,          \
+                         cudaGetErrorString(_e));                           \
+            return MM_EDEVICE;                                              \
+        }                                                                   \
+    } while (0)
+
+#define MM_CHECK_LAUNCH()                                                   \
+    do {                                                                    \
+        cudaError_t _e = cudaGetLastError();                                \
+        if (_e != cudaSuccess) {                                            \
+            mm_set_error("%s:%d launch: %s", __FILE__, __LINE__,             \
+                         cudaGetErrorString(_e));                           \
+            return MM_EDEVICE;                                              \
+        }                                                                   \
+    } while (0)
+
+#define MM_REQUIRE(cond, ...)                                               \
+    do {                                                                    \
+        if (!(cond)) {                                                      \
+            mm_set_error(__VA_ARGS__);                                      \
+            return MM_EINVAL;                                               \
+        }                                                                   \
+    } while (0)
+
+// Records a message for mm_last_error() (thread-local).
+void mm_set_error(const char *fmt, ...);
+
+static inline int mm_cdiv(long a, long b) { return (int)((a + b - 1) / b); }
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+    return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }

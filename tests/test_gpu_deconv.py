@@ -1,0 +1,133 @@
+"""GPU parity of the Wiener spectrum and the tiled deconvolution against the
+FP64 oracle and the reference's golden float16 slices."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import deconv as od
+from tests.test_oracle import f16_tolerance, load_tile
+
+pytestmark = pytest.mark.gpu
+
+# voxels: |gpu - oracle| <= REL * max|oracle| (float32 FFTs against float64)
+REL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def dc():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from mermake_gb300 import deconvolver
+    return deconvolver
+
+
+def u16(a):
+    return torch.from_numpy(np.asarray(a).astype(np.int32)).to(torch.uint16).cuda()
+
+
+def test_wiener_spectrum_matches_oracle(dc, golden_dir):
+    psf = np.load(os.path.join(golden_dir, "psf_750.npz"))["psf"]
+    Z, ts, zpad, ov, beta = 35, 300, 35, 89, 1e-3
+    d = dc.Deconvolver(psf, (Z, 1200, 1200), tile_size=ts, zpad=zpad, overlap=ov, beta=beta)
+    got = d.psf_fft[0].cpu().numpy().astype(np.complex128) * (d.Zp * d.P * d.P)
+    want = od.wiener_half(psf, Z, ts, zpad, ov, beta)
+    err = np.abs(got - want).max() / np.abs(want).max()
+    assert err < 1e-5, err
+
+
+@pytest.mark.parametrize("k", [0, 1, 2])
+def test_deconv_tiles_match_golden_and_oracle(dc, golden_dir, k):
+    """test_deconvolver.py:422-434 on the stored tiles: Deconvolver.apply of the
+    tile's input crop, against the reference's float16 goldens and the FP64 oracle."""
+    t = load_tile(golden_dir, k)
+    psf = np.load(os.path.join(golden_dir, "psf_750.npz"))["psf"]
+    Z, ts, ov = t["Z"], t["ts"], t["ov"]
+    x, y, x0, x1, y0, y1 = t["box"]
+    img = u16(t["img"])
+    d = dc.Deconvolver(psf, img.shape, tile_size=ts, zpad=Z, overlap=ov, beta=1e-3)
+    tiles = d.tile_boxes(img.shape)
+    ti = tiles.index(tuple(t["box"]))
+    res = torch.empty((1, Z, d.P, d.P), device="cuda")
+    d._call(img, dc.MM_DTYPE_U16, None, ti, 1, None, res_out=res)
+    xend, yend = d._extent(t["box"])
+    got = res[0, :, :xend, :yend].cpu().numpy().astype(np.float64)
+    W = od.wiener_half(psf, Z, ts, Z, ov, 1e-3)
+    want, _ = od.deconv_tile(t["img"], None, t["box"], W, ts, Z, ov)
+    err = np.abs(got - want).max() / np.abs(want).max()
+    print("tile", k, "max |gpu - oracle| / max|oracle| =", err)
+    assert err < REL
+    cen = got[:, ov:-ov, ov:-ov][:: t["zs"]]
+    gold = t["gold"]
+    cen = cen[:, : gold.shape[1], : gold.shape[2]]
+    diff = np.abs(cen - gold.astype(np.float64))
+    # float16 goldens: one f16 spacing + 1e-5 of the range, as for the oracle
+    assert np.mean(diff <= f16_tolerance(gold)) > 0.999
+    assert diff.max() <= 2 * f16_tolerance(gold).max()
+
+
+def small_case(seed=0, Z=10, X=50, Y=50, flat=True):
+    rng = np.random.default_rng(seed)
+    img = rng.integers(100, 5000, (Z, X, Y)).astype(np.uint16)
+    psf = np.zeros((5, 5, 5), np.float32)
+    psf[2, 2, 2] = 1.0
+    psf[1:4, 1:4, 1:4] += 0.1 * rng.random((3, 3, 3)).astype(np.float32)
+    fl = (0.8 + 0.2 * rng.random((X, Y))).astype(np.float32) if flat else None
+    return img, psf, fl
+
+
+@pytest.mark.parametrize("ts,zpad,ov,blur", [(30, 5, 5, None), (30, 5, 5, 8), (20, 3, 7, 5), (64, 9, 11, 30),
+                                             (17, 4, 3, None)])
+def test_tile_wise_matches_oracle(dc, ts, zpad, ov, blur):
+    """Every yielded tile and raw view of tile_wise (deconvolver.py:98-170)
+    with a flat field and optional blur subtraction."""
+    img, psf, fl = small_case(ts + zpad)
+    d = dc.Deconvolver(psf, img.shape, tile_size=ts, zpad=zpad, overlap=ov, beta=0.01)
+    o = od.Deconvolver(psf, img.shape, tile_size=ts, zpad=zpad, overlap=ov, beta=0.01)
+    n = 0
+    for (x, y, res, raw), (xo, yo, rres, rraw) in zip(d.tile_wise(u16(img), torch.from_numpy(fl).cuda(), blur),
+                                                      o.tile_wise(img, fl, blur)):
+        assert (x, y) == (xo, yo)
+        assert tuple(res.shape) == rres.shape == rraw.shape
+        g = res.cpu().numpy().astype(np.float64)
+        assert np.abs(g - rres).max() <= REL * np.abs(rres).max()
+        np.testing.assert_array_equal(raw.cpu().numpy(), rraw)
+        n += 1
+    assert n == len(od.tiles(img.shape, ts, ov))
+
+
+def test_apply_float_image_and_multi_psf(dc):
+    """float64 images (test_deconvolver.py uses cp.random.random) and a dict of
+    PSFs paired with tiles in order, truncated by zip (deconvolver.py:110-116)."""
+    rng = np.random.default_rng(4)
+    img = rng.random((10, 50, 50))
+    psf = np.zeros((5, 5, 5))
+    psf[2, 2, 2] = 1.0
+    psfs = {"a": psf, "b": psf * 0.9 + 0.01, "c": np.roll(psf, 1, axis=2)}
+    for p in (psf, psfs):
+        d = dc.Deconvolver(p, img.shape, tile_size=20, zpad=10, overlap=5, beta=0.001)
+        o = od.Deconvolver(p, img.shape, tile_size=20, zpad=10, overlap=5, beta=0.001)
+        got = d.apply(torch.from_numpy(img).cuda()).cpu().numpy()
+        want = o.apply(img.astype(np.float32))
+        ok = ~np.isnan(want)
+        assert np.abs(got[ok] - want[ok]).max() <= REL * np.abs(want[ok]).max()
+
+
+def test_full_deconv_signature(dc):
+    """test_deconvolver.py:436-470: shapes and intensity."""
+    img = torch.zeros((10, 50, 50), dtype=torch.float64, device="cuda")
+    img[5, 25, 25] = 100
+    psf = np.zeros((5, 5, 5))
+    psf[2, 2, 2] = 1.0
+    out = dc.full_deconv(img, psf, tile_size=30, overlap=5)
+    assert tuple(out.shape) == (10, 50, 50)
+    assert torch.isfinite(out).all()
+    assert abs(float(out.sum()) - 100) / 100 < 0.5
+
+
+def test_zpad_zero_is_rejected(dc):
+    img, psf, _ = small_case(flat=False)
+    with pytest.raises(ValueError, match="zpad"):
+        d = dc.Deconvolver(psf, img.shape, tile_size=30, zpad=0, overlap=5)
+        list(d.tile_wise(u16(img)))

@@ -1,0 +1,123 @@
+"""GPU parity of the per-FOV drivers: the batched hyb colour (mm_hyb_spots) and
+the DAPI block (mm_dapi_spots) against the plain per-tile loop of the same
+library (identical volumes, so identical maxima) and against the oracle."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import ckernels as ck
+from oracle import deconv as od
+from tests.test_gpu_kernels import assert_rows_close
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mm():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from mermake_gb300 import deconvolver, maxima, pipeline, synth
+    return dict(dc=deconvolver, mx=maxima, pl=pipeline, synth=synth)
+
+
+HYB = dict(tile_size=60, overlap=12, beta=1e-4, threshold=3600, blur_radius=10, delta=1, delta_fit=3,
+           sigmaZ=1, sigmaXY=1.5)
+
+
+def hyb_case(mm, seed=1, Z=12, X=170, Y=150):
+    img = mm["synth"].hyb_stack(Z, X, Y, 300, seed, gain=mm["synth"].flat_gain(X, Y))
+    flat = mm["synth"].flat_gain(X, Y)
+    psf = mm["synth"].gaussian_psf((9, 9, 9), 2.0, 1.3)
+    return img, flat, psf
+
+
+def plain_loop(mm, dec, img, flat, a):
+    """__main__.py:253-265 verbatim, on this library's tile_wise + find_local_maxima."""
+    out = []
+    ov = a["overlap"]
+    for x, y, tile, raw in dec.tile_wise(img, flat, **a):
+        Xh = mm["mx"].find_local_maxima(tile, raw=raw, **a)
+        keep = torch.all((Xh[:, 1:3] >= ov) & (Xh[:, 1:3] < torch.tensor([tile.shape[1] - ov, tile.shape[2] - ov],
+                                                                        device="cuda")), dim=-1)
+        if torch.any(keep):
+            Xh = Xh[keep]
+            Xh[:, 1] += x - ov
+            Xh[:, 2] += y - ov
+            out.append(Xh)
+    return torch.cat(out) if out else torch.zeros((0, 8), device="cuda")
+
+
+def test_hyb_batched_equals_plain_loop(mm):
+    img, flat, psf = hyb_case(mm)
+    Z = img.shape[0]
+    dec = mm["dc"].Deconvolver(psf, img.shape, zpad=Z - 1, **HYB)
+    dimg, dflat = img.cuda(), torch.from_numpy(flat).cuda()
+    want = ck.sort_rows(plain_loop(mm, dec, dimg, dflat, HYB).cpu().numpy())
+    for batch in (1, 4, 0):
+        got = ck.sort_rows(mm["pl"].hyb_spots(dec, dimg, dflat, batch=batch, **HYB).cpu().numpy())
+        assert len(want) > 20
+        np.testing.assert_array_equal(got, want)
+
+
+def test_hyb_spots_match_oracle_on_same_volumes(mm):
+    """The maxima set is bit-exact when both sides see the same deconvolved
+    tile; the fit agrees within tolerance."""
+    img, flat, psf = hyb_case(mm, seed=2)
+    Z = img.shape[0]
+    dec = mm["dc"].Deconvolver(psf, img.shape, zpad=Z - 1, **HYB)
+    dimg, dflat = img.cuda(), torch.from_numpy(flat).cuda()
+    for x, y, tile, raw in dec.tile_wise(dimg, dflat, **HYB):
+        t = tile.cpu().numpy()
+        r = raw.cpu().numpy()
+        got = ck.sort_rows(mm["mx"].find_local_maxima(tile, raw=raw, **HYB).cpu().numpy())
+        want = ck.sort_rows(ck.find_local_maxima(t, HYB["threshold"], 1, 3, r, 1, 1.5))
+        assert_rows_close(got, want)
+
+
+def test_hyb_end_to_end_against_oracle(mm):
+    """Full oracle path (FP64 deconvolution, C maxima/fit, keep/offset): the
+    maxima sets agree except at near-ties flipped by float32 FFT rounding."""
+    img, flat, psf = hyb_case(mm, seed=3)
+    Z = img.shape[0]
+    dec = mm["dc"].Deconvolver(psf, img.shape, zpad=Z - 1, **HYB)
+    got = ck.sort_rows(mm["pl"].hyb_spots(dec, img.cuda(), torch.from_numpy(flat).cuda(), **HYB).cpu().numpy())
+    o = od.Deconvolver(psf, img.shape, zpad=Z - 1, **HYB)
+    rows = []
+    ov = HYB["overlap"]
+    for x, y, res, raw in o.tile_wise(img.numpy(), flat, HYB["blur_radius"]):
+        Xh = ck.find_local_maxima(res.astype(np.float32), HYB["threshold"], 1, 3, raw, 1, 1.5)
+        k = np.all((Xh[:, 1:3] >= ov) & (Xh[:, 1:3] < [res.shape[1] - ov, res.shape[2] - ov]), axis=-1)
+        Xh = Xh[k]
+        Xh[:, 1] += x - ov
+        Xh[:, 2] += y - ov
+        rows.append(Xh)
+    want = ck.sort_rows(np.concatenate(rows))
+    gi = {tuple(np.round(r[:3], 2)) for r in got}
+    wi = {tuple(np.round(r[:3], 2)) for r in want}
+    assert len(want) > 20
+    assert len(gi & wi) >= 0.98 * max(len(gi), len(wi))
+
+
+DAPI = dict(tile_size=60, overlap=12, beta=0.01, threshold=3.0, blur_radius=20, delta=5, delta_fit=5,
+            sigmaZ=1, sigmaXY=1.5)
+
+
+def test_dapi_batched_equals_stepwise(mm):
+    """__main__.py:215-225: apply -> RMS -> maxima(+) -> negate -> maxima(-)."""
+    Z, X, Y = 10, 130, 140
+    img = mm["synth"].dapi_stack(Z, X, Y, 5, n_nuclei=12, radii=(3.0, 12.0, 12.0))
+    psf = mm["synth"].gaussian_psf((9, 9, 9), 2.0, 1.3)
+    dec = mm["dc"].Deconvolver(psf, img.shape, zpad=(Z - 1) // 2, **DAPI)
+    dimg = img.cuda()
+    plus, minus, buf, rms = mm["pl"].dapi_spots(dec, dimg, None, **DAPI)
+    ref_buf = dec.apply(dimg, None, **DAPI)
+    np.testing.assert_array_equal(buf.cpu().numpy(), ref_buf.cpu().numpy())
+    v = ref_buf.double()
+    rms_ref = np.float32(np.float32(np.sqrt(float((v * v).sum()))) / np.sqrt(v.numel()))
+    assert abs(rms - rms_ref) <= 2e-7 * rms_ref
+    normed = (ref_buf / torch.tensor(rms, dtype=torch.float32, device="cuda"))
+    p2 = mm["mx"].find_local_maxima(normed, raw=dimg, **DAPI)
+    m2 = mm["mx"].find_local_maxima(-normed, raw=dimg, **DAPI)
+    np.testing.assert_array_equal(ck.sort_rows(plus.cpu().numpy()), ck.sort_rows(p2.cpu().numpy()))
+    np.testing.assert_array_equal(ck.sort_rows(minus.cpu().numpy()), ck.sort_rows(m2.cpu().numpy()))
+    assert len(plus) > 0 and len(minus) > 0
