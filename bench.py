@@ -1,0 +1,435 @@
+#!/usr/bin/env python
+"""Benchmark of the per-FOV image path (deconv + blur + maxima + fit).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mermake_gb300|reference]
+                    [--workload fov3c|tile] [--form batched|plain]
+
+A step is one FOV of the workload, inputs resident in HBM:
+
+* ``fov3c`` (default): the full hyb FOV, 3 colours + DAPI, uint16
+  50 x 2048 x 2048 per channel, 40,000 puncta per colour, quadratic flat
+  field gain 0.8-1.0, DAPI of 300 nuclei; tile 500, overlap 89; hyb beta 1e-4,
+  blur 30, threshold 3600, delta 1, fit 3, zpad 49; DAPI beta 0.01, blur 50,
+  threshold 3.0, delta 5, fit 5, zpad 24.
+* ``quad``: one colour of 50 x 1000 x 1000 (2 x 2 tiles), 10,000 puncta, flat
+  field: the small case for profiler captures (spectra larger than L2).
+* ``tile``: one smFISH tile, uint16 40 x 500 x 500, 2,000 puncta, no flat field.
+
+``value`` is FOV input voxels per second (all channels) of the batched form
+(tiles of a colour in one batch, spots kept and offset on the device);
+``--form plain`` times the per-tile loop of ``Deconvolver.tile_wise`` +
+``find_local_maxima`` instead.  ``e2e`` is the same metric through the same
+public calls with the channels copied from pinned host memory every step and
+the spot tables read back.  ``roofline`` reports the dominant kernel (largest
+share of device time in the timed region) from the library's per-stage CUDA
+events, against the measured HBM copy bandwidth.  ``--impl reference`` times
+the CPU restatement of the reference's functions (FP64 NumPy/SciPy FFT
+deconvolution + C maxima/fit) on a bounded sample on the host cores.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L2_BYTES = 129 * 2 ** 20
+
+WORKLOADS = {
+    "fov3c": dict(Z=50, X=2048, Y=2048, colours=3, puncta=40000, flat=True, dapi=True, nuclei=300,
+                  hyb=dict(tile_size=500, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
+                           delta_fit=3, sigmaZ=1, sigmaXY=1.5),
+                  dapi_args=dict(tile_size=500, overlap=89, beta=0.01, threshold=3.0, blur_radius=50, delta=5,
+                                 delta_fit=5, sigmaZ=1, sigmaXY=1.5)),
+    "quad": dict(Z=50, X=1000, Y=1000, colours=1, puncta=10000, flat=True, dapi=False, nuclei=0,
+                 hyb=dict(tile_size=500, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
+                          delta_fit=3, sigmaZ=1, sigmaXY=1.5)),
+    "tile": dict(Z=40, X=500, Y=500, colours=1, puncta=2000, flat=False, dapi=False, nuclei=0,
+                 hyb=dict(tile_size=500, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
+                          delta_fit=3, sigmaZ=1, sigmaXY=1.5)),
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="mermake_gb300", choices=["mermake_gb300", "reference"])
+    ap.add_argument("--workload", default="fov3c", choices=sorted(WORKLOADS))
+    ap.add_argument("--form", default="batched", choices=["batched", "plain"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+def fov_voxels(w):
+    return (w["colours"] + (1 if w["dapi"] else 0)) * w["Z"] * w["X"] * w["Y"]
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def setup(w, device, seed=1000):
+    import torch
+
+    from mermake_gb300 import deconvolver, synth
+    Z, X, Y = w["Z"], w["X"], w["Y"]
+    psf = synth.gaussian_psf((40, 40, 40), 2.0, 1.3)
+    gain = synth.flat_gain(X, Y) if w["flat"] else None
+    chans, flats = [], []
+    for c in range(w["colours"]):
+        chans.append(synth.hyb_stack(Z, X, Y, w["puncta"], seed + 17 * c, device=device, gain=gain))
+        flats.append(torch.from_numpy(gain).to(device) if gain is not None else None)
+    dapi = None
+    if w["dapi"]:
+        dapi = synth.dapi_stack(Z, X, Y, seed + 99, device=device, n_nuclei=w["nuclei"])
+    dec_h = deconvolver.Deconvolver(psf, (Z, X, Y), zpad=Z - 1, **w["hyb"])
+    dec_d = deconvolver.Deconvolver(psf, (Z, X, Y), zpad=(Z - 1) // 2, **w["dapi_args"]) if w["dapi"] else None
+    torch.cuda.synchronize()
+    return dict(chans=chans, flats=flats, dapi=dapi, dec_h=dec_h, dec_d=dec_d, w=w)
+
+
+def run_fov(s, form, chans=None, dapi=None):
+    """One FOV through the public API; returns the spot tables (device)."""
+    import torch
+
+    from mermake_gb300 import maxima, pipeline
+    w = s["w"]
+    chans = s["chans"] if chans is None else chans
+    dapi = s["dapi"] if dapi is None else dapi
+    out = []
+    if w["dapi"]:
+        p, m, buf, _ = pipeline.dapi_spots(s["dec_d"], dapi, None, buffer=s.get("buffer"), **w["dapi_args"])
+        s["buffer"] = buf
+        out += [p, m]
+    for c, ch in enumerate(chans):
+        if form == "batched":
+            out.append(pipeline.hyb_spots(s["dec_h"], ch, s["flats"][c], **w["hyb"]))
+        else:
+            ov = w["hyb"]["overlap"]
+            rows = []
+            for x, y, tile, raw in s["dec_h"].tile_wise(ch, s["flats"][c], **w["hyb"]):
+                Xh = maxima.find_local_maxima(tile, raw=raw, **w["hyb"])
+                lim = torch.tensor([tile.shape[1] - ov, tile.shape[2] - ov], device=Xh.device)
+                keep = torch.all((Xh[:, 1:3] >= ov) & (Xh[:, 1:3] < lim), dim=-1)
+                if torch.any(keep):
+                    Xh = Xh[keep]
+                    Xh[:, 1] += x - ov
+                    Xh[:, 2] += y - ov
+                    rows.append(Xh)
+            out.append(torch.cat(rows) if rows else torch.zeros((0, 8), device=ch.device))
+    return out
+
+
+def timed(fn, K, W, barrier):
+    import torch
+    for _ in range(W):
+        fn()
+    barrier()
+    torch.cuda.synchronize()
+    st = torch.cuda.current_stream()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(K + 1)]
+    evs[0].record(st)
+    for k in range(K):
+        fn()
+        evs[k + 1].record(st)
+    torch.cuda.synchronize()
+    barrier()
+    per = [evs[k].elapsed_time(evs[k + 1]) for k in range(K)]
+    return evs[0].elapsed_time(evs[K]), per
+
+
+def pct(v, q):
+    v = sorted(v)
+    i = min(len(v) - 1, max(0, int(round(q / 100.0 * (len(v) - 1)))))
+    return v[i]
+
+
+def gpu_arm(args, rank, world, local):
+    import torch
+
+    from mermake_gb300 import _lib
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w = WORKLOADS[args.workload]
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+
+    def barrier():
+        if pg:
+            pg.barrier()
+
+    s = setup(w, dev, seed=1000 + rank)
+    vox = fov_voxels(w)
+
+    # device-resident timed region, with per-stage events live
+    _lib.profile_enable(True)
+    n0 = _lib.launch_count()
+    with ClockSampler(local) as clk:
+        total_ms, per = timed(lambda: run_fov(s, args.form), args.steps, args.warmup, barrier)
+    launches = _lib.launch_count() - n0
+    prof = _lib.profile_read()
+    _lib.profile_enable(False)
+    # the warm-up steps ran with profiling on too: scale stage totals to the timed steps
+    frac_timed = args.steps / float(args.steps + args.warmup)
+    t = torch.tensor([total_ms], device=dev)
+    if pg:
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = world * vox * args.steps / (total_ms / 1e3)
+
+    # dominant kernel
+    stages = {k: v for k, v in prof.items() if v[2] > 0}
+    dom = max(stages, key=lambda k: stages[k][0])
+    dms, dbytes, dl = stages[dom]
+    peaks = {}
+    pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pp):
+        peaks = json.load(open(pp))
+    peak = peaks.get("hbm_gbs")
+    peak_src = "measured" if peak else "fallback"
+    peak = peak or 6800.0
+    achieved = (dbytes / dl) / ((dms / dl) / 1e3) / 1e9
+    traffic = None
+    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tp):
+        traffic = json.load(open(tp)).get(dom)
+    stage_share = {k: round(v[0] / sum(x[0] for x in stages.values()), 4) for k, v in stages.items()}
+
+    line = {
+        "metric": "FOV voxels/s deconv+blur+maxima+fit",
+        "value": value,
+        "unit": "voxels/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded Poisson background + Gaussian puncta / nuclei, shapes of the named workload)",
+        "config": {"workload": args.workload, "form": args.form, "Z": w["Z"], "X": w["X"], "Y": w["Y"],
+                   "channels": w["colours"] + (1 if w["dapi"] else 0), "tile_size": w["hyb"]["tile_size"],
+                   "overlap": w["hyb"]["overlap"], "fov_voxels": vox,
+                   "l2": "inputs larger than L2 (%.2f GB per FOV vs 129 MB)" % (vox * 2 / 1e9),
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "latency_ms": {"p50": pct(per, 50), "p99": pct(per, 99)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+                     "bytes_per_launch": dbytes / dl, "ms_per_launch": dms / dl,
+                     "stage_share": stage_share},
+        "clocks": clk.summary(),
+    }
+
+    if not args.no_e2e:
+        import torch
+        host_ch = [c.cpu().pin_memory() for c in s["chans"]]
+        host_dapi = s["dapi"].cpu().pin_memory() if s["dapi"] is not None else None
+        dev_ch = [torch.empty_like(c) for c in s["chans"]]
+        dev_dapi = torch.empty_like(s["dapi"]) if s["dapi"] is not None else None
+        io = {"h2d": 0, "d2h": 0}
+
+        def e2e_step():
+            for h, d in zip(host_ch, dev_ch):
+                d.copy_(h, non_blocking=True)
+            if host_dapi is not None:
+                dev_dapi.copy_(host_dapi, non_blocking=True)
+            outs = run_fov(s, args.form, chans=dev_ch, dapi=dev_dapi)
+            hb = [o.to("cpu") for o in outs]
+            io["h2d"] = sum(h.numel() * h.element_size() for h in host_ch) + (
+                host_dapi.numel() * host_dapi.element_size() if host_dapi is not None else 0)
+            io["d2h"] = sum(h.numel() * h.element_size() for h in hb)
+
+        e_ms, _ = timed(e2e_step, args.steps, 1, barrier)
+        t = torch.tensor([e_ms], device=dev)
+        if pg:
+            pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        e_ms = float(t.item())
+        line["e2e"] = {"value": world * vox * args.steps / (e_ms / 1e3), "unit": "voxels/s",
+                       "h2d_bytes_per_step": io["h2d"], "d2h_bytes_per_step": io["d2h"],
+                       "ms_per_step": e_ms / args.steps}
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, s)
+    if pg:
+        pg.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# CPU restatement of the reference (oracle) on a bounded sample
+# ---------------------------------------------------------------------------
+def cpu_sample(w, img_np, flat_np, psf, t_index):
+    """Deconv + blur + maxima + fit of one tile with the oracle (FP64 FFT,
+    C maxima/fit); returns the FOV voxels that tile accounts for."""
+    import numpy as np
+
+    from oracle import ckernels as ck
+    from oracle import deconv as od
+    a = w["hyb"]
+    Z = w["Z"]
+    W = cpu_sample.W
+    if W is None:
+        W = cpu_sample.W = od.wiener_half(psf, Z, a["tile_size"], Z - 1, a["overlap"], a["beta"])
+    box = od.tiles(img_np.shape, a["tile_size"], a["overlap"])[t_index]
+    res, raw = od.deconv_tile(img_np, flat_np, box, W, a["tile_size"], Z - 1, a["overlap"], a["blur_radius"])
+    Xh = ck.find_local_maxima(res.astype(np.float32), a["threshold"], a["delta"], a["delta_fit"], raw,
+                              a["sigmaZ"], a["sigmaXY"])
+    x, y = box[0], box[1]
+    return Z * min(a["tile_size"], w["X"] - x) * min(a["tile_size"], w["Y"] - y), len(Xh)
+
+
+cpu_sample.W = None
+
+
+def cpu_baseline(w, s=None, steps=1):
+    """Times the oracle on one interior hyb tile of the workload."""
+    import numpy as np
+
+    from mermake_gb300 import synth
+    from oracle import build as obuild
+    obuild.build_oracle()
+    Z, X, Y = w["Z"], w["X"], w["Y"]
+    a = w["hyb"]
+    # the tile and its overlap only: generate (on the CPU) just the tile's input region
+    x0 = a["tile_size"] if X > a["tile_size"] else 0
+    psf = synth.gaussian_psf((40, 40, 40), 2.0, 1.3)
+    if s is not None:
+        img = s["chans"][0].cpu().numpy()
+        flat = s["flats"][0].cpu().numpy() if s["flats"][0] is not None else None
+    else:
+        gain = synth.flat_gain(X, Y) if w["flat"] else None
+        img = synth.hyb_stack(Z, X, Y, w["puncta"], 1000, gain=gain).numpy()
+        flat = gain
+    ny = -(-Y // a["tile_size"])
+    t_index = (1 if X > a["tile_size"] else 0) * ny + (1 if Y > a["tile_size"] else 0)
+    cpu_sample(w, img, flat, psf, t_index)  # warm (Wiener spectrum, FFT plans)
+    t0 = time.perf_counter()
+    vox = 0
+    for _ in range(steps):
+        v, _ = cpu_sample(w, img, flat, psf, t_index)
+        vox += v
+    dt = time.perf_counter() - t0
+    return {"value": vox / dt, "unit": "voxels/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": "%d x interior hyb tile %dx%d of the %s workload (padded %dx%dx%d): FP64 scipy.fft "
+                      "deconvolution + blur, C maxima/fit (OpenMP); Wiener spectrum built untimed"
+                      % (steps, a["tile_size"], a["tile_size"], "fov3c" if w["dapi"] else "tile",
+                         3 * Z - 2, a["tile_size"] + 2 * a["overlap"], a["tile_size"] + 2 * a["overlap"]),
+            "seconds": dt}
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    w = WORKLOADS[args.workload]
+    cb = cpu_baseline(w, None, steps=max(1, args.steps))
+    line = {
+        "impl": "reference",
+        "metric": "FOV voxels/s deconv+blur+maxima+fit",
+        "value": cb["value"],
+        "unit": "voxels/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": cb["seconds"] * 1e3 / max(1, args.steps),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded Poisson background + Gaussian puncta, shapes of the named workload)",
+        "config": {"workload": args.workload, "form": "reference CPU restatement", "Z": w["Z"], "X": w["X"],
+                   "Y": w["Y"]},
+        "cpu_baseline": cb,
+        "e2e": {"value": cb["value"], "unit": "voxels/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    gpu_arm(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

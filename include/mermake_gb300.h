@@ -147,6 +147,20 @@ int mm_tile_geometry(int Z, int X, int Y, int tile_size, int zpad, int overlap, 
  * (element e of line l at data[e*nlines + l]); inverse uses exp(+i...). */
 int mm_fft_c2c(void *data, int n, int nlines, int inverse, void *stream);
 
+/* Instrumentation, no reference counterpart (the reference has no timing on
+ * this path).  mm_profile_enable(ctx, 1) resets and starts per-stage CUDA-event
+ * timing of this context's launches (stages: rows_fwd, cols_fwd, zpass,
+ * cols_inv, rows_inv_blur_y, blur_x_sub, make_raw, maxima_fit, sumsq, wiener);
+ * mm_profile_read fills up to nmax entries of total milliseconds, algorithmic
+ * bytes (the DRAM traffic each stage's function needs at minimum) and launch
+ * counts, synchronising the recorded events, and returns the number of
+ * stages.  mm_stage_name(i) names stage i.  mm_launch_count() is the number of
+ * kernels this library has launched in the process. */
+int mm_profile_enable(mm_ctx *ctx, int on);
+int mm_profile_read(mm_ctx *ctx, int nmax, double *ms, double *bytes, int64_t *launches);
+const char *mm_stage_name(int i);
+uint64_t mm_launch_count(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,6 +59,10 @@ _SIGS = {
                        _i32, _i32, _f32, _f32, _i32, _vp, _vp, _u32, _pu32, _vp, _u32, _pu32, _pf32, _vp], _i32),
     "mm_tile_geometry": ([_i32] * 8 + [_vp] * 4, _i32),
     "mm_fft_c2c": ([_vp, _i32, _i32, _i32, _vp], _i32),
+    "mm_profile_enable": ([_vp, _i32], _i32),
+    "mm_profile_read": ([_vp, _i32, C.POINTER(C.c_double), C.POINTER(C.c_double), _pi64], _i32),
+    "mm_stage_name": ([_i32], C.c_char_p),
+    "mm_launch_count": ([], C.c_uint64),
 }
 
 
@@ -133,3 +137,24 @@ def i64arr(vals):
 
 def ptr(t):
     return _vp(t.data_ptr()) if t is not None else _vp(0)
+
+
+def profile_enable(on=True, device=None):
+    check(lib().mm_profile_enable(ctx(device), int(bool(on))))
+
+
+def profile_read(device=None):
+    """{stage: (ms, algorithmic bytes, launches)} accumulated since profile_enable."""
+    L = lib()
+    n = 32
+    ms = (C.c_double * n)()
+    by = (C.c_double * n)()
+    la = (C.c_int64 * n)()
+    k = L.mm_profile_read(ctx(device), n, ms, by, la)
+    if k < 0:
+        check(k)
+    return {L.mm_stage_name(i).decode(): (ms[i], by[i], int(la[i])) for i in range(k)}
+
+
+def launch_count():
+    return int(lib().mm_launch_count())

@@ -4,6 +4,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "deconv.cuh"
@@ -14,6 +15,10 @@ thread_local char g_err[1024] = "";
 enum Slot { WS_SPEC = 0, WS_RES, WS_TMP, WS_VOL, WS_CAND, WS_SMALL, WS_N };
 }  // namespace
 
+static std::atomic<unsigned long long> g_launches{0};
+void mm_launch_counter_add() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+unsigned long long mm_launch_counter_get() { return g_launches.load(); }
+
 void mm_set_error(const char *fmt, ...) {
     va_list ap;
     va_start(ap, fmt);
@@ -21,15 +26,71 @@ void mm_set_error(const char *fmt, ...) {
     va_end(ap);
 }
 
+// Per-stage timing: when enabled, every stage launch is bracketed by CUDA
+// events on the launching stream; elapsed times are collected when the
+// records are read (or the record buffer fills), together with the stage's
+// algorithmic bytes (the minimum DRAM traffic its function needs).
+enum Stage { ST_ROWS_FWD = 0, ST_COLS_FWD, ST_ZPASS, ST_COLS_INV, ST_ROWS_INV, ST_BLUR_X, ST_MAKE_RAW,
+             ST_MAXIMA_FIT, ST_SUMSQ, ST_WIENER, ST_N };
+static const char *kStageNames[ST_N] = {"rows_fwd", "cols_fwd", "zpass", "cols_inv", "rows_inv_blur_y",
+                                        "blur_x_sub", "make_raw", "maxima_fit", "sumsq", "wiener"};
+constexpr int kMaxRec = 1024;
+
+struct Prof {
+    bool on = false;
+    int n = 0;
+    cudaEvent_t ev0[kMaxRec], ev1[kMaxRec];
+    int stage[kMaxRec];
+    double bytes[kMaxRec];
+    bool created = false;
+    double ms[ST_N] = {};
+    double tot_bytes[ST_N] = {};
+    long long launches[ST_N] = {};
+};
+
 struct mm_ctx {
     std::mutex mu;
     void *ws[WS_N] = {};
     size_t ws_bytes[WS_N] = {};
     unsigned *h_counters = nullptr;  // pinned: [0] candidates, [1] rows, [2] rows (2nd set)
     int device = 0;
+    Prof prof;
 };
 
 namespace {
+
+int prof_collect(mm_ctx *c) {
+    Prof &p = c->prof;
+    for (int i = 0; i < p.n; ++i) {
+        MM_CUDA_TRY(cudaEventSynchronize(p.ev1[i]));
+        float ms = 0.f;
+        MM_CUDA_TRY(cudaEventElapsedTime(&ms, p.ev0[i], p.ev1[i]));
+        p.ms[p.stage[i]] += ms;
+        p.tot_bytes[p.stage[i]] += p.bytes[i];
+        p.launches[p.stage[i]] += 1;
+    }
+    p.n = 0;
+    return MM_OK;
+}
+
+// RAII bracket around one stage launch
+struct StageTimer {
+    mm_ctx *c;
+    int idx = -1;
+    cudaStream_t st;
+    StageTimer(mm_ctx *c_, int stage, double bytes, cudaStream_t st_) : c(c_), st(st_) {
+        Prof &p = c->prof;
+        if (!p.on) return;
+        if (p.n == kMaxRec) prof_collect(c);
+        idx = p.n++;
+        p.stage[idx] = stage;
+        p.bytes[idx] = bytes;
+        cudaEventRecord(p.ev0[idx], st);
+    }
+    ~StageTimer() {
+        if (idx >= 0) cudaEventRecord(c->prof.ev1[idx], st);
+    }
+};
 
 int ws_get(mm_ctx *c, Slot s, size_t bytes, void **out) {
     if (bytes == 0) bytes = 16;
@@ -78,6 +139,14 @@ int small_get(mm_ctx *c, Small **out) {
     return rc;
 }
 
+int ntiles_of(const TileGeom &g) {
+    int nx = (g.X + g.ts - 1) / g.ts;
+    int n = nx * g.ny;
+    // zip(tiles, psf_ffts) truncates when several spectra are given (deconvolver.py:110, 116)
+    if (g.npsf > 1 && g.npsf < n) n = g.npsf;
+    return n;
+}
+
 int fill_geom(TileGeom &g, int Z, int X, int Y, long long isz, long long isx, long long fsx, int ts, int zpad,
               int ov, int npsf) {
     MM_REQUIRE(Z > 0 && X > 0 && Y > 0, "empty channel (%d, %d, %d)", Z, X, Y);
@@ -97,16 +166,11 @@ int fill_geom(TileGeom &g, int Z, int X, int Y, long long isz, long long isx, lo
     g.ny = (Y + ts - 1) / ts;
     g.t0 = 0; g.nt = 0;
     g.npsf = npsf;
+    g.ntot = 0;
+    g.ntot = ntiles_of(g);
     return MM_OK;
 }
 
-int ntiles_of(const TileGeom &g) {
-    int nx = (g.X + g.ts - 1) / g.ts;
-    int n = nx * g.ny;
-    // zip(tiles, psf_ffts) truncates when several spectra are given (deconvolver.py:110, 116)
-    if (g.npsf > 1 && g.npsf < n) n = g.npsf;
-    return n;
-}
 
 // tile_wise core for tiles [g.t0, g.t0 + g.nt)
 int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *flat, const float2 *W, int blur_radius,
@@ -122,19 +186,44 @@ int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *
     if (blur_radius >= 0 && (rc = ws_get(c, WS_TMP, sizeof(float) * tile_r * g.nt, &tmp))) return rc;
     float2 *S = (float2 *)spec;
     const long long wstride = (long long)g.Zp * plane_c;
-    if ((rc = mm_launch_rows_fwd_img(g, image, dtype, flat, S, st))) return rc;
-    if ((rc = mm_launch_cols(S, g.P, g.H, g.H, plane_c, g.nt * g.Z, false, st))) return rc;
-    if ((rc = mm_launch_zpass(g, S, W, wstride, st))) return rc;
-    if ((rc = mm_launch_cols(S, g.P, g.H, g.H, plane_c, g.nt * g.Z, true, st))) return rc;
-    if ((rc = mm_launch_rows_inv(S, g.nt * g.Z * g.P, g.P, g.H, (float *)res, st))) return rc;
+    // algorithmic bytes of each stage for this batch (its inputs read once, outputs written once)
+    double in_b = 0;
+    for (int t = g.t0; t < g.t0 + g.nt; ++t) {
+        TileDesc d = mm_tile_desc(g, t);
+        in_b += (double)g.Z * d.xd * d.yd * (dtype == MM_DTYPE_U16 ? 2 : 4) + (flat ? 4.0 * d.xd * d.yd : 0.0);
+    }
+    const double spec_b = 8.0 * tile_c * g.nt, real_b = 4.0 * tile_r * g.nt, w_b = 8.0 * wstride * g.nt;
+    {
+        StageTimer t(c, ST_ROWS_FWD, in_b + spec_b, st);
+        if ((rc = mm_launch_rows_fwd_img(g, image, dtype, flat, S, st))) return rc;
+    }
+    {
+        StageTimer t(c, ST_COLS_FWD, 2 * spec_b, st);
+        if ((rc = mm_launch_cols(S, g.P, g.H, g.H, plane_c, g.nt * g.Z, false, st))) return rc;
+    }
+    {
+        StageTimer t(c, ST_ZPASS, 2 * spec_b + w_b, st);
+        if ((rc = mm_launch_zpass(g, S, W, wstride, st))) return rc;
+    }
+    {
+        StageTimer t(c, ST_COLS_INV, 2 * spec_b, st);
+        if ((rc = mm_launch_cols(S, g.P, g.H, g.H, plane_c, g.nt * g.Z, true, st))) return rc;
+    }
     const int delta = blur_radius >= 0 ? blur_radius / 2 : -1;
-    if (delta >= 0 && (rc = mm_launch_blur_y((float *)res, (float *)tmp, g.nt * g.Z * g.P, g.P, delta, st)))
-        return rc;
+    {
+        StageTimer t(c, ST_ROWS_INV, spec_b + real_b * (delta >= 0 ? 2 : 1), st);
+        if ((rc = mm_launch_rows_inv(S, g.nt * g.Z * g.P, g.P, g.H, (float *)res, (float *)tmp, delta, st)))
+            return rc;
+    }
     if (delta >= 0 || stitch) {
+        StageTimer t(c, ST_BLUR_X, (delta >= 0 ? 3 : 2) * real_b, st);
         if ((rc = mm_launch_blur_x_sub(g, (float *)res, (float *)tmp, delta, (float *)res, stitch, osz, osx, st)))
             return rc;
     }
-    if (raw_out && (rc = mm_launch_make_raw(g, image, dtype, flat, raw_out, st))) return rc;
+    if (raw_out) {
+        StageTimer t(c, ST_MAKE_RAW, in_b + real_b, st);
+        if ((rc = mm_launch_make_raw(g, image, dtype, flat, raw_out, st))) return rc;
+    }
     return MM_OK;
 }
 
@@ -169,6 +258,11 @@ int mm_ctx_create(mm_ctx **out) {
 int mm_ctx_destroy(mm_ctx *c) {
     if (!c) return MM_OK;
     cudaDeviceSynchronize();
+    if (c->prof.created)
+        for (int i = 0; i < kMaxRec; ++i) {
+            cudaEventDestroy(c->prof.ev0[i]);
+            cudaEventDestroy(c->prof.ev1[i]);
+        }
     for (int s = 0; s < WS_N; ++s)
         if (c->ws[s]) cudaFree(c->ws[s]);
     if (c->h_counters) cudaFreeHost(c->h_counters);
@@ -192,6 +286,7 @@ int mm_wiener_spectrum(mm_ctx *c, const float *psf, int pz, int px, int py, int 
     if ((rc = ws_get(c, WS_VOL, sizeof(float) * (size_t)nz * nx * nx, &vol))) return rc;
     if ((rc = ws_get(c, WS_SPEC, sizeof(float2) * (size_t)nz * nx * H, &spec))) return rc;
     if ((rc = small_get(c, &sm))) return rc;
+    StageTimer tm(c, ST_WIENER, 4.0 * nz * nx * nx + 8.0 * nz * nx * H, st);
     return mm_wiener_build_impl(psf, pz, px, py, tile_height, tile_size, zpad, overlap, beta, (float2 *)W,
                                 (float *)vol, (float2 *)spec, &sm->sumsq, st);
 }
@@ -302,9 +397,17 @@ int mm_hyb_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t 
             a.th = threshold; a.delta = delta; a.delta_fit = delta_fit;
             a.sigmaZ = sigmaZ; a.sigmaXY = sigmaXY;
             a.div = 0.f; a.divp = nullptr; a.neg = 0; a.keep_filter = 1;
-            if ((rc = mm_launch_maxima_fit(a, (uint2 *)cand, (unsigned)cap, &sm->cand, out, out_cap, &sm->rows,
-                                           t0 == 0, st)))
-                return rc;
+            {
+                double vb = 0;
+                for (int t = gb.t0; t < gb.t0 + gb.nt; ++t) {
+                    TileDesc d = mm_tile_desc(gb, t);
+                    vb += 4.0 * Z * d.xend * d.yend;
+                }
+                StageTimer tm(c, ST_MAXIMA_FIT, vb, st);
+                if ((rc = mm_launch_maxima_fit(a, (uint2 *)cand, (unsigned)cap, &sm->cand, out, out_cap, &sm->rows,
+                                               t0 == 0, st)))
+                    return rc;
+            }
             if ((rc = mm_launch_note_overflow(&sm->cand, (unsigned)cap, &sm->overflow, st))) return rc;
         }
         MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters, &sm->rows, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
@@ -349,7 +452,10 @@ int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t
                             (long long)X * Y, Y, st)))
             return rc;
     }
-    if ((rc = mm_launch_sumsq(buffer, N, &sm->sumsq, st))) return rc;
+    {
+        StageTimer tm(c, ST_SUMSQ, 4.0 * N, st);
+        if ((rc = mm_launch_sumsq(buffer, N, &sm->sumsq, st))) return rc;
+    }
     if ((rc = mm_launch_rms_div(&sm->sumsq, N, &sm->div, st))) return rc;
     for (int attempt = 0; attempt < 2; ++attempt) {
         size_t cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
@@ -369,8 +475,11 @@ int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t
             a.div = 0.f; a.divp = &sm->div; a.neg = sign; a.keep_filter = 0;
             float *o = sign ? out_minus : out_plus;
             unsigned oc = sign ? cap_minus : cap_plus;
-            if ((rc = mm_launch_maxima_fit(a, (uint2 *)cand, (unsigned)cap, &sm->cand, o, oc, nullptr, 0, st)))
-                return rc;
+            {
+                StageTimer tm(c, ST_MAXIMA_FIT, 4.0 * N, st);
+                if ((rc = mm_launch_maxima_fit(a, (uint2 *)cand, (unsigned)cap, &sm->cand, o, oc, nullptr, 0, st)))
+                    return rc;
+            }
             unsigned *dst = sign ? &sm->rows2 : &sm->rows;
             MM_CUDA_TRY(cudaMemcpyAsync(dst, &sm->cand, sizeof(unsigned), cudaMemcpyDeviceToDevice, st));
             if ((rc = mm_launch_note_overflow(&sm->cand, (unsigned)cap, &sm->overflow, st))) return rc;
@@ -420,3 +529,45 @@ extern "C" int mm_fft_c2c(void *data, int n, int nlines, int inverse, void *stre
     MM_REQUIRE(data && n >= 1 && nlines >= 1, "bad FFT arguments");
     return mm_launch_cols((float2 *)data, n, nlines, nlines, 0, 1, inverse != 0, (cudaStream_t)stream);
 }
+
+extern "C" int mm_profile_enable(mm_ctx *c, int on) {
+    MM_REQUIRE(c, "null context");
+    std::lock_guard<std::mutex> lock(c->mu);
+    Prof &p = c->prof;
+    if (on && !p.created) {
+        for (int i = 0; i < kMaxRec; ++i) {
+            MM_CUDA_TRY(cudaEventCreate(&p.ev0[i]));
+            MM_CUDA_TRY(cudaEventCreate(&p.ev1[i]));
+        }
+        p.created = true;
+    }
+    if (p.n) {
+        int rc = prof_collect(c);
+        if (rc) return rc;
+    }
+    for (int i = 0; i < ST_N; ++i) {
+        p.ms[i] = 0;
+        p.tot_bytes[i] = 0;
+        p.launches[i] = 0;
+    }
+    p.on = on != 0;
+    return MM_OK;
+}
+
+extern "C" int mm_profile_read(mm_ctx *c, int nmax, double *ms, double *bytes, int64_t *launches) {
+    MM_REQUIRE(c, "null context");
+    std::lock_guard<std::mutex> lock(c->mu);
+    int rc = prof_collect(c);
+    if (rc) return rc;
+    const int n = nmax < ST_N ? nmax : ST_N;
+    for (int i = 0; i < n; ++i) {
+        if (ms) ms[i] = c->prof.ms[i];
+        if (bytes) bytes[i] = c->prof.tot_bytes[i];
+        if (launches) launches[i] = c->prof.launches[i];
+    }
+    return ST_N;
+}
+
+extern "C" const char *mm_stage_name(int i) { return (i >= 0 && i < ST_N) ? kStageNames[i] : ""; }
+
+extern "C" uint64_t mm_launch_count(void) { return mm_launch_counter_get(); }

@@ -9,303 +9,259 @@
 //   rows_fwd_img  y: gather u16 (or f32) tile rows through the pad maps, divide by the
 //                 flat, pack two real rows per complex line, FFT, unpack to
 //                 two half spectra.                       (deconvolver.py:123-148, 155)
-//   cols          x: in-place complex FFT along a strided axis (fwd / inv)
-//   zpass         z: gather mapped planes, FFT(Zp), multiply by the
-//                 pre-scaled Wiener spectrum, IFFT(Zp), keep [zpad, zpad+Z)
-//                                                         (deconvolver.py:155-157)
-//   rows_inv      y: two half spectra -> one complex line -> IFFT -> two real rows
-//   blur_y, blur_x_sub   box blur (blur.cu:1-52 semantics) and subtraction,
-//                 optionally stitching the centre into the FOV output
+//   (the x and z passes are in fft_cols.cu and fft_z.cu)
+//   rows_inv      y: two half spectra -> one complex line -> IFFT -> two real
+//                 rows, and their box mean along y (sliding window)
+//   blur_x_sub    box mean along x of that, subtracted from the result
+//                 (blur.cu:1-52 semantics), optionally stitching the centre
+//                 into the FOV output
 //                                                         (deconvolver.py:160-163, 183)
 //   make_raw      the raw view handed to the spot fit     (deconvolver.py:165-170)
 #include "deconv.cuh"
 
 namespace {
 
-constexpr int kThreads = 256;
-constexpr int kSmemLimit = 200 * 1024;
-
-// Lines per CTA for a length-n transform: the largest power of two (<= maxnl)
-// whose ping-pong buffers plus tables fit the shared-memory budget.
-int pick_nl(const FftPlan &P, int maxnl) {
-    int nl = maxnl;
-    while (nl > 1) {
-        size_t b = (size_t)2 * P.n * (nl + 1) * sizeof(float2) + (size_t)(P.n + P.ntab) * sizeof(float2);
-        if (b <= (size_t)kSmemLimit) break;
-        nl >>= 1;
-    }
-    return nl;
-}
-
-size_t fft_smem(const FftPlan &P, int nl) {
-    return (size_t)2 * P.n * (nl + 1) * sizeof(float2) + (size_t)(P.n + P.ntab) * sizeof(float2);
-}
+constexpr int kThreads = kFftThreads;
+constexpr int kSmemLimit = kFftSmemLimit;
 
 template <typename K>
-int set_smem(K kernel, size_t bytes) {
+int set_smem(K *kernel, size_t bytes) {
     MM_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
     return MM_OK;
 }
 
 // ---------------------------------------------------------------------------
-// y pass, forward, u16 tile source
+// y pass, forward, tile source (u16 or f32) through the pad maps.  One warp
+// gathers one padded row at a time (row-level map and addresses computed once,
+// lanes over the row), eight loads in flight per lane.
 // ---------------------------------------------------------------------------
-template <typename T>
+template <typename T, int LMAX>
 __global__ void __launch_bounds__(kThreads)
 k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ flat,
                float2 *__restrict__ S, FftPlan P, int nl) {
-    extern __shared__ float2 smem[];
-    const int n = P.n, ld = nl + 1;
-    float2 *A = smem, *B = A + n * ld, *tw = B + n * ld, *tab = tw + n;
-    fft_load_tables(P, tw, tab);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = P.n;
+    const FftSmem L = fft_smem_layout(smem_raw, P, nl);
+    fft_load_tables(P, L.tw, L.tab);
 
     const int ti = g.t0 + blockIdx.y;
     const TileDesc d = mm_tile_desc(g, ti);
     const long long nrows = (long long)g.Z * g.P;
     const long long row0 = (long long)blockIdx.x * 2 * nl;
-
-    for (int it = threadIdx.x; it < 2 * nl * n; it += blockDim.x) {
-        int q = it / n, e = it % n;
-        long long row = row0 + q;
-        float v = 0.f;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    float *Af = reinterpret_cast<float *>(L.A);
+    for (int q = warp; q < 2 * nl; q += nw) {
+        const long long row = row0 + q;
+        const int l = q >> 1, comp = q & 1;
+        const T *src = nullptr;
+        const float *fsrc = nullptr;
         if (row < nrows) {
-            int z = (int)(row / g.P), xp = (int)(row % g.P);
-            int sx = mm_map_xy(xp, d.x == 0, d.xd, g.P, g.ov);
-            int sy = mm_map_xy(e, d.y == 0, d.yd, g.P, g.ov);
-            if (sx >= 0 && sy >= 0) {
-                int gx = d.x0 + sx, gy = d.y0 + sy;
-                v = (float)img[z * g.isz + gx * g.isx + gy];
-                if (flat) v = __fdiv_rn(v, flat[gx * g.fsx + gy]);
+            const int z = (int)(row / g.P), xp = (int)(row % g.P);
+            const int sx = mm_map_xy(xp, d.x == 0, d.xd, g.P, g.ov);
+            if (sx >= 0) {
+                src = img + z * g.isz + (long long)(d.x0 + sx) * g.isx + d.y0;
+                if (flat) fsrc = flat + (long long)(d.x0 + sx) * g.fsx + d.y0;
             }
         }
-        float *s = reinterpret_cast<float *>(&A[e * ld + (q >> 1)]);
-        s[q & 1] = v;
+        constexpr int U = 8;
+        for (int e0 = lane; e0 < n; e0 += 32 * U) {
+            float v[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int e = e0 + 32 * u;
+                v[u] = 0.f;
+                if (src && e < n) {
+                    const int sy = mm_map_xy(e, d.y == 0, d.yd, g.P, g.ov);
+                    if (sy >= 0) {
+                        // transform input: the fast division is within 2 ulp; the raw
+                        // view (k_make_raw) keeps the reference's IEEE quotient
+                        v[u] = (float)src[sy];
+                        if (fsrc) v[u] = __fdividef(v[u], fsrc[sy]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int e = e0 + 32 * u;
+                if (e < n) Af[2 * sidx(e, l, nl) + comp] = v[u];
+            }
+        }
     }
     __syncthreads();
-    float2 *R = fft_lines<false>(A, B, ld, nl, P, tw, tab);
+    float2 *R = fft_lines<false, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
 
     const int H = g.H;
+    const float invH = 1.0f / (float)H;
     float2 *Sb = S + (long long)blockIdx.y * nrows * H;
     for (int it = threadIdx.x; it < nl * H; it += blockDim.x) {
-        int l = it / H, k = it % H;
-        long long r0 = row0 + 2 * l;
-        float2 ck = R[k * ld + l];
-        float2 cn = R[((n - k) % n) * ld + l];
-        float2 x1 = make_float2(0.5f * (ck.x + cn.x), 0.5f * (ck.y - cn.y));
-        float2 x2 = make_float2(0.5f * (ck.y + cn.y), -0.5f * (ck.x - cn.x));
-        if (r0 < nrows) Sb[r0 * H + k] = x1;
-        if (r0 + 1 < nrows) Sb[(r0 + 1) * H + k] = x2;
+        const int l = fdiv_i(it, H, invH), k = it - l * H;
+        const long long r0 = row0 + 2 * l;
+        const float2 ck = R[sidx(k, l, nl)];
+        const float2 cn = R[sidx((n - k) % n, l, nl)];
+        if (r0 < nrows) Sb[r0 * H + k] = make_float2(0.5f * (ck.x + cn.x), 0.5f * (ck.y - cn.y));
+        if (r0 + 1 < nrows) Sb[(r0 + 1) * H + k] = make_float2(0.5f * (ck.y + cn.y), -0.5f * (ck.x - cn.x));
     }
 }
 
 // y pass, forward, dense f32 source (the padded PSF volume)
+template <int LMAX>
 __global__ void __launch_bounds__(kThreads)
 k_rows_fwd_f32(const float *__restrict__ vol, long long nrows, float2 *__restrict__ S, FftPlan P, int nl) {
-    extern __shared__ float2 smem[];
-    const int n = P.n, ld = nl + 1, H = n / 2 + 1;
-    float2 *A = smem, *B = A + n * ld, *tw = B + n * ld, *tab = tw + n;
-    fft_load_tables(P, tw, tab);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = P.n, H = n / 2 + 1;
+    const float invH = 1.0f / (float)H, invn = 1.0f / (float)n;
+    const FftSmem L = fft_smem_layout(smem_raw, P, nl);
+    fft_load_tables(P, L.tw, L.tab);
     const long long row0 = (long long)blockIdx.x * 2 * nl;
+    float *Af = reinterpret_cast<float *>(L.A);
     for (int it = threadIdx.x; it < 2 * nl * n; it += blockDim.x) {
-        int q = it / n, e = it % n;
-        long long row = row0 + q;
-        float v = row < nrows ? vol[row * n + e] : 0.f;
-        float *s = reinterpret_cast<float *>(&A[e * ld + (q >> 1)]);
-        s[q & 1] = v;
+        const int q = fdiv_i(it, n, invn), e = it - q * n;
+        const long long row = row0 + q;
+        Af[2 * sidx(e, q >> 1, nl) + (q & 1)] = row < nrows ? vol[row * n + e] : 0.f;
     }
     __syncthreads();
-    float2 *R = fft_lines<false>(A, B, ld, nl, P, tw, tab);
+    float2 *R = fft_lines<false, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
     for (int it = threadIdx.x; it < nl * H; it += blockDim.x) {
-        int l = it / H, k = it % H;
-        long long r0 = row0 + 2 * l;
-        float2 ck = R[k * ld + l];
-        float2 cn = R[((n - k) % n) * ld + l];
+        const int l = fdiv_i(it, H, invH), k = it - l * H;
+        const long long r0 = row0 + 2 * l;
+        const float2 ck = R[sidx(k, l, nl)];
+        const float2 cn = R[sidx((n - k) % n, l, nl)];
         if (r0 < nrows) S[r0 * H + k] = make_float2(0.5f * (ck.x + cn.x), 0.5f * (ck.y - cn.y));
         if (r0 + 1 < nrows) S[(r0 + 1) * H + k] = make_float2(0.5f * (ck.y + cn.y), -0.5f * (ck.x - cn.x));
     }
 }
 
 // ---------------------------------------------------------------------------
-// strided complex FFT, in place: line l of plane p starts at S + p*plane_stride + l,
-// element e at + e*se.  Lines are contiguous, so a CTA's loads are runs of nl.
+// y pass, inverse: rows 2l and 2l+1 of H-long half spectra -> one complex line
+// -> IFFT -> two real rows.  With delta >= 0 the row's box mean along y
+// (blur.cu:1-52 semantics: window [c-delta, c+delta] clipped, divided by the
+// in-range count) is written to `blur` as well: each lane slides a window
+// over a contiguous segment of the row held in shared memory.
 // ---------------------------------------------------------------------------
-template <bool INV>
+template <int LMAX>
 __global__ void __launch_bounds__(kThreads)
-k_cols(float2 *__restrict__ S, long long se, int nlines, long long plane_stride, FftPlan P, int nl) {
-    extern __shared__ float2 smem[];
-    const int n = P.n, ld = nl + 1;
-    float2 *A = smem, *B = A + n * ld, *tw = B + n * ld, *tab = tw + n;
-    fft_load_tables(P, tw, tab);
-    float2 *base = S + (long long)blockIdx.y * plane_stride;
-    const int l0 = blockIdx.x * nl;
-    for (int it = threadIdx.x; it < nl * n; it += blockDim.x) {
-        int l = it % nl, e = it / nl;
-        A[e * ld + l] = (l0 + l < nlines) ? base[e * se + l0 + l] : make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    float2 *R = fft_lines<INV>(A, B, ld, nl, P, tw, tab);
-    for (int it = threadIdx.x; it < nl * n; it += blockDim.x) {
-        int l = it % nl, e = it / nl;
-        if (l0 + l < nlines) base[e * se + l0 + l] = R[e * ld + l];
-    }
-}
-
-// ---------------------------------------------------------------------------
-// z pass of the deconvolution: forward FFT over the padded depth, Wiener
-// multiply, inverse FFT, keep the real planes.  W is (Zp, P, H) per spectrum,
-// already scaled by 1 / (Zp * P * P).
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads)
-k_zpass(TileGeom g, float2 *__restrict__ S, const float2 *__restrict__ W, long long wstride, FftPlan P,
-        int nl) {
-    extern __shared__ float2 smem[];
-    const int n = P.n, ld = nl + 1;
-    float2 *A = smem, *B = A + n * ld, *tw = B + n * ld, *tab = tw + n;
-    fft_load_tables(P, tw, tab);
-    const int ti = g.t0 + blockIdx.y;
-    const TileDesc d = mm_tile_desc(g, ti);
-    const long long plane = (long long)g.P * g.H;
-    float2 *St = S + (long long)blockIdx.y * g.Z * plane;
-    const float2 *Wt = W + (long long)d.psf * wstride;
-    const long long q0 = (long long)blockIdx.x * nl;
-    for (int it = threadIdx.x; it < nl * n; it += blockDim.x) {
-        int l = it % nl, e = it / nl;
-        int src = mm_map_z(e, g.Z, g.zpad, g.Zp);
-        float2 v = make_float2(0.f, 0.f);
-        if (src >= 0 && q0 + l < plane) v = St[src * plane + q0 + l];
-        A[e * ld + l] = v;
-    }
-    __syncthreads();
-    float2 *R = fft_lines<false>(A, B, ld, nl, P, tw, tab);
-    float2 *O = (R == A) ? B : A;
-    for (int it = threadIdx.x; it < nl * n; it += blockDim.x) {
-        int l = it % nl, e = it / nl;
-        float2 w = (q0 + l < plane) ? Wt[e * plane + q0 + l] : make_float2(0.f, 0.f);
-        O[e * ld + l] = cmul(R[e * ld + l], w);
-    }
-    __syncthreads();
-    float2 *R2 = fft_lines<true>(O, R, ld, nl, P, tw, tab);
-    for (int it = threadIdx.x; it < nl * g.Z; it += blockDim.x) {
-        int l = it % nl, z = it / nl;
-        if (q0 + l < plane) St[z * plane + q0 + l] = R2[(g.zpad + z) * ld + l];
-    }
-}
-
-// z pass, forward only, all planes (the PSF transform)
-__global__ void __launch_bounds__(kThreads)
-k_zfwd(float2 *__restrict__ S, long long plane, FftPlan P, int nl) {
-    extern __shared__ float2 smem[];
-    const int n = P.n, ld = nl + 1;
-    float2 *A = smem, *B = A + n * ld, *tw = B + n * ld, *tab = tw + n;
-    fft_load_tables(P, tw, tab);
-    const long long q0 = (long long)blockIdx.x * nl;
-    for (int it = threadIdx.x; it < nl * n; it += blockDim.x) {
-        int l = it % nl, e = it / nl;
-        A[e * ld + l] = (q0 + l < plane) ? S[e * plane + q0 + l] : make_float2(0.f, 0.f);
-    }
-    __syncthreads();
-    float2 *R = fft_lines<false>(A, B, ld, nl, P, tw, tab);
-    for (int it = threadIdx.x; it < nl * n; it += blockDim.x) {
-        int l = it % nl, e = it / nl;
-        if (q0 + l < plane) S[e * plane + q0 + l] = R[e * ld + l];
-    }
-}
-
-// ---------------------------------------------------------------------------
-// y pass, inverse: rows 2l and 2l+1 of H-long half spectra -> real rows of P.
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads)
-k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restrict__ out, FftPlan P, int nl) {
-    extern __shared__ float2 smem[];
-    const int n = P.n, ld = nl + 1;
-    float2 *A = smem, *B = A + n * ld, *tw = B + n * ld, *tab = tw + n;
-    fft_load_tables(P, tw, tab);
+k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restrict__ out,
+           float *__restrict__ blur, int delta, FftPlan P, int nl) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = P.n;
+    const FftSmem L = fft_smem_layout(smem_raw, P, nl);
+    fft_load_tables(P, L.tw, L.tab);
     const long long row0 = (long long)blockIdx.x * 2 * nl;
     const bool even = (n % 2) == 0;
-    for (int it = threadIdx.x; it < nl * H; it += blockDim.x) {
-        int l = it / H, k = it % H;
-        long long r0 = row0 + 2 * l;
-        float2 x1 = r0 < nrows ? S[r0 * H + k] : make_float2(0.f, 0.f);
-        float2 x2 = r0 + 1 < nrows ? S[(r0 + 1) * H + k] : make_float2(0.f, 0.f);
-        if (k == 0 || (even && k == n / 2)) {
-            A[k * ld + l] = make_float2(x1.x, x2.x);
-        } else {
-            A[k * ld + l] = make_float2(x1.x - x2.y, x1.y + x2.x);
-            A[(n - k) * ld + l] = make_float2(x1.x + x2.y, x2.x - x1.y);
+    const float invH = 1.0f / (float)H, invn = 1.0f / (float)n;
+    constexpr int U = 4;
+    for (int base = threadIdx.x; base < nl * H; base += U * blockDim.x) {
+        float2 x1[U], x2[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int it = base + u * blockDim.x;
+            x1[u] = x2[u] = make_float2(0.f, 0.f);
+            if (it < nl * H) {
+                const int l = fdiv_i(it, H, invH), k = it - l * H;
+                const long long r0 = row0 + 2 * l;
+                if (r0 < nrows) x1[u] = S[r0 * H + k];
+                if (r0 + 1 < nrows) x2[u] = S[(r0 + 1) * H + k];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int it = base + u * blockDim.x;
+            if (it >= nl * H) break;
+            const int l = fdiv_i(it, H, invH), k = it - l * H;
+            if (k == 0 || (even && k == n / 2)) {
+                L.A[sidx(k, l, nl)] = make_float2(x1[u].x, x2[u].x);
+            } else {
+                L.A[sidx(k, l, nl)] = make_float2(x1[u].x - x2[u].y, x1[u].y + x2[u].x);
+                L.A[sidx(n - k, l, nl)] = make_float2(x1[u].x + x2[u].y, x2[u].x - x1[u].y);
+            }
         }
     }
     __syncthreads();
-    float2 *R = fft_lines<true>(A, B, ld, nl, P, tw, tab);
+    float2 *R = fft_lines<true, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
+    const float *Rf = reinterpret_cast<const float *>(R);
     for (int it = threadIdx.x; it < 2 * nl * n; it += blockDim.x) {
-        int q = it / n, e = it % n;
-        long long row = row0 + q;
-        if (row < nrows) {
-            float2 c = R[e * ld + (q >> 1)];
-            out[row * n + e] = (q & 1) ? c.y : c.x;
+        const int q = fdiv_i(it, n, invn), e = it - q * n;
+        const long long row = row0 + q;
+        if (row < nrows) out[row * n + e] = Rf[2 * sidx(e, q >> 1, nl) + (q & 1)];
+    }
+    if (delta < 0) return;
+    // y blur: the free ping-pong buffer holds 2 nl rows of n floats
+    float *Bf = reinterpret_cast<float *>(R == L.A ? L.B : L.A);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int seg = (n + 31) / 32;
+    for (int q = warp; q < 2 * nl; q += nw) {
+        const int l = q >> 1, comp = q & 1;
+        const int s0 = lane * seg, s1 = min(s0 + seg, n);
+        if (s0 < n) {
+            int lo = max(s0 - delta, 0), hi = min(s0 + delta, n - 1);
+            float sum = 0.f;
+            for (int i = lo; i <= hi; ++i) sum += Rf[2 * sidx(i, l, nl) + comp];
+            for (int e = s0; e < s1; ++e) {
+                if (e > s0) {
+                    const int add = e + delta, drop = e - delta - 1;
+                    if (add <= n - 1) sum += Rf[2 * sidx(add, l, nl) + comp];
+                    if (drop >= 0) sum -= Rf[2 * sidx(drop, l, nl) + comp];
+                }
+                const int cnt = min(e + delta, n - 1) - max(e - delta, 0) + 1;
+                Bf[q * n + e] = sum / (float)cnt;
+            }
         }
+        __syncwarp();
+        const long long row = row0 + q;
+        if (row < nrows)
+            for (int e = lane; e < n; e += 32) blur[row * n + e] = Bf[q * n + e];
     }
 }
 
 // ---------------------------------------------------------------------------
-// box blur, blur.cu:1-52 semantics: mean over [c-delta, c+delta] clipped to the
-// axis, divided by the in-range count.
+// x blur (box mean along x, blur.cu:1-52 semantics) of `tmp`, subtracted from
+// res; writes the tile result in place and/or the stitched centre
+// (deconvolver.py:160-163, 183).  One CTA = one z plane of one tile and 32
+// consecutive y columns held in shared memory; each warp slides the window
+// down a segment of rows.  delta < 0: no blur (res copied).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kThreads)
-k_blur_y(const float *__restrict__ in, float *__restrict__ out, long long nrows, int P, int delta) {
-    extern __shared__ float rowbuf[];
-    const int rows_per = blockDim.x / 32;
-    const long long row = (long long)blockIdx.x * rows_per + threadIdx.x / 32;
-    const int lane = threadIdx.x % 32;
-    float *r = rowbuf + (threadIdx.x / 32) * P;
-    if (row < nrows)
-        for (int e = lane; e < P; e += 32) r[e] = in[row * P + e];
-    __syncwarp();
-    if (row >= nrows) return;
-    for (int e = lane; e < P; e += 32) {
-        int s = e - delta < 0 ? 0 : e - delta;
-        int t = e + delta > P - 1 ? P - 1 : e + delta;
-        float sum = 0.f;
-        for (int i = s; i <= t; ++i) sum += r[i];
-        out[row * P + e] = sum / (float)(t - s + 1);
-    }
-}
-
-// x blur of tmp, subtracted from res; writes the tile result in place and/or
-// the stitched centre (deconvolver.py:183).  One CTA = one z plane of one tile
-// and 32 consecutive y columns.  delta < 0: no blur (res copied).
 __global__ void __launch_bounds__(kThreads)
 k_blur_x_sub(TileGeom g, const float *__restrict__ res, const float *__restrict__ tmp, int delta,
              float *__restrict__ res_out, float *__restrict__ stitch, long long osz, long long osx) {
-    extern __shared__ float colbuf[];  // P x 33
+    extern __shared__ __align__(16) float colbuf[];  // P x 32
     const int P = g.P;
     const int ti = g.t0 + blockIdx.z;
     const TileDesc d = mm_tile_desc(g, ti);
     const int z = blockIdx.y;
     const int y0 = blockIdx.x * 32;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int y = y0 + lane;
     const long long pbase = ((long long)blockIdx.z * g.Z + z) * P * P;
     if (delta >= 0) {
-        for (int it = threadIdx.x; it < P * 32; it += blockDim.x) {
-            int x = it / 32, c = it % 32;
-            colbuf[x * 33 + c] = (y0 + c < P) ? tmp[pbase + (long long)x * P + y0 + c] : 0.f;
-        }
+        for (int x = warp; x < P; x += nw) colbuf[x * 32 + lane] = (y < P) ? tmp[pbase + (long long)x * P + y] : 0.f;
         __syncthreads();
     }
-    for (int it = threadIdx.x; it < P * 32; it += blockDim.x) {
-        int x = it / 32, c = it % 32;
-        int y = y0 + c;
+    const int seg = (P + nw - 1) / nw;
+    const int x0 = warp * seg, x1 = min(x0 + seg, P);
+    float sum = 0.f;
+    if (delta >= 0 && x0 < P) {
+        const int lo = max(x0 - delta, 0), hi = min(x0 + delta, P - 1);
+        for (int i = lo; i <= hi; ++i) sum += colbuf[i * 32 + lane];
+    }
+    for (int x = x0; x < x1; ++x) {
+        if (delta >= 0 && x > x0) {
+            const int add = x + delta, drop = x - delta - 1;
+            if (add <= P - 1) sum += colbuf[add * 32 + lane];
+            if (drop >= 0) sum -= colbuf[drop * 32 + lane];
+        }
         if (y >= P) continue;
         float v = res[pbase + (long long)x * P + y];
         if (delta >= 0) {
-            int s = x - delta < 0 ? 0 : x - delta;
-            int t = x + delta > P - 1 ? P - 1 : x + delta;
-            float sum = 0.f;
-            for (int i = s; i <= t; ++i) sum += colbuf[i * 33 + c];
-            v = v - sum / (float)(t - s + 1);
+            const int cnt = min(x + delta, P - 1) - max(x - delta, 0) + 1;
+            v = v - sum / (float)cnt;
         }
         if (res_out) res_out[pbase + (long long)x * P + y] = v;
         if (stitch && x >= g.ov && x < d.xend - g.ov && y >= g.ov && y < d.yend - g.ov) {
-            long long ox = d.x + x - g.ov, oy = d.y + y - g.ov;
-            if (ox < g.X && oy < g.Y) stitch[z * osz + ox * osx + oy] = v;
+            const int ox = d.x + x - g.ov, oy = d.y + y - g.ov;
+            // inside its own span a tile is the final writer; past it, ask who is
+            const bool own = ox < d.x + g.ts && oy < d.y + g.ts;
+            if (ox < g.X && oy < g.Y && (own || mm_stitch_owner(g, ox, oy) == ti))
+                stitch[z * osz + (long long)ox * osx + oy] = v;
         }
     }
 }
@@ -354,15 +310,13 @@ int mm_launch_rows_fwd_img(const TileGeom &g, const void *img, int dtype, const 
     int nl = pick_nl(P, 16);
     size_t sm = fft_smem(P, nl);
     dim3 grid(mm_cdiv((long)g.Z * g.P, 2 * nl), g.nt);
-    if (dtype == MM_DTYPE_U16) {
-        if ((rc = set_smem(k_rows_fwd_img<uint16_t>, sm))) return rc;
-        k_rows_fwd_img<uint16_t><<<grid, kThreads, sm, st>>>(g, (const uint16_t *)img, flat, S, P, nl);
-    } else {
-        if ((rc = set_smem(k_rows_fwd_img<float>, sm))) return rc;
-        k_rows_fwd_img<float><<<grid, kThreads, sm, st>>>(g, (const float *)img, flat, S, P, nl);
-    }
-    MM_CHECK_LAUNCH();
-    return MM_OK;
+    TileGeom ga = g;
+    const void *imga = img;
+    const float *fa = flat;
+    void *args[] = {&ga, &imga, &fa, &S, &P, &nl};
+    const void *fn = dtype == MM_DTYPE_U16 ? MM_BY_CLASS(P, k_rows_fwd_img, uint16_t,)
+                                          : MM_BY_CLASS(P, k_rows_fwd_img, float,);
+    return launch_fft_kernel(fn, grid, sm, st, args);
 }
 
 int mm_launch_rows_fwd_f32(const float *vol, int nrows, int Pn, float2 *S, cudaStream_t st) {
@@ -371,80 +325,26 @@ int mm_launch_rows_fwd_f32(const float *vol, int nrows, int Pn, float2 *S, cudaS
     if (rc) return rc;
     int nl = pick_nl(P, 16);
     size_t sm = fft_smem(P, nl);
-    if ((rc = set_smem(k_rows_fwd_f32, sm))) return rc;
-    k_rows_fwd_f32<<<mm_cdiv(nrows, 2 * nl), kThreads, sm, st>>>(vol, nrows, S, P, nl);
-    MM_CHECK_LAUNCH();
-    return MM_OK;
+    long long nr = nrows;
+    void *args[] = {&vol, &nr, &S, &P, &nl};
+    return launch_fft_kernel(MM_BY_CLASS(P, k_rows_fwd_f32, ), dim3(mm_cdiv(nrows, 2 * nl)), sm, st, args);
 }
 
-int mm_launch_cols(float2 *S, int n, long long se, int nlines, long long plane_stride, int nplanes, bool inv,
-                   cudaStream_t st) {
-    FftPlan P;
-    int rc = mm_fft_plan_get(n, &P);
-    if (rc) return rc;
-    int nl = pick_nl(P, 16);
-    size_t sm = fft_smem(P, nl);
-    dim3 grid(mm_cdiv(nlines, nl), nplanes);
-    if (inv) {
-        if ((rc = set_smem(k_cols<true>, sm))) return rc;
-        k_cols<true><<<grid, kThreads, sm, st>>>(S, se, nlines, plane_stride, P, nl);
-    } else {
-        if ((rc = set_smem(k_cols<false>, sm))) return rc;
-        k_cols<false><<<grid, kThreads, sm, st>>>(S, se, nlines, plane_stride, P, nl);
-    }
-    MM_CHECK_LAUNCH();
-    return MM_OK;
-}
-
-int mm_launch_zpass(const TileGeom &g, float2 *S, const float2 *W, long long wstride, cudaStream_t st) {
-    FftPlan P;
-    int rc = mm_fft_plan_get(g.Zp, &P);
-    if (rc) return rc;
-    int nl = pick_nl(P, 32);
-    size_t sm = fft_smem(P, nl);
-    if ((rc = set_smem(k_zpass, sm))) return rc;
-    dim3 grid(mm_cdiv((long)g.P * g.H, nl), g.nt);
-    k_zpass<<<grid, kThreads, sm, st>>>(g, S, W, wstride, P, nl);
-    MM_CHECK_LAUNCH();
-    return MM_OK;
-}
-
-int mm_launch_zfwd(float2 *S, int Zp, int plane, cudaStream_t st) {
-    FftPlan P;
-    int rc = mm_fft_plan_get(Zp, &P);
-    if (rc) return rc;
-    int nl = pick_nl(P, 32);
-    size_t sm = fft_smem(P, nl);
-    if ((rc = set_smem(k_zfwd, sm))) return rc;
-    k_zfwd<<<mm_cdiv(plane, nl), kThreads, sm, st>>>(S, plane, P, nl);
-    MM_CHECK_LAUNCH();
-    return MM_OK;
-}
-
-int mm_launch_rows_inv(const float2 *S, int nrows, int Pn, int H, float *out, cudaStream_t st) {
+int mm_launch_rows_inv(const float2 *S, int nrows, int Pn, int H, float *out, float *blur, int delta,
+                       cudaStream_t st) {
     FftPlan P;
     int rc = mm_fft_plan_get(Pn, &P);
     if (rc) return rc;
     int nl = pick_nl(P, 16);
     size_t sm = fft_smem(P, nl);
-    if ((rc = set_smem(k_rows_inv, sm))) return rc;
-    k_rows_inv<<<mm_cdiv(nrows, 2 * nl), kThreads, sm, st>>>(S, nrows, H, out, P, nl);
-    MM_CHECK_LAUNCH();
-    return MM_OK;
-}
-
-int mm_launch_blur_y(const float *in, float *out, int nrows, int P, int delta, cudaStream_t st) {
-    size_t sm = (size_t)(kThreads / 32) * P * sizeof(float);
-    int rc;
-    if ((rc = set_smem(k_blur_y, sm))) return rc;
-    k_blur_y<<<mm_cdiv(nrows, kThreads / 32), kThreads, sm, st>>>(in, out, nrows, P, delta);
-    MM_CHECK_LAUNCH();
-    return MM_OK;
+    long long nr = nrows;
+    void *args[] = {&S, &nr, &H, &out, &blur, &delta, &P, &nl};
+    return launch_fft_kernel(MM_BY_CLASS(P, k_rows_inv, ), dim3(mm_cdiv(nrows, 2 * nl)), sm, st, args);
 }
 
 int mm_launch_blur_x_sub(const TileGeom &g, const float *res, const float *tmp, int delta, float *res_out,
                          float *stitch, long long osz, long long osx, cudaStream_t st) {
-    size_t sm = delta >= 0 ? (size_t)g.P * 33 * sizeof(float) : 0;
+    size_t sm = delta >= 0 ? (size_t)g.P * 32 * sizeof(float) : 0;
     int rc;
     if ((rc = set_smem(k_blur_x_sub, sm > 0 ? sm : 1))) return rc;
     dim3 grid(mm_cdiv(g.P, 32), g.Z, g.nt);

@@ -13,6 +13,7 @@ struct TileGeom {
     int ny;               // tiles along y
     int t0, nt;           // first tile and tile count of this launch
     int npsf;             // number of Wiener spectra (1 = shared)
+    int ntot;             // tiles the whole call processes (zip-truncated when npsf > 1)
 };
 
 struct TileDesc {
@@ -41,6 +42,28 @@ __device__ __host__ inline TileDesc mm_tile_desc(const TileGeom &g, int ti) {
     d.yend = d.yd + ((d.y == 0 || d.yd < g.P) ? g.ov : 0);
     d.psf = g.npsf == 1 ? 0 : ti;
     return d;
+}
+
+// Deconvolver.apply (deconvolver.py:179-183) writes tile centres in x-major
+// order, each over [x, x + xend - 2 ov) x [y, y + yend - 2 ov).  A truncated
+// second-to-last tile reaches past its own span into the last tile's, which
+// overwrites it later.  So the value that survives at an output pixel is the
+// one of the last tile (in order) whose span covers it: the tile (ox / ts,
+// oy / ts) when that tile is processed, else the latest covering predecessor
+// (only the tile just before the owner along an axis can reach past its span).
+__device__ __host__ inline int mm_stitch_owner(const TileGeom &g, int ox, int oy) {
+    const int ix = ox / g.ts, iy = oy / g.ts;
+    const int own = ix * g.ny + iy;
+    if (own < g.ntot) return own;
+    int best = -1;
+    for (int cx = ix; cx >= ix - 1 && cx >= 0; --cx)
+        for (int cy = iy; cy >= iy - 1 && cy >= 0; --cy) {
+            const int t = cx * g.ny + cy;
+            if (t >= g.ntot || t <= best) continue;
+            const TileDesc d = mm_tile_desc(g, t);
+            if (ox >= d.x && ox < d.x + d.xend - 2 * g.ov && oy >= d.y && oy < d.y + d.yend - 2 * g.ov) best = t;
+        }
+    return best;
 }
 
 // Padded index -> source index inside the tile, or -1 for a zero.  Restates
@@ -93,8 +116,8 @@ int mm_launch_cols(float2 *S, int n, long long se, int nlines, long long plane_s
                    bool inv, cudaStream_t st);
 int mm_launch_zpass(const TileGeom &g, float2 *S, const float2 *W, long long wstride, cudaStream_t st);
 int mm_launch_zfwd(float2 *S, int Zp, int plane, cudaStream_t st);
-int mm_launch_rows_inv(const float2 *S, int nrows, int P, int H, float *out, cudaStream_t st);
-int mm_launch_blur_y(const float *in, float *out, int nrows, int P, int delta, cudaStream_t st);
+int mm_launch_rows_inv(const float2 *S, int nrows, int P, int H, float *out, float *blur, int delta,
+                       cudaStream_t st);
 int mm_launch_blur_x_sub(const TileGeom &g, const float *res, const float *tmp, int delta,
                          float *res_out, float *stitch, long long osz, long long osx, cudaStream_t st);
 int mm_launch_make_raw(const TileGeom &g, const void *img, int dtype, const float *flat, float *raw,

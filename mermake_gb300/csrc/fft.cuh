@@ -3,15 +3,27 @@
 // The deconvolution needs transforms at the exact padded tile lengths of the
 // reference (deconvolver.py:86-90, 155-157), which carry large prime factors
 // (678 = 2*3*113, 478 = 2*239, 148 = 4*37, 118 = 2*59, ...).  A length is
-// factored into radix-2/3/4/5/7 stages, computed in registers, and "generic"
-// odd-prime stages, computed as a direct DFT that pairs x[r] with x[R-r] (half
-// the multiplies of a plain DFT).  The generic stages run first, where the
-// Stockham twiddles are all 1.
+// factored into stages of three kinds:
+//   * radix 2/3/4/5/7 and the odd primes 11, 13, 17: one thread per butterfly,
+//     values in registers;
+//   * primes 19..61, 79, 89 and 113 ("lane" stage; the primes of the
+//     reference's padded lengths 2*Z-1+... and 678 = 2*3*113, plus every prime
+//     up to 61): one warp per butterfly and one lane per
+//     output pair (k, R-k); each lane keeps its column of the DFT matrix in
+//     registers for the whole stage, and the warp reads the paired inputs
+//     a_r = x_r + x_{R-r}, b_r = x_r - x_{R-r} as shared-memory broadcasts
+//     (one 16-byte load per 4 FMAs);
+//   * any other prime: a direct DFT with table look-ups ("generic" stage).
+// The lane and generic stages pair x[r] with x[R-r], halving the multiplies of a
+// plain DFT, and run first, where the Stockham twiddles are all 1.
 //
-// Layout: a CTA holds `nl` lines; element e of line l is at s[e*ld + l]
-// ("column" layout, ld = nl + 1 to break bank conflicts on row loads).  Each
-// stage reads one buffer and writes the other (ping-pong), so a kernel gives
-// two buffers of n*ld float2 each.  Twiddles exp(-2*pi*i*m/n) are computed on
+// Layout: a CTA holds `nl` lines (a power of two); element e of line l is at
+// s[sidx(e, l, nl)] = s[e*nl + (l ^ (e & (nl-1)))]: lines are interleaved
+// ("column" layout, so a half warp reads one element of 16 lines as 128
+// contiguous bytes), and the XOR swizzle spreads the strided accesses of the
+// row loads and of the lane stages over the banks.  Each stage reads one buffer
+// and writes the other (ping-pong), so a kernel gives two buffers of n*nl
+// float2 each.  Twiddles exp(-2*pi*i*m/n) are computed on
 // the host in double precision and rounded once to float.
 #pragma once
 #include "mm_common.cuh"
@@ -22,6 +34,7 @@
 struct FftPlan {
     int n;
     int nst;
+    int lclass;               // 0, 63 or 127: largest lane-stage prime class (fft_lines<., LMAX>)
     int rad[MM_FFT_MAXST];
     int ns[MM_FFT_MAXST];     // product of the radices of the earlier stages
     int ptab[MM_FFT_MAXST];   // generic stage: offset of its cos/sin table in `tab`
@@ -29,6 +42,20 @@ struct FftPlan {
     const float2 *tw;         // device, n entries: exp(-2 pi i m / n)
     const float2 *tab;        // device, per generic stage R entries: exp(-2 pi i m / R)
 };
+
+// element e of line l in a CTA's line buffer (see the layout note above)
+__device__ __forceinline__ int sidx(int e, int l, int nl) { return e * nl + (l ^ (e & (nl - 1))); }
+
+// a / d for 0 <= a < 2^24 through the float reciprocal inv = 1/d, corrected to
+// the exact quotient (integer division by a run-time divisor costs ~20
+// instructions; this is 6)
+__device__ __forceinline__ int fdiv_i(int a, int d, float inv) {
+    int q = __float2int_rz(__int2float_rn(a) * inv);
+    const int r = a - q * d;
+    q += (r >= d) - (r < 0);
+    return q;
+}
+__device__ __forceinline__ int log2_pow2(int nl) { return __ffs(nl) - 1; }
 
 // ---- small radices, all values in registers ------------------------------
 template <bool INV>
@@ -145,19 +172,194 @@ __device__ __forceinline__ void dft_small<7, false>(float2 *v) { dft_odd<7, fals
 template <>
 __device__ __forceinline__ void dft_small<7, true>(float2 *v) { dft_odd<7, true>(v); }
 
+// Odd radix 11, 13, 17 in registers, cos/sin loaded once per stage from the plan table.
 template <int R, bool INV>
-__device__ __forceinline__ void stage_small(const float2 *__restrict__ src, float2 *__restrict__ dst,
-                                            int n, int ld, int nl, int Ns, const float2 *tw) {
+__device__ __forceinline__ void dft_odd_tab(float2 *v, const float *c, const float *sn) {
+    constexpr int H = (R - 1) / 2;
+    float2 a[H], b[H];
+#pragma unroll
+    for (int r = 1; r <= H; ++r) {
+        a[r - 1] = cadd(v[r], v[R - r]);
+        b[r - 1] = csub(v[r], v[R - r]);
+    }
+    float2 x0 = v[0];
+    float2 s0 = x0;
+#pragma unroll
+    for (int r = 0; r < H; ++r) s0 = cadd(s0, a[r]);
+#pragma unroll
+    for (int k = 1; k <= H; ++k) {
+        float ax = x0.x, ay = x0.y, bx = 0.f, by = 0.f;
+#pragma unroll
+        for (int r = 1; r <= H; ++r) {
+            const int m = (r * k) % R;
+            const float cc = m <= H ? c[m] : c[R - m];
+            const float ss = m <= H ? sn[m] : -sn[R - m];
+            ax += a[r - 1].x * cc;
+            ay += a[r - 1].y * cc;
+            bx += b[r - 1].x * ss;
+            by += b[r - 1].y * ss;
+        }
+        if (!INV) {
+            v[k] = make_float2(ax + by, ay - bx);
+            v[R - k] = make_float2(ax - by, ay + bx);
+        } else {
+            v[k] = make_float2(ax - by, ay + bx);
+            v[R - k] = make_float2(ax + by, ay - bx);
+        }
+    }
+    v[0] = s0;
+}
+
+template <int R, bool INV>
+__device__ __noinline__ void stage_odd_tab(const float2 *__restrict__ src, float2 *__restrict__ dst, int n,
+                                           int nl, int Ns, const float2 *tw, const float2 *cs) {
+    constexpr int H = (R - 1) / 2;
+    float c[H + 1], sn[H + 1];
+#pragma unroll
+    for (int m = 0; m <= H; ++m) {
+        c[m] = cs[m].x;
+        sn[m] = -cs[m].y;  // table holds (cos, -sin)
+    }
     const int m = n / R;
     const int tstep = n / (Ns * R);
     const int items = m * nl;
+    const int lnl = log2_pow2(nl);
+    const float invNs = 1.0f / (float)Ns;
     for (int it = threadIdx.x; it < items; it += blockDim.x) {
-        int l = it % nl;
-        int j = it / nl;
-        int k = j % Ns;
+        const int l = it & (nl - 1);
+        const int j = it >> lnl;
+        const int k = j - fdiv_i(j, Ns, invNs) * Ns;
         float2 v[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = src[(j + r * m) * ld + l];
+        for (int r = 0; r < R; ++r) v[r] = src[sidx(j + r * m, l, nl)];
+        if (Ns > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                float2 w = tw[k * r * tstep];
+                v[r] = INV ? cmulc(v[r], w) : cmul(v[r], w);
+            }
+        }
+        dft_odd_tab<R, INV>(v, c, sn);
+        int d = (j - k) * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) dst[sidx(d + r * Ns, l, nl)] = v[r];
+    }
+}
+
+// Lane stage (primes 19..113, see top): warp per butterfly, lane per output pair.
+// Each warp takes two butterflies per iteration (eight independent FMA
+// chains).  scr: MM_FFT_SCR_PER_WARP float4 of shared scratch per warp.
+#define MM_FFT_SCR_PER_WARP 128
+template <int R, bool INV>
+__device__ __noinline__ void stage_lane(const float2 *__restrict__ src, float2 *__restrict__ dst, int n,
+                                        int nl, int Ns, const float2 *__restrict__ tw,
+                                        const float2 *__restrict__ cs, float4 *__restrict__ scr_all) {
+    constexpr int H = (R - 1) / 2;
+    constexpr int G = (H + 31) / 32;  // warps per butterfly
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    const int g = warp % G, strm = warp / G, nstrm = nw / G;
+    if (strm >= nstrm) return;
+    float4 *scr = scr_all + warp * MM_FFT_SCR_PER_WARP;
+    const int k = g * 32 + lane + 1;
+    const bool kv = k <= H;
+    float cr[H], sr[H];
+#pragma unroll
+    for (int r = 1; r <= H; ++r) {
+        const float2 w = cs[kv ? (r * k) % R : 0];  // (cos, -sin) of 2 pi r k / R
+        cr[r - 1] = w.x;
+        sr[r - 1] = w.y;
+    }
+    const int m = n / R;
+    const int tstep = n / (Ns * R);
+    const int nb = m * nl;
+    const int lnl = log2_pow2(nl);
+    const float invNs = 1.0f / (float)Ns;
+    for (int b0 = strm; b0 < nb; b0 += 2 * nstrm) {
+        const bool two = b0 + nstrm < nb;
+        float2 x0[2];
+        float sx[2], sy[2];
+        int dd[2], ll[2];
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int bf = q ? (two ? b0 + nstrm : b0) : b0;
+            const int l = bf & (nl - 1), j = bf >> lnl, kk = j - fdiv_i(j, Ns, invNs) * Ns;
+            ll[q] = l;
+            dd[q] = (j - kk) * R + kk;
+            x0[q] = src[sidx(j, l, nl)];
+            sx[q] = 0.f;
+            sy[q] = 0.f;
+            for (int r = lane + 1; r <= H; r += 32) {
+                float2 u = src[sidx(j + r * m, l, nl)], v = src[sidx(j + (R - r) * m, l, nl)];
+                if (Ns > 1) {
+                    const float2 wu = tw[kk * r * tstep], wv = tw[kk * (R - r) * tstep];
+                    u = INV ? cmulc(u, wu) : cmul(u, wu);
+                    v = INV ? cmulc(v, wv) : cmul(v, wv);
+                }
+                const float4 t = make_float4(u.x + v.x, u.y + v.y, u.x - v.x, u.y - v.y);
+                scr[q * 64 + r - 1] = t;
+                sx[q] += t.x;
+                sy[q] += t.y;
+            }
+        }
+        __syncwarp();
+        float ax0 = x0[0].x, ay0 = x0[0].y, bx0 = 0.f, by0 = 0.f;
+        float ax1 = x0[1].x, ay1 = x0[1].y, bx1 = 0.f, by1 = 0.f;
+#pragma unroll
+        for (int r = 0; r < H; ++r) {
+            const float4 t0 = scr[r], t1 = scr[64 + r];
+            ax0 += t0.x * cr[r];
+            ay0 += t0.y * cr[r];
+            bx0 += t0.z * sr[r];
+            by0 += t0.w * sr[r];
+            ax1 += t1.x * cr[r];
+            ay1 += t1.y * cr[r];
+            bx1 += t1.z * sr[r];
+            by1 += t1.w * sr[r];
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            if (q == 1 && !two) break;
+            const float ax = q ? ax1 : ax0, ay = q ? ay1 : ay0, bx = q ? bx1 : bx0, by = q ? by1 : by0;
+            if (kv) {
+                float2 o1, o2;
+                if (!INV) {
+                    o1 = make_float2(ax - by, ay + bx);
+                    o2 = make_float2(ax + by, ay - bx);
+                } else {
+                    o1 = make_float2(ax + by, ay - bx);
+                    o2 = make_float2(ax - by, ay + bx);
+                }
+                dst[sidx(dd[q] + k * Ns, ll[q], nl)] = o1;
+                dst[sidx(dd[q] + (R - k) * Ns, ll[q], nl)] = o2;
+            }
+            if (g == 0) {
+                float tx = sx[q], ty = sy[q];
+                for (int o = 16; o > 0; o >>= 1) {
+                    tx += __shfl_xor_sync(0xffffffffu, tx, o);
+                    ty += __shfl_xor_sync(0xffffffffu, ty, o);
+                }
+                if (lane == 0) dst[sidx(dd[q], ll[q], nl)] = make_float2(x0[q].x + tx, x0[q].y + ty);
+            }
+        }
+        __syncwarp();
+    }
+}
+
+template <int R, bool INV>
+__device__ __forceinline__ void stage_small(const float2 *__restrict__ src, float2 *__restrict__ dst,
+                                            int n, int nl, int Ns, const float2 *tw) {
+    const int m = n / R;
+    const int tstep = n / (Ns * R);
+    const int items = m * nl;
+    const int lnl = log2_pow2(nl);
+    const float invNs = 1.0f / (float)Ns;
+    for (int it = threadIdx.x; it < items; it += blockDim.x) {
+        const int l = it & (nl - 1);
+        const int j = it >> lnl;
+        const int k = j - fdiv_i(j, Ns, invNs) * Ns;
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = src[sidx(j + r * m, l, nl)];
         if (Ns > 1) {
 #pragma unroll
             for (int r = 1; r < R; ++r) {
@@ -168,7 +370,7 @@ __device__ __forceinline__ void stage_small(const float2 *__restrict__ src, floa
         dft_small<R, INV>(v);
         int d = (j - k) * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) dst[(d + r * Ns) * ld + l] = v[r];
+        for (int r = 0; r < R; ++r) dst[sidx(d + r * Ns, l, nl)] = v[r];
     }
 }
 
@@ -176,7 +378,7 @@ __device__ __forceinline__ void stage_small(const float2 *__restrict__ src, floa
 // the Stockham twiddles in place; phase 2 has one work item per (line,
 // butterfly, output pair k / R-k) and loops over the R inputs.
 template <bool INV>
-__device__ void stage_generic(float2 *__restrict__ src, float2 *__restrict__ dst, int n, int ld,
+__device__ void stage_generic(float2 *__restrict__ src, float2 *__restrict__ dst, int n,
                               int nl, int R, int Ns, const float2 *tw, const float2 *cs) {
     const int m = n / R;
     const int tstep = n / (Ns * R);
@@ -187,8 +389,8 @@ __device__ void stage_generic(float2 *__restrict__ src, float2 *__restrict__ dst
             int j = e % m, r = e / m;
             if (r == 0) continue;
             float2 w = tw[(j % Ns) * r * tstep];
-            float2 x = src[e * ld + l];
-            src[e * ld + l] = INV ? cmulc(x, w) : cmul(x, w);
+            float2 x = src[sidx(e, l, nl)];
+            src[sidx(e, l, nl)] = INV ? cmulc(x, w) : cmul(x, w);
         }
         __syncthreads();
     }
@@ -201,17 +403,15 @@ __device__ void stage_generic(float2 *__restrict__ src, float2 *__restrict__ dst
         int j = rest / (H + 1);
         int kk = j % Ns;
         int d = (j - kk) * R + kk;
-        const float2 *x = src + j * ld + l;
-        const int xs = m * ld;
-        float2 x0 = x[0];
+        float2 x0 = src[sidx(j, l, nl)];
         if (k == 0) {
             float sx = x0.x, sy = x0.y;
             for (int r = 1; r < R; ++r) {
-                float2 t = x[r * xs];
+                float2 t = src[sidx(j + r * m, l, nl)];
                 sx += t.x;
                 sy += t.y;
             }
-            dst[d * ld + l] = make_float2(sx, sy);
+            dst[sidx(d, l, nl)] = make_float2(sx, sy);
             continue;
         }
         float ax = x0.x, ay = x0.y, bx = 0.f, by = 0.f;
@@ -220,7 +420,7 @@ __device__ void stage_generic(float2 *__restrict__ src, float2 *__restrict__ dst
             mi += k;
             if (mi >= R) mi -= R;
             float2 w = cs[mi];  // (cos, -sin) of 2 pi mi / R
-            float2 u = x[r * xs], v = x[(R - r) * xs];
+            float2 u = src[sidx(j + r * m, l, nl)], v = src[sidx(j + (R - r) * m, l, nl)];
             ax += (u.x + v.x) * w.x;
             ay += (u.y + v.y) * w.x;
             bx += (u.x - v.x) * w.y;
@@ -235,25 +435,42 @@ __device__ void stage_generic(float2 *__restrict__ src, float2 *__restrict__ dst
             o1 = make_float2(ax + by, ay - bx);
             o2 = make_float2(ax - by, ay + bx);
         }
-        dst[(d + k * Ns) * ld + l] = o1;
-        dst[(d + (R - k) * Ns) * ld + l] = o2;
+        dst[sidx(d + k * Ns, l, nl)] = o1;
+        dst[sidx(d + (R - k) * Ns, l, nl)] = o2;
     }
 }
 
 // Runs the whole plan on nl lines.  Returns the buffer holding the result.
-template <bool INV>
-__device__ float2 *fft_lines(float2 *A, float2 *B, int ld, int nl, const FftPlan &P,
-                             const float2 *tw_s, const float2 *tab_s) {
+#define MM_LANE_CASE(R)                                                                        \
+    case R:                                                                                    \
+        if constexpr (R <= LMAX)                                                               \
+            stage_lane<R, INV>(src, dst, P.n, nl, Ns, tw_s, tab_s + P.ptab[st], scr);          \
+        else                                                                                   \
+            stage_generic<INV>(src, dst, P.n, nl, R, Ns, tw_s, tab_s + P.ptab[st]);            \
+        break;
+#define MM_ODD_CASE(R) \
+    case R: stage_odd_tab<R, INV>(src, dst, P.n, nl, Ns, tw_s, tab_s + P.ptab[st]); break;
+
+// LMAX: the largest prime given a lane stage in this instantiation (0, 63 or
+// 127; the host picks the class of the plan, mm_fft_lane_class), so that
+// kernels whose lengths only need small lane stages keep fewer registers.
+template <bool INV, int LMAX>
+__device__ float2 *fft_lines(float2 *A, float2 *B, int nl, const FftPlan &P,
+                             const float2 *tw_s, const float2 *tab_s, float4 *scr) {
     float2 *src = A, *dst = B;
     for (int st = 0; st < P.nst; ++st) {
         const int R = P.rad[st], Ns = P.ns[st];
         switch (R) {
-            case 2: stage_small<2, INV>(src, dst, P.n, ld, nl, Ns, tw_s); break;
-            case 3: stage_small<3, INV>(src, dst, P.n, ld, nl, Ns, tw_s); break;
-            case 4: stage_small<4, INV>(src, dst, P.n, ld, nl, Ns, tw_s); break;
-            case 5: stage_small<5, INV>(src, dst, P.n, ld, nl, Ns, tw_s); break;
-            case 7: stage_small<7, INV>(src, dst, P.n, ld, nl, Ns, tw_s); break;
-            default: stage_generic<INV>(src, dst, P.n, ld, nl, R, Ns, tw_s, tab_s + P.ptab[st]); break;
+            case 2: stage_small<2, INV>(src, dst, P.n, nl, Ns, tw_s); break;
+            case 3: stage_small<3, INV>(src, dst, P.n, nl, Ns, tw_s); break;
+            case 4: stage_small<4, INV>(src, dst, P.n, nl, Ns, tw_s); break;
+            case 5: stage_small<5, INV>(src, dst, P.n, nl, Ns, tw_s); break;
+            case 7: stage_small<7, INV>(src, dst, P.n, nl, Ns, tw_s); break;
+            MM_ODD_CASE(11) MM_ODD_CASE(13) MM_ODD_CASE(17)
+            MM_LANE_CASE(19) MM_LANE_CASE(23) MM_LANE_CASE(29) MM_LANE_CASE(31) MM_LANE_CASE(37)
+            MM_LANE_CASE(41) MM_LANE_CASE(43) MM_LANE_CASE(47) MM_LANE_CASE(53) MM_LANE_CASE(59)
+            MM_LANE_CASE(61) MM_LANE_CASE(79) MM_LANE_CASE(89) MM_LANE_CASE(113)
+            default: stage_generic<INV>(src, dst, P.n, nl, R, Ns, tw_s, tab_s + P.ptab[st]); break;
         }
         __syncthreads();
         float2 *t = src;
@@ -263,11 +480,69 @@ __device__ float2 *fft_lines(float2 *A, float2 *B, int ld, int nl, const FftPlan
     return src;
 }
 
+// Shared-memory layout of an FFT kernel: ping-pong line buffers A and B
+// (n * nl float2 each), the twiddle table (n), the radix tables (ntab),
+// then MM_FFT_SCR_PER_WARP float4 of scratch per warp for the lane stages
+// (16-byte aligned).
+struct FftSmem {
+    float2 *A, *B, *tw, *tab;
+    float4 *scr;
+};
+__device__ __host__ inline size_t fft_smem_bytes(int n, int ntab, int nl, int nwarps) {
+    size_t b = sizeof(float2) * ((size_t)2 * n * nl + n + ntab);
+    b = (b + 15) & ~(size_t)15;
+    return b + sizeof(float4) * MM_FFT_SCR_PER_WARP * nwarps;
+}
+__device__ inline FftSmem fft_smem_layout(void *base, const FftPlan &P, int nl) {
+    FftSmem L;
+    L.A = (float2 *)base;
+    L.B = L.A + P.n * nl;
+    L.tw = L.B + P.n * nl;
+    L.tab = L.tw + P.n;
+    size_t off = sizeof(float2) * ((size_t)2 * P.n * nl + P.n + P.ntab);
+    off = (off + 15) & ~(size_t)15;
+    L.scr = (float4 *)((char *)base + off);
+    return L;
+}
+
 // Copies the plan tables into shared memory (call by all threads, then sync).
 __device__ __forceinline__ void fft_load_tables(const FftPlan &P, float2 *tw_s, float2 *tab_s) {
     for (int i = threadIdx.x; i < P.n; i += blockDim.x) tw_s[i] = P.tw[i];
     for (int i = threadIdx.x; i < P.ntab; i += blockDim.x) tab_s[i] = P.tab[i];
 }
 
+// cp.async helpers: global -> shared copies without register staging, so a
+// thread keeps many loads in flight.
+__device__ __forceinline__ void cp_async8(void *smem_dst, const void *gsrc) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // Host side: plan cache (fft_plan.cu).
 int mm_fft_plan_get(int n, FftPlan *out);
+
+// ---- launch helpers shared by the FFT kernel translation units -------------
+constexpr int kFftThreads = 256;
+constexpr int kFftSmemLimit = 200 * 1024;
+
+static inline size_t fft_smem(const FftPlan &P, int nl) {
+    return fft_smem_bytes(P.n, P.ntab, nl, kFftThreads / 32);
+}
+// Lines per CTA: the largest power of two <= maxnl whose buffers fit the budget.
+static inline int pick_nl(const FftPlan &P, int maxnl) {
+    int nl = maxnl;
+    while (nl > 1 && fft_smem(P, nl) > (size_t)kFftSmemLimit) nl >>= 1;
+    return nl;
+}
+// Pointer to the kernel template instantiation of the plan's lane class.
+#define MM_BY_CLASS(P, KERNEL_TMPL, ...)                                    \
+    ((P).lclass == 0 ? (const void *)KERNEL_TMPL<__VA_ARGS__ 0>             \
+     : (P).lclass == 63 ? (const void *)KERNEL_TMPL<__VA_ARGS__ 63>         \
+                        : (const void *)KERNEL_TMPL<__VA_ARGS__ 127>)
+static inline int launch_fft_kernel(const void *fn, dim3 grid, size_t sm, cudaStream_t st, void **args) {
+    MM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    MM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(kFftThreads), args, sm, st));
+    mm_launch_counter_add();
+    return MM_OK;
+}

@@ -1,0 +1,53 @@
+// x pass of the tiled deconvolution, and the engine's general strided
+// transform: in-place complex FFT along a strided axis (forward or inverse).
+#include "deconv.cuh"
+
+namespace {
+constexpr int kThreads = kFftThreads;
+constexpr int kSmemLimit = kFftSmemLimit;
+
+// ---------------------------------------------------------------------------
+// strided complex FFT, in place: line l of plane p starts at S + p*plane_stride + l,
+// element e at + e*se.  Lines are contiguous, so a CTA's loads are runs of nl,
+// staged into shared memory with cp.async.
+// ---------------------------------------------------------------------------
+template <bool INV, int LMAX>
+__global__ void __launch_bounds__(kThreads)
+k_cols(float2 *__restrict__ S, long long se, int nlines, long long plane_stride, FftPlan P, int nl) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int n = P.n, lnl = log2_pow2(nl);
+    const FftSmem L = fft_smem_layout(smem_raw, P, nl);
+    fft_load_tables(P, L.tw, L.tab);
+    float2 *base = S + (long long)blockIdx.y * plane_stride;
+    const int l0 = blockIdx.x * nl;
+    for (int it = threadIdx.x; it < nl * n; it += blockDim.x) {
+        const int l = it & (nl - 1), e = it >> lnl;
+        if (l0 + l < nlines)
+            cp_async8(&L.A[sidx(e, l, nl)], &base[e * se + l0 + l]);
+        else
+            L.A[sidx(e, l, nl)] = make_float2(0.f, 0.f);
+    }
+    cp_async_wait_all();
+    __syncthreads();
+    float2 *R = fft_lines<INV, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
+    for (int it = threadIdx.x; it < nl * n; it += blockDim.x) {
+        const int l = it & (nl - 1), e = it >> lnl;
+        if (l0 + l < nlines) base[e * se + l0 + l] = R[sidx(e, l, nl)];
+    }
+}
+
+}  // namespace
+
+int mm_launch_cols(float2 *S, int n, long long se, int nlines, long long plane_stride, int nplanes, bool inv,
+                   cudaStream_t st) {
+    FftPlan P;
+    int rc = mm_fft_plan_get(n, &P);
+    if (rc) return rc;
+    int nl = pick_nl(P, 16);
+    size_t sm = fft_smem(P, nl);
+    dim3 grid(mm_cdiv(nlines, nl), nplanes);
+    void *args[] = {&S, &se, &nlines, &plane_stride, &P, &nl};
+    const void *fn = inv ? MM_BY_CLASS(P, k_cols, true,) : MM_BY_CLASS(P, k_cols, false,);
+    return launch_fft_kernel(fn, grid, sm, st, args);
+}
+

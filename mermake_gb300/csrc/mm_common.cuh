@@ -17,6 +17,7 @@
 
 #define MM_CHECK_LAUNCH()                                                   \
     do {                                                                    \
+        mm_launch_counter_add();                                            \
         cudaError_t _e = cudaGetLastError();                                \
         if (_e != cudaSuccess) {                                            \
             mm_set_error("%s:%d launch: %s", __FILE__, __LINE__,             \
@@ -35,6 +36,9 @@
 
 // Records a message for mm_last_error() (thread-local).
 void mm_set_error(const char *fmt, ...);
+// Counts kernel launches made by this library (mm_launch_count()).
+void mm_launch_counter_add();
+unsigned long long mm_launch_counter_get();
 
 static inline int mm_cdiv(long a, long b) { return (int)((a + b - 1) / b); }
 

@@ -173,3 +173,20 @@ def sort_rows(Xh):
     if len(Xh) == 0:
         return Xh
     return Xh[np.lexsort((Xh[:, 2], Xh[:, 1], Xh[:, 0]))]
+
+
+def match_rows(got, want, tol=1e-2):
+    """Pairs the rows of two Xh arrays one to one by nearest centroid (the
+    row order of either side is arbitrary, and sorting by float centroids
+    misaligns rows whose coordinates differ in the last bits).  Returns the
+    paired (got, want); raises AssertionError if the sets differ."""
+    from scipy.spatial import cKDTree
+    got = np.asarray(got)
+    want = np.asarray(want)
+    assert got.shape == want.shape, (got.shape, want.shape)
+    if len(got) == 0:
+        return got, want
+    d, idx = cKDTree(want[:, :3].astype(np.float64)).query(got[:, :3].astype(np.float64))
+    assert np.all(d <= tol), float(d.max())
+    assert len(np.unique(idx)) == len(idx), "rows do not pair one to one"
+    return got, want[idx]
