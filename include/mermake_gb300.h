@@ -110,6 +110,24 @@ int mm_find_local_maxima(mm_ctx *ctx, const float *image, int Z, int X, int Y, i
                          int delta_fit, float sigmaZ, float sigmaXY, float norm_div, int negate, float *out,
                          uint32_t out_cap, uint32_t *count, void *stream);
 
+/* find_local_maxima for callers that cannot allocate device memory while they
+ * run (code inside another framework's memory pool or under a fixed memory
+ * budget, real-time loops that must not take cudaMalloc's implicit device
+ * synchronisation).  No counterpart in the reference: it is
+ * mm_find_local_maxima with the candidate list held in a static device array
+ * of the library instead of context scratch, so it takes no mm_ctx and calls
+ * no allocating routine.  Same arguments and results as mm_find_local_maxima;
+ * the caller still owns image, raw, out and count.  Limit: Z*X*Y <= 2,097,152
+ * voxels (MM_EINVAL beyond); the array (16 MiB) is held by every GPU that
+ * loads the library until the process exits.  The first call on a device
+ * looks the array up (cudaGetSymbolAddress) and initialises a table, so make
+ * it before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race and must be serialised by the caller. */
+int mm_find_local_maxima_noalloc(const float *image, int Z, int X, int Y, int64_t isz, int64_t isx,
+                                 const void *raw, int raw_dtype, int64_t rsz, int64_t rsx, float threshold,
+                                 int delta, int delta_fit, float sigmaZ, float sigmaXY, float norm_div, int negate,
+                                 float *out, uint32_t out_cap, uint32_t *count, void *stream);
+
 /* One hyb colour (mermake/__main__.py:242-265): tile_wise over every tile,
  * find_local_maxima on each yielded tile with its raw view, keep rows with
  * overlap <= xc, yc < extent - overlap, shift by the tile origin, concatenate.

@@ -53,6 +53,8 @@ _SIGS = {
                         + [_vp, _vp, _vp, _i64, _i64, _vp], _i32),
     "mm_find_local_maxima": ([_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i32, _i64, _i64, _f32, _i32, _i32,
                               _f32, _f32, _f32, _i32, _vp, _u32, _pu32, _vp], _i32),
+    "mm_find_local_maxima_noalloc": ([_vp, _i32, _i32, _i32, _i64, _i64, _vp, _i32, _i64, _i64, _f32, _i32, _i32,
+                                      _f32, _f32, _f32, _i32, _vp, _u32, _pu32, _vp], _i32),
     "mm_hyb_spots": ([_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i64, _vp, _i32, _i32, _i32, _i32, _i32, _f32,
                       _i32, _i32, _f32, _f32, _i32, _vp, _u32, _pu32, _vp], _i32),
     "mm_dapi_spots": ([_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i64, _vp, _i32, _i32, _i32, _i32, _i32, _f32,

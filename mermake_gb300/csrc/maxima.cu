@@ -23,6 +23,8 @@
 //            (delta_fit = 0) gives NaN for hn and a, as in the reference.
 //            In tile mode the row is kept only if overlap <= xc < xend-overlap and
 //            the same for yc, then shifted by the tile origin (__main__.py:256-260).
+#include <mutex>
+
 #include "deconv.cuh"
 
 namespace {
@@ -319,4 +321,80 @@ int mm_launch_maxima_fit(const MaximaArgs &a, uint2 *cand, unsigned cand_cap, un
                                    out_count, a.keep_filter);
     MM_CHECK_LAUNCH();
     return MM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// find_local_maxima without allocation (mm_find_local_maxima_noalloc).
+//
+// Some callers cannot allocate device memory while they run: code executing
+// inside another framework's memory pool or under a fixed device-memory
+// budget, and real-time loops that must not take cudaMalloc's implicit device
+// synchronisation.  For them the candidate list and its counter live in this
+// file-scope array, reserved once when the library is loaded on a device and
+// kept by every GPU that loads the library until the process exits.  Host code
+// may not use the array's name as a device address, so the address is fetched
+// with cudaGetSymbolAddress once per device, with that device current, on the
+// first call; that first call should come before any stream capture.  Every
+// call shares the array: calls whose work overlaps on the GPU (other streams,
+// other host threads) race on it and must be serialised by the caller.
+// ---------------------------------------------------------------------------
+#define MM_NOALLOC_MAX_VOXELS (1u << 21)  // 2,097,152 voxels -> 16 MiB of candidates
+#define MM_NOALLOC_HEAD 256               // counter block before the candidate list
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MM_NOALLOC_HEAD +
+                                                                 sizeof(uint2) * MM_NOALLOC_MAX_VOXELS];
+
+namespace {
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64] = {};
+}  // namespace
+
+extern "C" int mm_find_local_maxima_noalloc(const float *image, int Z, int X, int Y, int64_t isz, int64_t isx,
+                                            const void *raw, int raw_dtype, int64_t rsz, int64_t rsx,
+                                            float threshold, int delta, int delta_fit, float sigmaZ, float sigmaXY,
+                                            float norm_div, int negate, float *out, uint32_t out_cap,
+                                            uint32_t *count, void *stream) {
+    MM_REQUIRE(image && raw && count, "null argument");
+    MM_REQUIRE(delta <= 5, "Delta must be an less than or equal to 5 due to MAX_KERNEL_POINTS");
+    MM_REQUIRE(delta >= 0 && delta_fit >= 0, "negative delta");
+    MM_REQUIRE(raw_dtype == 0 || raw_dtype == 1, "raw_dtype must be 0 (float32) or 1 (uint16)");
+    MM_REQUIRE(Z >= 0 && X >= 0 && Y >= 0 && Z < 65536 && X < 65536 && Y < 65536, "dimensions must be in [0, 65536)");
+    const unsigned long long nvox = (unsigned long long)Z * X * Y;
+    MM_REQUIRE(nvox <= MM_NOALLOC_MAX_VOXELS,
+               "volume of %llu voxels exceeds the %u-voxel limit of mm_find_local_maxima_noalloc "
+               "(its candidate list is a fixed static array); use mm_find_local_maxima",
+               nvox, MM_NOALLOC_MAX_VOXELS);
+    *count = 0;
+    if (nvox == 0) return MM_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    int dev = 0;
+    MM_CUDA_TRY(cudaGetDevice(&dev));
+    MM_REQUIRE(dev >= 0 && dev < 64, "device index %d out of range", dev);
+    void *base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void *p = nullptr;
+            MM_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+            int rc = mm_maxima_ensure_init(st);  // neighbour-offset table, launched once per device
+            if (rc) return rc;
+            g_noalloc_ptr[dev] = p;
+        }
+        base = g_noalloc_ptr[dev];
+    }
+    unsigned *ncand = static_cast<unsigned *>(base);
+    uint2 *cand = reinterpret_cast<uint2 *>(static_cast<unsigned char *>(base) + MM_NOALLOC_HEAD);
+    MaximaArgs a = {};
+    a.img = image; a.isz = isz; a.isx = isx; a.ivol = 0;
+    a.Z = Z; a.X = X; a.Y = Y; a.nvol = 1;
+    a.tiles = nullptr;
+    a.raw_kind = raw_dtype; a.raw = raw; a.rsz = rsz; a.rsx = rsx; a.rvol = 0;
+    a.th = threshold; a.delta = delta; a.delta_fit = delta_fit;
+    a.sigmaZ = sigmaZ; a.sigmaXY = sigmaXY;
+    a.div = norm_div; a.divp = nullptr; a.neg = negate; a.keep_filter = 0;
+    // the launcher clears the candidate counter (the array keeps the last call's contents)
+    int rc = mm_launch_maxima_fit(a, cand, MM_NOALLOC_MAX_VOXELS, ncand, out, out_cap, nullptr, 0, st);
+    if (rc) return rc;
+    MM_CUDA_TRY(cudaMemcpyAsync(count, ncand, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    MM_CUDA_TRY(cudaStreamSynchronize(st));
+    return *count > out_cap ? MM_EOVERFLOW : MM_OK;
 }
