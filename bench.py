@@ -191,10 +191,12 @@ def run_fov(s, form, chans=None, dapi=None):
     return out
 
 
-def timed(fn, K, W, barrier):
+def timed(fn, K, W, barrier, before_timed=None):
     import torch
     for _ in range(W):
         fn()
+    if before_timed:
+        before_timed()
     barrier()
     torch.cuda.synchronize()
     st = torch.cuda.current_stream()
@@ -236,15 +238,20 @@ def gpu_arm(args, rank, world, local):
     vox = fov_voxels(w)
 
     # device-resident timed region, with per-stage events live
-    _lib.profile_enable(True)
-    n0 = _lib.launch_count()
+    n0 = [0]
+
+    def start_counting():
+        # per-stage events and the launch count cover the timed steps only
+        torch.cuda.synchronize()
+        _lib.profile_enable(True)
+        n0[0] = _lib.launch_count()
+
     with ClockSampler(local) as clk:
-        total_ms, per = timed(lambda: run_fov(s, args.form), args.steps, args.warmup, barrier)
-    launches = _lib.launch_count() - n0
+        total_ms, per = timed(lambda: run_fov(s, args.form), args.steps, args.warmup, barrier, start_counting)
+    launches = _lib.launch_count() - n0[0]
     prof = _lib.profile_read()
     _lib.profile_enable(False)
-    # the warm-up steps ran with profiling on too: scale stage totals to the timed steps
-    frac_timed = args.steps / float(args.steps + args.warmup)
+    spots = [int(o.shape[0]) for o in run_fov(s, args.form)]
     t = torch.tensor([total_ms], device=dev)
     if pg:
         pg.all_reduce(t, op=pg.ReduceOp.MAX)
@@ -289,6 +296,7 @@ def gpu_arm(args, rank, world, local):
                    "l2": "inputs larger than L2 (%.2f GB per FOV vs 129 MB)" % (vox * 2 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single"},
         "latency_ms": {"p50": pct(per, 50), "p99": pct(per, 99)},
+        "spots_per_fov": spots,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,

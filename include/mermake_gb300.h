@@ -165,6 +165,27 @@ int mm_tile_geometry(int Z, int X, int Y, int tile_size, int zpad, int overlap, 
  * (element e of line l at data[e*nlines + l]); inverse uses exp(+i...). */
 int mm_fft_c2c(void *data, int n, int nlines, int inverse, void *stream);
 
+/* Drift alignment of maxima point sets (mermake/align.py:12-129, utils.py:10-36).
+ * mm_aligner_create is Aligner.__init__(X_ref, resc, trim, th): rows of X_ref
+ * (n rows of `cols` float32, row stride ld, device) whose last column exceeds
+ * th are kept (th = NaN: all rows), their first three columns are the
+ * reference points, and the reference's splat image (round(X/resc), trimmed in
+ * x and y) stays resident on the device.  No row left -> MM_EINVAL (the
+ * reference raises ValueError).  mm_aligner_translation is
+ * get_best_translation_points(X, target, return_counts=True): same threshold
+ * on X's last column, argmax of the full correlation of the two splat images
+ * (computed exactly as a histogram of voxel-pair differences), five
+ * nearest-neighbour refinements; writes tzxy[3] and npts (host) and
+ * synchronises the stream.  mm_aligner_info reports the kept reference points,
+ * the unique reference voxels and the image shape. */
+typedef struct mm_aligner mm_aligner;
+int mm_aligner_create(const float *X_ref, int n, int cols, int64_t ld, float th, int resc, int trim,
+                      mm_aligner **out, void *stream);
+int mm_aligner_translation(mm_aligner *al, const float *X, int n, int cols, int64_t ld, float target, float *tzxy,
+                           int *npts, void *stream);
+int mm_aligner_info(const mm_aligner *al, int *n_points, int *n_voxels, int *shape3);
+int mm_aligner_destroy(mm_aligner *al);
+
 /* Instrumentation, no reference counterpart (the reference has no timing on
  * this path).  mm_profile_enable(ctx, 1) resets and starts per-stage CUDA-event
  * timing of this context's launches (stages: rows_fwd, cols_fwd, zpass,

@@ -63,7 +63,7 @@ k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ 
                 if (flat) fsrc = flat + (long long)(d.x0 + sx) * g.fsx + d.y0;
             }
         }
-        constexpr int U = 8;
+        constexpr int U = 24;  // a whole padded row (up to 768) in flight per warp
         for (int e0 = lane; e0 < n; e0 += 32 * U) {
             float v[U];
 #pragma unroll
@@ -188,7 +188,8 @@ k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restri
     // y blur: the free ping-pong buffer holds 2 nl rows of n floats
     float *Bf = reinterpret_cast<float *>(R == L.A ? L.B : L.A);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const int seg = (n + 31) / 32;
+    // odd segment length: the 32 lanes' strided reads fall in distinct banks
+    const int seg = ((n + 31) / 32) | 1;
     for (int q = warp; q < 2 * nl; q += nw) {
         const int l = q >> 1, comp = q & 1;
         const int s0 = lane * seg, s1 = min(s0 + seg, n);
@@ -222,7 +223,7 @@ k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restri
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kThreads)
 k_blur_x_sub(TileGeom g, const float *__restrict__ res, const float *__restrict__ tmp, int delta,
-             float *__restrict__ res_out, float *__restrict__ stitch, long long osz, long long osx) {
+             float *res_out, float *__restrict__ stitch, long long osz, long long osx) {
     extern __shared__ __align__(16) float colbuf[];  // P x 32
     const int P = g.P;
     const int ti = g.t0 + blockIdx.z;
@@ -233,7 +234,13 @@ k_blur_x_sub(TileGeom g, const float *__restrict__ res, const float *__restrict_
     const int y = y0 + lane;
     const long long pbase = ((long long)blockIdx.z * g.Z + z) * P * P;
     if (delta >= 0) {
-        for (int x = warp; x < P; x += nw) colbuf[x * 32 + lane] = (y < P) ? tmp[pbase + (long long)x * P + y] : 0.f;
+        for (int x = warp; x < P; x += nw) {
+            if (y < P)
+                cp_async4(&colbuf[x * 32 + lane], &tmp[pbase + (long long)x * P + y]);
+            else
+                colbuf[x * 32 + lane] = 0.f;
+        }
+        cp_async_wait_all();
         __syncthreads();
     }
     const int seg = (P + nw - 1) / nw;
@@ -243,25 +250,35 @@ k_blur_x_sub(TileGeom g, const float *__restrict__ res, const float *__restrict_
         const int lo = max(x0 - delta, 0), hi = min(x0 + delta, P - 1);
         for (int i = lo; i <= hi; ++i) sum += colbuf[i * 32 + lane];
     }
-    for (int x = x0; x < x1; ++x) {
-        if (delta >= 0 && x > x0) {
-            const int add = x + delta, drop = x - delta - 1;
-            if (add <= P - 1) sum += colbuf[add * 32 + lane];
-            if (drop >= 0) sum -= colbuf[drop * 32 + lane];
-        }
-        if (y >= P) continue;
-        float v = res[pbase + (long long)x * P + y];
-        if (delta >= 0) {
-            const int cnt = min(x + delta, P - 1) - max(x - delta, 0) + 1;
-            v = v - sum / (float)cnt;
-        }
-        if (res_out) res_out[pbase + (long long)x * P + y] = v;
-        if (stitch && x >= g.ov && x < d.xend - g.ov && y >= g.ov && y < d.yend - g.ov) {
-            const int ox = d.x + x - g.ov, oy = d.y + y - g.ov;
-            // inside its own span a tile is the final writer; past it, ask who is
-            const bool own = ox < d.x + g.ts && oy < d.y + g.ts;
-            if (ox < g.X && oy < g.Y && (own || mm_stitch_owner(g, ox, oy) == ti))
-                stitch[z * osz + (long long)ox * osx + oy] = v;
+    constexpr int U = 8;  // rows of res loaded ahead of the in-place stores
+    for (int xb = x0; xb < x1; xb += U) {
+        float v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+            v[u] = (y < P && xb + u < x1) ? res[pbase + (long long)(xb + u) * P + y] : 0.f;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int x = xb + u;
+            if (x >= x1) break;
+            if (delta >= 0 && x > x0) {
+                const int add = x + delta, drop = x - delta - 1;
+                if (add <= P - 1) sum += colbuf[add * 32 + lane];
+                if (drop >= 0) sum -= colbuf[drop * 32 + lane];
+            }
+            if (y >= P) continue;
+            float val = v[u];
+            if (delta >= 0) {
+                const int cnt = min(x + delta, P - 1) - max(x - delta, 0) + 1;
+                val = val - sum / (float)cnt;
+            }
+            if (res_out) res_out[pbase + (long long)x * P + y] = val;
+            if (stitch && x >= g.ov && x < d.xend - g.ov && y >= g.ov && y < d.yend - g.ov) {
+                const int ox = d.x + x - g.ov, oy = d.y + y - g.ov;
+                // inside its own span a tile is the final writer; past it, ask who is
+                const bool own = ox < d.x + g.ts && oy < d.y + g.ts;
+                if (ox < g.X && oy < g.Y && (own || mm_stitch_owner(g, ox, oy) == ti))
+                    stitch[z * osz + (long long)ox * osx + oy] = val;
+            }
         }
     }
 }

@@ -4,11 +4,11 @@
 // reference (deconvolver.py:86-90, 155-157), which carry large prime factors
 // (678 = 2*3*113, 478 = 2*239, 148 = 4*37, 118 = 2*59, ...).  A length is
 // factored into stages of three kinds:
-//   * radix 2/3/4/5/7 and the odd primes 11, 13, 17: one thread per butterfly,
+//   * radix 2/3/4/5/7 and the odd primes 11..37: one thread per butterfly,
 //     values in registers;
-//   * primes 19..61, 79, 89 and 113 ("lane" stage; the primes of the
-//     reference's padded lengths 2*Z-1+... and 678 = 2*3*113, plus every prime
-//     up to 61): one warp per butterfly and one lane per
+//   * primes 41..61, 79, 89 and 113 ("lane" stage; with 59, 79, 89 and 113
+//     the primes of the reference's padded lengths such as 118 = 2*59 and
+//     678 = 2*3*113): one warp per butterfly and one lane per
 //     output pair (k, R-k); each lane keeps its column of the DFT matrix in
 //     registers for the whole stage, and the warp reads the paired inputs
 //     a_r = x_r + x_{R-r}, b_r = x_r - x_{R-r} as shared-memory broadcasts
@@ -172,53 +172,20 @@ __device__ __forceinline__ void dft_small<7, false>(float2 *v) { dft_odd<7, fals
 template <>
 __device__ __forceinline__ void dft_small<7, true>(float2 *v) { dft_odd<7, true>(v); }
 
-// Odd radix 11, 13, 17 in registers, cos/sin loaded once per stage from the plan table.
-template <int R, bool INV>
-__device__ __forceinline__ void dft_odd_tab(float2 *v, const float *c, const float *sn) {
-    constexpr int H = (R - 1) / 2;
-    float2 a[H], b[H];
-#pragma unroll
-    for (int r = 1; r <= H; ++r) {
-        a[r - 1] = cadd(v[r], v[R - r]);
-        b[r - 1] = csub(v[r], v[R - r]);
-    }
-    float2 x0 = v[0];
-    float2 s0 = x0;
-#pragma unroll
-    for (int r = 0; r < H; ++r) s0 = cadd(s0, a[r]);
-#pragma unroll
-    for (int k = 1; k <= H; ++k) {
-        float ax = x0.x, ay = x0.y, bx = 0.f, by = 0.f;
-#pragma unroll
-        for (int r = 1; r <= H; ++r) {
-            const int m = (r * k) % R;
-            const float cc = m <= H ? c[m] : c[R - m];
-            const float ss = m <= H ? sn[m] : -sn[R - m];
-            ax += a[r - 1].x * cc;
-            ay += a[r - 1].y * cc;
-            bx += b[r - 1].x * ss;
-            by += b[r - 1].y * ss;
-        }
-        if (!INV) {
-            v[k] = make_float2(ax + by, ay - bx);
-            v[R - k] = make_float2(ax - by, ay + bx);
-        } else {
-            v[k] = make_float2(ax - by, ay + bx);
-            v[R - k] = make_float2(ax + by, ay - bx);
-        }
-    }
-    v[0] = s0;
-}
-
+// Odd radix 11..37 with one thread per butterfly: the paired inputs
+// a_r = x_r + x_{R-r}, b_r = x_r - x_{R-r} and the stage's cos/sin values
+// (loaded once per stage from the plan table) sit in registers; each output
+// pair (k, R-k) is accumulated and written to shared memory at once, so no
+// output array is held.
 template <int R, bool INV>
 __device__ __noinline__ void stage_odd_tab(const float2 *__restrict__ src, float2 *__restrict__ dst, int n,
                                            int nl, int Ns, const float2 *tw, const float2 *cs) {
     constexpr int H = (R - 1) / 2;
-    float c[H + 1], sn[H + 1];
+    float c[H], sn[H];
 #pragma unroll
-    for (int m = 0; m <= H; ++m) {
-        c[m] = cs[m].x;
-        sn[m] = -cs[m].y;  // table holds (cos, -sin)
+    for (int m = 1; m <= H; ++m) {
+        c[m - 1] = cs[m].x;
+        sn[m - 1] = -cs[m].y;  // table holds (cos, -sin)
     }
     const int m = n / R;
     const int tstep = n / (Ns * R);
@@ -229,51 +196,95 @@ __device__ __noinline__ void stage_odd_tab(const float2 *__restrict__ src, float
         const int l = it & (nl - 1);
         const int j = it >> lnl;
         const int k = j - fdiv_i(j, Ns, invNs) * Ns;
-        float2 v[R];
+        const float2 x0 = src[sidx(j, l, nl)];
+        float2 a[H], b[H];
+        float2 s0 = x0;
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = src[sidx(j + r * m, l, nl)];
-        if (Ns > 1) {
-#pragma unroll
-            for (int r = 1; r < R; ++r) {
-                float2 w = tw[k * r * tstep];
-                v[r] = INV ? cmulc(v[r], w) : cmul(v[r], w);
+        for (int r = 1; r <= H; ++r) {
+            float2 u = src[sidx(j + r * m, l, nl)], v = src[sidx(j + (R - r) * m, l, nl)];
+            if (Ns > 1) {
+                const float2 wu = tw[k * r * tstep], wv = tw[k * (R - r) * tstep];
+                u = INV ? cmulc(u, wu) : cmul(u, wu);
+                v = INV ? cmulc(v, wv) : cmul(v, wv);
             }
+            a[r - 1] = cadd(u, v);
+            b[r - 1] = csub(u, v);
+            s0 = cadd(s0, a[r - 1]);
         }
-        dft_odd_tab<R, INV>(v, c, sn);
-        int d = (j - k) * R + k;
+        const int d = (j - k) * R + k;
+        dst[sidx(d, l, nl)] = s0;
 #pragma unroll
-        for (int r = 0; r < R; ++r) dst[sidx(d + r * Ns, l, nl)] = v[r];
+        for (int q = 1; q <= H; ++q) {
+            float ax = x0.x, ay = x0.y, bx = 0.f, by = 0.f;
+#pragma unroll
+            for (int r = 1; r <= H; ++r) {
+                const int mm = (r * q) % R;
+                const float cc = mm <= H ? c[mm - 1] : c[R - mm - 1];
+                const float ss = mm <= H ? sn[mm - 1] : -sn[R - mm - 1];
+                ax += a[r - 1].x * cc;
+                ay += a[r - 1].y * cc;
+                bx += b[r - 1].x * ss;
+                by += b[r - 1].y * ss;
+            }
+            float2 o1, o2;
+            if (!INV) {
+                o1 = make_float2(ax + by, ay - bx);
+                o2 = make_float2(ax - by, ay + bx);
+            } else {
+                o1 = make_float2(ax - by, ay + bx);
+                o2 = make_float2(ax + by, ay - bx);
+            }
+            dst[sidx(d + q * Ns, l, nl)] = o1;
+            dst[sidx(d + (R - q) * Ns, l, nl)] = o2;
+        }
     }
 }
 
-// Lane stage (primes 19..113, see top): warp per butterfly, lane per output pair.
-// Each warp takes two butterflies per iteration (eight independent FMA
-// chains).  scr: MM_FFT_SCR_PER_WARP float4 of shared scratch per warp.
+// Lane stage (primes 41..113, see top): warps per butterfly, lane per output
+// pair.  For H = (R-1)/2 <= 32 one warp covers all pairs and keeps the whole
+// DFT column (2H values) in registers.  For 32 < H <= 64 two k-groups of lanes
+// are needed, and the r range is split in halves between two warps as well, so
+// that each lane keeps at most 64 coefficients: four warps (2 k-groups x 2
+// r-halves) form a stream, the r-half warps add their partial sums through
+// shared memory between two named barriers.  Each stream takes two butterflies
+// per iteration (eight independent FMA chains per warp).
+// scr: MM_FFT_SCR_PER_WARP float4 of shared scratch per warp.
 #define MM_FFT_SCR_PER_WARP 128
 template <int R, bool INV>
 __device__ __noinline__ void stage_lane(const float2 *__restrict__ src, float2 *__restrict__ dst, int n,
                                         int nl, int Ns, const float2 *__restrict__ tw,
                                         const float2 *__restrict__ cs, float4 *__restrict__ scr_all) {
     constexpr int H = (R - 1) / 2;
-    constexpr int G = (H + 31) / 32;  // warps per butterfly
+    constexpr int G = (H + 31) / 32;         // k-groups
+    constexpr int RS = H > 32 ? 2 : 1;       // r-halves
+    constexpr int HH = (H + RS - 1) / RS;    // r values per half
+    constexpr int W = G * RS;                // warps per stream
+    static_assert(HH <= 32 || RS == 1, "lane stage handles H <= 64");
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-    const int g = warp % G, strm = warp / G, nstrm = nw / G;
+    const int sub = warp % W, strm = warp / W, nstrm = nw / W;
     if (strm >= nstrm) return;
+    const int g = sub / RS, h = sub % RS;
+    const int r_lo = h * HH + 1;  // this warp's r range: [r_lo, r_lo + HH) within [1, H]
     float4 *scr = scr_all + warp * MM_FFT_SCR_PER_WARP;
+    // exchange area: the r-half-1 warp of a k-group writes its partial sums into
+    // its r-half-0 partner's scratch [64, 128)
+    float4 *xch = scr_all + (strm * W + g * RS) * MM_FFT_SCR_PER_WARP + 64;
     const int k = g * 32 + lane + 1;
     const bool kv = k <= H;
-    float cr[H], sr[H];
+    float cr[HH], sr[HH];
 #pragma unroll
-    for (int r = 1; r <= H; ++r) {
-        const float2 w = cs[kv ? (r * k) % R : 0];  // (cos, -sin) of 2 pi r k / R
-        cr[r - 1] = w.x;
-        sr[r - 1] = w.y;
+    for (int i = 0; i < HH; ++i) {
+        const int r = r_lo + i;
+        const float2 w = (kv && r <= H) ? cs[(r * k) % R] : make_float2(0.f, 0.f);  // (cos, -sin)
+        cr[i] = w.x;
+        sr[i] = w.y;
     }
     const int m = n / R;
     const int tstep = n / (Ns * R);
     const int nb = m * nl;
     const int lnl = log2_pow2(nl);
     const float invNs = 1.0f / (float)Ns;
+    constexpr int SLOT = RS == 1 ? 64 : 32;  // a/b entries per butterfly in scr
     for (int b0 = strm; b0 < nb; b0 += 2 * nstrm) {
         const bool two = b0 + nstrm < nb;
         float2 x0[2];
@@ -288,59 +299,92 @@ __device__ __noinline__ void stage_lane(const float2 *__restrict__ src, float2 *
             x0[q] = src[sidx(j, l, nl)];
             sx[q] = 0.f;
             sy[q] = 0.f;
-            for (int r = lane + 1; r <= H; r += 32) {
-                float2 u = src[sidx(j + r * m, l, nl)], v = src[sidx(j + (R - r) * m, l, nl)];
-                if (Ns > 1) {
-                    const float2 wu = tw[kk * r * tstep], wv = tw[kk * (R - r) * tstep];
-                    u = INV ? cmulc(u, wu) : cmul(u, wu);
-                    v = INV ? cmulc(v, wv) : cmul(v, wv);
+            for (int i = lane; i < HH; i += 32) {
+                const int r = r_lo + i;
+                float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (r <= H) {
+                    float2 u = src[sidx(j + r * m, l, nl)], v = src[sidx(j + (R - r) * m, l, nl)];
+                    if (Ns > 1) {
+                        const float2 wu = tw[kk * r * tstep], wv = tw[kk * (R - r) * tstep];
+                        u = INV ? cmulc(u, wu) : cmul(u, wu);
+                        v = INV ? cmulc(v, wv) : cmul(v, wv);
+                    }
+                    t = make_float4(u.x + v.x, u.y + v.y, u.x - v.x, u.y - v.y);
                 }
-                const float4 t = make_float4(u.x + v.x, u.y + v.y, u.x - v.x, u.y - v.y);
-                scr[q * 64 + r - 1] = t;
+                scr[q * SLOT + i] = t;
                 sx[q] += t.x;
                 sy[q] += t.y;
             }
         }
         __syncwarp();
-        float ax0 = x0[0].x, ay0 = x0[0].y, bx0 = 0.f, by0 = 0.f;
-        float ax1 = x0[1].x, ay1 = x0[1].y, bx1 = 0.f, by1 = 0.f;
+        float ax0 = 0.f, ay0 = 0.f, bx0 = 0.f, by0 = 0.f;
+        float ax1 = 0.f, ay1 = 0.f, bx1 = 0.f, by1 = 0.f;
 #pragma unroll
-        for (int r = 0; r < H; ++r) {
-            const float4 t0 = scr[r], t1 = scr[64 + r];
-            ax0 += t0.x * cr[r];
-            ay0 += t0.y * cr[r];
-            bx0 += t0.z * sr[r];
-            by0 += t0.w * sr[r];
-            ax1 += t1.x * cr[r];
-            ay1 += t1.y * cr[r];
-            bx1 += t1.z * sr[r];
-            by1 += t1.w * sr[r];
+        for (int i = 0; i < HH; ++i) {
+            const float4 t0 = scr[i], t1 = scr[SLOT + i];
+            ax0 += t0.x * cr[i];
+            ay0 += t0.y * cr[i];
+            bx0 += t0.z * sr[i];
+            by0 += t0.w * sr[i];
+            ax1 += t1.x * cr[i];
+            ay1 += t1.y * cr[i];
+            bx1 += t1.z * sr[i];
+            by1 += t1.w * sr[i];
         }
+        // sums of a_r over this warp's r range (for X[0]), reduced in k-group 0
+        if (g == 0) {
 #pragma unroll
-        for (int q = 0; q < 2; ++q) {
-            if (q == 1 && !two) break;
-            const float ax = q ? ax1 : ax0, ay = q ? ay1 : ay0, bx = q ? bx1 : bx0, by = q ? by1 : by0;
-            if (kv) {
-                float2 o1, o2;
-                if (!INV) {
-                    o1 = make_float2(ax - by, ay + bx);
-                    o2 = make_float2(ax + by, ay - bx);
-                } else {
-                    o1 = make_float2(ax + by, ay - bx);
-                    o2 = make_float2(ax - by, ay + bx);
-                }
-                dst[sidx(dd[q] + k * Ns, ll[q], nl)] = o1;
-                dst[sidx(dd[q] + (R - k) * Ns, ll[q], nl)] = o2;
-            }
-            if (g == 0) {
-                float tx = sx[q], ty = sy[q];
+            for (int q = 0; q < 2; ++q)
                 for (int o = 16; o > 0; o >>= 1) {
-                    tx += __shfl_xor_sync(0xffffffffu, tx, o);
-                    ty += __shfl_xor_sync(0xffffffffu, ty, o);
+                    sx[q] += __shfl_xor_sync(0xffffffffu, sx[q], o);
+                    sy[q] += __shfl_xor_sync(0xffffffffu, sy[q], o);
                 }
-                if (lane == 0) dst[sidx(dd[q], ll[q], nl)] = make_float2(x0[q].x + tx, x0[q].y + ty);
+        }
+        if (RS == 2) {
+            if (h == 1) {
+                xch[lane] = make_float4(ax0, ay0, bx0, by0);
+                xch[32 + lane] = make_float4(ax1, ay1, bx1, by1);
+                if (g == 0 && lane == 0) {
+                    // the two butterflies' sums go to this warp's own free scratch [64, 65)
+                    *reinterpret_cast<float4 *>(scr + 64) = make_float4(sx[0], sy[0], sx[1], sy[1]);
+                }
+            }
+            asm volatile("bar.sync %0, %1;" ::"r"(1 + strm), "r"(W * 32) : "memory");
+            if (h == 0) {
+                const float4 p0 = xch[lane], p1 = xch[32 + lane];
+                ax0 += p0.x; ay0 += p0.y; bx0 += p0.z; by0 += p0.w;
+                ax1 += p1.x; ay1 += p1.y; bx1 += p1.z; by1 += p1.w;
             }
         }
+        if (h == 0) {
+            float tx[2] = {sx[0], sx[1]}, ty[2] = {sy[0], sy[1]};
+            if (RS == 2 && g == 0) {
+                // sums of the partner r-half warp (warp g=0, h=1 of this stream)
+                const float4 o = scr_all[(strm * W + 1) * MM_FFT_SCR_PER_WARP + 64];
+                tx[0] += o.x; ty[0] += o.y;
+                tx[1] += o.z; ty[1] += o.w;
+            }
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                if (q == 1 && !two) break;
+                const float ax = (q ? ax1 : ax0) + x0[q].x, ay = (q ? ay1 : ay0) + x0[q].y;
+                const float bx = q ? bx1 : bx0, by = q ? by1 : by0;
+                if (kv) {
+                    float2 o1, o2;
+                    if (!INV) {
+                        o1 = make_float2(ax - by, ay + bx);
+                        o2 = make_float2(ax + by, ay - bx);
+                    } else {
+                        o1 = make_float2(ax + by, ay - bx);
+                        o2 = make_float2(ax - by, ay + bx);
+                    }
+                    dst[sidx(dd[q] + k * Ns, ll[q], nl)] = o1;
+                    dst[sidx(dd[q] + (R - k) * Ns, ll[q], nl)] = o2;
+                }
+                if (g == 0 && lane == 0) dst[sidx(dd[q], ll[q], nl)] = make_float2(x0[q].x + tx[q], x0[q].y + ty[q]);
+            }
+        }
+        if (RS == 2) asm volatile("bar.sync %0, %1;" ::"r"(1 + strm), "r"(W * 32) : "memory");
         __syncwarp();
     }
 }
@@ -466,8 +510,8 @@ __device__ float2 *fft_lines(float2 *A, float2 *B, int nl, const FftPlan &P,
             case 4: stage_small<4, INV>(src, dst, P.n, nl, Ns, tw_s); break;
             case 5: stage_small<5, INV>(src, dst, P.n, nl, Ns, tw_s); break;
             case 7: stage_small<7, INV>(src, dst, P.n, nl, Ns, tw_s); break;
-            MM_ODD_CASE(11) MM_ODD_CASE(13) MM_ODD_CASE(17)
-            MM_LANE_CASE(19) MM_LANE_CASE(23) MM_LANE_CASE(29) MM_LANE_CASE(31) MM_LANE_CASE(37)
+            MM_ODD_CASE(11) MM_ODD_CASE(13) MM_ODD_CASE(17) MM_ODD_CASE(19) MM_ODD_CASE(23)
+            MM_ODD_CASE(29) MM_ODD_CASE(31) MM_ODD_CASE(37)
             MM_LANE_CASE(41) MM_LANE_CASE(43) MM_LANE_CASE(47) MM_LANE_CASE(53) MM_LANE_CASE(59)
             MM_LANE_CASE(61) MM_LANE_CASE(79) MM_LANE_CASE(89) MM_LANE_CASE(113)
             default: stage_generic<INV>(src, dst, P.n, nl, R, Ns, tw_s, tab_s + P.ptab[st]); break;
@@ -517,14 +561,18 @@ __device__ __forceinline__ void cp_async8(void *smem_dst, const void *gsrc) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gsrc) : "memory");
 }
+__device__ __forceinline__ void cp_async4(void *smem_dst, const void *gsrc) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gsrc) : "memory");
+}
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
 // Host side: plan cache (fft_plan.cu).
 int mm_fft_plan_get(int n, FftPlan *out);
 
 // ---- launch helpers shared by the FFT kernel translation units -------------
-constexpr int kFftThreads = 256;
-constexpr int kFftSmemLimit = 200 * 1024;
+constexpr int kFftThreads = 512;
+constexpr int kFftSmemLimit = 224 * 1024;
 
 static inline size_t fft_smem(const FftPlan &P, int nl) {
     return fft_smem_bytes(P.n, P.ntab, nl, kFftThreads / 32);

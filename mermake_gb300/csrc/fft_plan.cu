@@ -14,7 +14,7 @@ namespace {
 std::mutex g_mu;
 std::map<std::pair<int, int>, FftPlan> g_plans;
 
-// Radix kinds (fft.cuh): 2/3/4/5/7 constant-table registers; 11, 13, 17 table
+// Radix kinds (fft.cuh): 2/3/4/5/7 constant-table registers; 11..37 table
 // registers; the other odd primes lane or generic stages, which run first.
 // Every stage except 2/3/4/5/7 needs its cos/sin table.
 void factor(int n, std::vector<int> &first, std::vector<int> &small) {
@@ -24,8 +24,8 @@ void factor(int n, std::vector<int> &first, std::vector<int> &small) {
         while (n % p == 0) { small.push_back(p); n /= p; }
     std::vector<int> mid;
     for (int p = 11; (long)p * p <= n; p += 2)
-        while (n % p == 0) { (p <= 17 ? mid : first).push_back(p); n /= p; }
-    if (n > 1) (n <= 17 ? mid : first).push_back(n);
+        while (n % p == 0) { (p <= 37 ? mid : first).push_back(p); n /= p; }
+    if (n > 1) (n <= 37 ? mid : first).push_back(n);
     // the table-driven odd stages go after the large ones, before the constant radices
     small.insert(small.begin(), mid.begin(), mid.end());
 }
@@ -76,11 +76,11 @@ int mm_fft_plan_get(int n, FftPlan *out) {
         Ns *= R;
         P.nst++;
     }
-    // lane-stage class (fft.cuh): 0 none, 63 primes 19..61, 127 also 79, 89, 113
+    // lane-stage class (fft.cuh): 0 none, 63 primes 41..61, 127 also 79, 89, 113
     P.lclass = 0;
     for (int i = 0; i < P.nst; ++i) {
         const int R = P.rad[i];
-        if (R >= 19 && R <= 61 && P.lclass < 63) P.lclass = 63;
+        if (R >= 41 && R <= 61 && P.lclass < 63) P.lclass = 63;
         if (R == 79 || R == 89 || R == 113) P.lclass = 127;
     }
     if (P.nst > MM_FFT_MAXST) {

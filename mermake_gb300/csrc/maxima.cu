@@ -16,7 +16,8 @@
 // k_fit      one warp per spot: gathers the sphere |d|^2 <= delta_fit^2 in the
 //            reference's (dz, dx, dy) order (first 600 in-range samples,
 //            maxima.cu:148, 190-232) and forms every output of
-//            delta_fit_cross_corr from double-precision moment sums:
+//            delta_fit_cross_corr from moment sums (float32 per lane on
+//            centre-shifted values, double across the warp):
 //              bg = min v;  centroid = sum (c+d)(v-bg) / sum (v-bg)  (fallback c);
 //              hn = cov(v, G) / (std'(v) std(G));  a = cov(raw, G) / (std'(raw) std(G))
 //            with std' = std, or 1 where std == 0 (maxima.cu:233-341).  std(G) == 0
@@ -34,9 +35,21 @@ constexpr int kSphereCap = 515;
 __device__ char4 g_sphere[kMaxDelta + 1][kSphereCap];  // neighbour offsets, nearest first
 __device__ int g_sphere_n[kMaxDelta + 1];
 __device__ int g_sphere_ready;
+// fit samples: the sphere |d|^2 <= df^2 incl. the centre, in the reference's
+// (dz, dx, dy) loop order (maxima.cu:190-193)
+__device__ char4 g_fit_sphere[kMaxDelta + 1][kSphereCap];
+__device__ int g_fit_sphere_n[kMaxDelta + 1];
 
 __global__ void k_init_sphere() {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    for (int d = 0; d <= kMaxDelta; ++d) {
+        int n = 0;
+        for (int dz = -d; dz <= d; ++dz)
+            for (int dx = -d; dx <= d; ++dx)
+                for (int dy = -d; dy <= d; ++dy)
+                    if (dz * dz + dx * dx + dy * dy <= d * d) g_fit_sphere[d][n++] = make_char4(dz, dx, dy, 0);
+        g_fit_sphere_n[d] = n;
+    }
     for (int d = 0; d <= kMaxDelta; ++d) {
         int n = 0;
         for (int r2 = 1; r2 <= d * d; ++r2)
@@ -164,6 +177,10 @@ __device__ __forceinline__ double wsum(double v) {
     return v;
 }
 
+// Per-spot fit.  Each lane sums its samples in float32 after shifting the
+// image and raw values by the centre voxel's (every moment used below is
+// shift-invariant, so the shift removes the cancellation); the warp reduction
+// and the final statistics are double precision.
 __global__ void __launch_bounds__(256)
 k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand, unsigned cap, int delta_fit,
       float sigmaZ, float sigmaXY, Xform t, float *__restrict__ out, unsigned out_cap,
@@ -171,9 +188,11 @@ k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand
     t = xf_resolve(t);
     const unsigned lane = threadIdx.x & 31;
     const unsigned nc = min(*ncand, cap);
+    const bool table = delta_fit <= kMaxDelta;
     const int side = 2 * delta_fit + 1;
-    const int cube = side * side * side;
+    const int nsamp = table ? g_fit_sphere_n[delta_fit] : side * side * side;
     const int df2 = delta_fit * delta_fit;
+    const float gz = 2 * sigmaZ * sigmaZ, gxy = 2 * sigmaXY * sigmaXY;
     for (unsigned s = (blockIdx.x * blockDim.x + threadIdx.x) / 32; s < nc; s += gridDim.x * blockDim.x / 32) {
         uint2 c = cand[s];
         const int z0 = c.x & 0xffff, x0 = c.x >> 16, y0 = c.y & 0xffff, vi = c.y >> 16;
@@ -182,77 +201,86 @@ k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand
         vol_dims(V, vi, X, Y, d);
         const int Z = V.Z;
         const float *img = V.img + vi * V.ivol;
-        double n = 0, sv = 0, svv = 0, sg = 0, sgg = 0, svg = 0, sr = 0, srr = 0, srg = 0;
-        double sdz = 0, sdx = 0, sdy = 0, svdz = 0, svdx = 0, svdy = 0;
+        const float cv = xf(img[z0 * V.isz + x0 * V.isx + y0], t);
+        const float crw = raw_at(V, vi, d, z0, x0, y0);
+        float n = 0, sv = 0, svv = 0, sg = 0, sgg = 0, svg = 0, sr = 0, srr = 0, srg = 0;
+        float sdz = 0, sdx = 0, sdy = 0, svdz = 0, svdx = 0, svdy = 0;
         float vmin = 1e20f;
         int taken = 0;  // in-range samples before this chunk (cap 600, maxima.cu:194)
-        for (int c0 = 0; c0 < cube && taken < 600; c0 += 32) {
-            int ci = c0 + (int)lane;
+        for (int c0 = 0; c0 < nsamp && taken < 600; c0 += 32) {
+            const int ci = c0 + (int)lane;
             int dz = 0, dx = 0, dy = 0;
             bool ok = false;
             int zz = 0, xx = 0, yy = 0;
-            if (ci < cube) {
-                dz = ci / (side * side) - delta_fit;
-                dx = (ci / side) % side - delta_fit;
-                dy = ci % side - delta_fit;
-                if (dz * dz + dx * dx + dy * dy <= df2) {
+            if (ci < nsamp) {
+                bool in;
+                if (table) {
+                    const char4 o = g_fit_sphere[delta_fit][ci];
+                    dz = o.x; dx = o.y; dy = o.z;
+                    in = true;
+                } else {
+                    dz = ci / (side * side) - delta_fit;
+                    dx = (ci / side) % side - delta_fit;
+                    dy = ci % side - delta_fit;
+                    in = dz * dz + dx * dx + dy * dy <= df2;
+                }
+                if (in) {
                     zz = refl(z0 + dz, Z);
                     xx = refl(x0 + dx, X);
                     yy = refl(y0 + dy, Y);
                     ok = zz >= 0 && zz < Z && xx >= 0 && xx < X && yy >= 0 && yy < Y;
                 }
             }
-            unsigned m = __ballot_sync(0xffffffffu, ok);
-            int rank = taken + __popc(m & ((1u << lane) - 1));
+            const unsigned m = __ballot_sync(0xffffffffu, ok);
+            const int rank = taken + __popc(m & ((1u << lane) - 1));
             taken += __popc(m);
             if (ok && rank < 600) {
-                float v = xf(img[zz * V.isz + xx * V.isx + yy], t);
-                float r = raw_at(V, vi, d, zz, xx, yy);
-                float g = expf(-(dz * dz / (2 * sigmaZ * sigmaZ) + dx * dx / (2 * sigmaXY * sigmaXY) +
-                                 dy * dy / (2 * sigmaXY * sigmaXY)));
-                double dv = v, dr = r, dg = g;
-                n += 1;
+                const float v = xf(img[zz * V.isz + xx * V.isx + yy], t);
+                const float r = raw_at(V, vi, d, zz, xx, yy);
+                const float g = expf(-(dz * dz / gz + dx * dx / gxy + dy * dy / gxy));
+                const float dv = v - cv, dr = r - crw;
+                n += 1.f;
                 sv += dv; svv += dv * dv;
-                sg += dg; sgg += dg * dg; svg += dv * dg;
-                sr += dr; srr += dr * dr; srg += dr * dg;
-                sdz += dz; sdx += dx; sdy += dy;
+                sg += g; sgg += g * g; svg += dv * g;
+                sr += dr; srr += dr * dr; srg += dr * g;
+                sdz += (float)dz; sdx += (float)dx; sdy += (float)dy;
                 svdz += dv * dz; svdx += dv * dx; svdy += dv * dy;
                 vmin = fminf(vmin, v);
             }
         }
-        n = wsum(n); sv = wsum(sv); svv = wsum(svv); sg = wsum(sg); sgg = wsum(sgg); svg = wsum(svg);
-        sr = wsum(sr); srr = wsum(srr); srg = wsum(srg);
-        sdz = wsum(sdz); sdx = wsum(sdx); sdy = wsum(sdy);
-        svdz = wsum(svdz); svdx = wsum(svdx); svdy = wsum(svdy);
+        const double N = wsum(n), Sv = wsum(sv), Svv = wsum(svv), Sg = wsum(sg), Sgg = wsum(sgg), Svg = wsum(svg);
+        const double Sr = wsum(sr), Srr = wsum(srr), Srg = wsum(srg);
+        const double Sdz = wsum(sdz), Sdx = wsum(sdx), Sdy = wsum(sdy);
+        const double Svdz = wsum(svdz), Svdx = wsum(svdx), Svdy = wsum(svdy);
         for (int o = 16; o > 0; o >>= 1) vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
-        if (lane != 0 || n == 0) continue;
-        const double bg = vmin;
-        const double mg = sg / n, mv = sv / n, mr = sr / n;
-        const double varg = fmax(sgg / n - mg * mg, 0.0);
-        const double varv = fmax(svv / n - mv * mv, 0.0);
-        const double varr = fmax(srr / n - mr * mr, 0.0);
+        if (lane != 0 || N == 0) continue;
+        const double mg = Sg / N, mv = Sv / N, mr = Sr / N;
+        const double varg = fmax(Sgg / N - mg * mg, 0.0);
+        const double varv = fmax(Svv / N - mv * mv, 0.0);
+        const double varr = fmax(Srr / N - mr * mr, 0.0);
         const double stdg = sqrt(varg);
         double stdv = sqrt(varv), stdr = sqrt(varr);
         if (!(stdv > 0)) stdv = 1.0;
         if (!(stdr > 0)) stdr = 1.0;
-        const double hn = (svg / n - mv * mg) / (stdv * stdg);
-        const double a = (srg / n - mr * mg) / (stdr * stdg);
-        // sum (c + d)(v - bg) = c * sum(v - bg) + sum d v - bg sum d
-        const double sw = sv - n * bg;
+        const double hn = (Svg / N - mv * mg) / (stdv * stdg);
+        const double a = (Srg / N - mr * mg) / (stdr * stdg);
+        // sum (c + d)(v - bg) / sum (v - bg), with v - bg = dv + (cv - bg)
+        const double shift = (double)cv - (double)vmin;
+        const double sw = Sv + N * shift;
         double zc, xc, yc;
         if (sw > 0) {
-            zc = (z0 * sw + svdz - bg * sdz) / sw;
-            xc = (x0 * sw + svdx - bg * sdx) / sw;
-            yc = (y0 * sw + svdy - bg * sdy) / sw;
+            zc = z0 + (Svdz + shift * Sdz) / sw;
+            xc = x0 + (Svdx + shift * Sdx) / sw;
+            yc = y0 + (Svdy + shift * Sdy) / sw;
         } else {
             zc = z0; xc = x0; yc = y0;
         }
         float row[8];
         row[0] = (float)zc; row[1] = (float)xc; row[2] = (float)yc; row[3] = vmin;
         row[4] = (float)a;
-        row[5] = raw_at(V, vi, d, z0, x0, y0);
+        row[5] = crw;
         row[6] = (float)hn;
-        row[7] = xf(img[z0 * V.isz + x0 * V.isx + y0], t);
+        row[7] = cv;
         unsigned o;
         if (keep_filter) {
             const int ov = V.g.ov;

@@ -1,0 +1,78 @@
+"""GPU drift alignment (align.py:12-176) against the reference's drift pickle and
+the CPU oracle."""
+import json
+import os
+import types
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import align as oalign
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def al():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from mermake_gb300 import align
+    return align
+
+
+@pytest.fixture(scope="module")
+def feats(golden_dir):
+    d = np.load(os.path.join(golden_dir, "dapi_features.npz"))
+    return d["Xh_plus"], d["Xh_minus"]
+
+
+def test_drift_matches_reference_pickle(al, feats, golden_dir):
+    """drift_Conv_zscan__020--_set1.pkl: DualAligner(th=4) self-alignment."""
+    kat = json.load(open(os.path.join(golden_dir, "drift_kat.json")))["drifts"][0]
+    im = types.SimpleNamespace(Xh_plus=torch.from_numpy(feats[0]).cuda(), Xh_minus=torch.from_numpy(feats[1]).cuda(),
+                               path="x/y.zarr")
+    (drifts, files, ifov, ref_path), _ = al.drift([im])
+    tf, tp, tm, Np, Nm = drifts[0]
+    assert (Np, Nm) == (kat[3], kat[4]) == (621, 261)
+    np.testing.assert_array_equal(tp, kat[1])
+    np.testing.assert_array_equal(tm, kat[2])
+    np.testing.assert_array_equal(tf, kat[0])
+    assert np.all(np.signbit(tf) == np.signbit(np.asarray(kat[0], np.float32)))
+
+
+def shifted(X, shift, seed, drop=0.1, jitter=0.3):
+    rng = np.random.default_rng(seed)
+    Y = X.copy()
+    Y[:, :3] += np.asarray(shift, np.float32)
+    Y[:, :3] += rng.normal(0, jitter, (len(Y), 3)).astype(np.float32)
+    keep = rng.random(len(Y)) > drop
+    return np.ascontiguousarray(Y[keep])
+
+
+@pytest.mark.parametrize("shift", [(0.0, 0.0, 0.0), (1.3, -7.6, 12.2), (-2.7, 19.4, -18.8), (3.0, 0.4, 6.6)])
+def test_translation_matches_oracle(al, feats, shift):
+    """Known shifts (cfg 3 range: +-3 z, +-20 px xy) with point loss and jitter:
+    the GPU shift equals the oracle's within 0.01 px and the match counts agree."""
+    for k, X in enumerate(feats):
+        ref = X[:, :3].copy()
+        mov = shifted(X, shift, seed=k + 7)
+        g = al.Aligner(torch.from_numpy(ref).cuda(), th=4)
+        o = oalign.Aligner(ref, th=4)
+        tg, ng = g.get_best_translation_points(torch.from_numpy(mov).cuda(), return_counts=True)
+        to, no = o.get_best_translation_points(mov, return_counts=True)
+        assert ng == no
+        np.testing.assert_allclose(tg, to, atol=0.01)
+        np.testing.assert_allclose(tg, shift, atol=0.5)
+
+
+def test_dual_aligner_and_no_points(al, feats):
+    ref = types.SimpleNamespace(Xh_plus=feats[0], Xh_minus=feats[1])
+    mov = types.SimpleNamespace(Xh_plus=shifted(feats[0], (0.5, 4.0, -3.0), 1),
+                                Xh_minus=shifted(feats[1], (0.5, 4.0, -3.0), 2))
+    got = al.DualAligner(ref, th=4).get_best_translation_pointsV2(mov)
+    want = oalign.DualAligner(ref, th=4).get_best_translation_pointsV2(mov)
+    np.testing.assert_allclose(got[0], want[0], atol=0.01)
+    assert got[3:] == want[3:]
+    with pytest.raises(ValueError, match="No points left"):
+        al.Aligner(torch.zeros((5, 3), device="cuda"), th=4)
