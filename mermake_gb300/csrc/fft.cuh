@@ -4,7 +4,7 @@
 // reference (deconvolver.py:86-90, 155-157), which carry large prime factors
 // (678 = 2*3*113, 478 = 2*239, 148 = 4*37, 118 = 2*59, ...).  A length is
 // factored into stages of three kinds:
-//   * radix 2/3/4/5/7 and the odd primes 11..37: one thread per butterfly,
+//   * radix 2/3/4/5/6/7 and the odd primes 11..37: one thread per butterfly,
 //     values in registers;
 //   * primes 41..61, 79, 89 and 113 ("lane" stage; with 59, 79, 89 and 113
 //     the primes of the reference's padded lengths such as 118 = 2*59 and
@@ -171,6 +171,29 @@ template <>
 __device__ __forceinline__ void dft_small<7, false>(float2 *v) { dft_odd<7, false>(v); }
 template <>
 __device__ __forceinline__ void dft_small<7, true>(float2 *v) { dft_odd<7, true>(v); }
+
+// radix 6 = 2 x 3: X[k] = E[k mod 3] + w6^k O[k mod 3], E/O the 3-point DFTs of
+// the even/odd samples (one pass instead of a radix-2 and a radix-3 stage)
+template <bool INV>
+__device__ __forceinline__ void dft6(float2 *v) {
+    float2 e[3] = {v[0], v[2], v[4]}, o[3] = {v[1], v[3], v[5]};
+    dft_odd<3, INV>(e);
+    dft_odd<3, INV>(o);
+    const float h = 0.5f, r = 0.86602540378443864676f;
+    // w6 = (1/2, -+sqrt3/2), w6^2 = (-1/2, -+sqrt3/2)
+    const float2 w1 = make_float2(h, INV ? r : -r), w2 = make_float2(-h, INV ? r : -r);
+    const float2 o1 = cmul(o[1], w1), o2 = cmul(o[2], w2);
+    v[0] = cadd(e[0], o[0]);
+    v[3] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], o1);
+    v[4] = csub(e[1], o1);
+    v[2] = cadd(e[2], o2);
+    v[5] = csub(e[2], o2);
+}
+template <>
+__device__ __forceinline__ void dft_small<6, false>(float2 *v) { dft6<false>(v); }
+template <>
+__device__ __forceinline__ void dft_small<6, true>(float2 *v) { dft6<true>(v); }
 
 // Odd radix 11..37 with one thread per butterfly: the paired inputs
 // a_r = x_r + x_{R-r}, b_r = x_r - x_{R-r} and the stage's cos/sin values
@@ -509,6 +532,7 @@ __device__ float2 *fft_lines(float2 *A, float2 *B, int nl, const FftPlan &P,
             case 3: stage_small<3, INV>(src, dst, P.n, nl, Ns, tw_s); break;
             case 4: stage_small<4, INV>(src, dst, P.n, nl, Ns, tw_s); break;
             case 5: stage_small<5, INV>(src, dst, P.n, nl, Ns, tw_s); break;
+            case 6: stage_small<6, INV>(src, dst, P.n, nl, Ns, tw_s); break;
             case 7: stage_small<7, INV>(src, dst, P.n, nl, Ns, tw_s); break;
             MM_ODD_CASE(11) MM_ODD_CASE(13) MM_ODD_CASE(17) MM_ODD_CASE(19) MM_ODD_CASE(23)
             MM_ODD_CASE(29) MM_ODD_CASE(31) MM_ODD_CASE(37)

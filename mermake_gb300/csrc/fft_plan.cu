@@ -3,6 +3,7 @@
 #include <math.h>
 #include <stdlib.h>
 
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <utility>
@@ -22,6 +23,15 @@ void factor(int n, std::vector<int> &first, std::vector<int> &small) {
     while (n % 2 == 0) { small.push_back(2); n /= 2; }
     for (int p : {3, 5, 7})
         while (n % p == 0) { small.push_back(p); n /= p; }
+    // a 2 and a 3 become one radix-6 pass
+    {
+        auto i2 = std::find(small.begin(), small.end(), 2);
+        auto i3 = std::find(small.begin(), small.end(), 3);
+        if (i2 != small.end() && i3 != small.end()) {
+            small.erase(i3);
+            *std::find(small.begin(), small.end(), 2) = 6;
+        }
+    }
     std::vector<int> mid;
     for (int p = 11; (long)p * p <= n; p += 2)
         while (n % p == 0) { (p <= 37 ? mid : first).push_back(p); n /= p; }

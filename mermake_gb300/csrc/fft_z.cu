@@ -18,6 +18,7 @@ constexpr int kSmemLimit = kFftSmemLimit;
 // L1) when they share a spectrum.  The CTA walks the batch group by group.
 // ---------------------------------------------------------------------------
 constexpr int kZThreads = 256;
+constexpr int kZq = 16;  // plane positions per CTA
 
 template <int LMAX>
 __global__ void __launch_bounds__(kZThreads, 1)
@@ -25,20 +26,36 @@ k_zpass(TileGeom g, float2 *__restrict__ S, const float2 *__restrict__ W, long l
         int tg) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = P.n, lnl = log2_pow2(nl);
-    const int nq = nl / tg, lnq = log2_pow2(nq);
+    const int lnq = log2_pow2(kZq);
     const FftSmem L = fft_smem_layout(smem_raw, P, nl);
-    int *zmap = reinterpret_cast<int *>(reinterpret_cast<unsigned char *>(L.scr) +
-                                        sizeof(float4) * MM_FFT_SCR_PER_WARP * (kZThreads / 32));
+    // the Wiener chunk of the CTA's kZq positions (Zp x kZq), then the z map
+    float2 *Ws = reinterpret_cast<float2 *>(reinterpret_cast<unsigned char *>(L.scr) +
+                                            sizeof(float4) * MM_FFT_SCR_PER_WARP * (kZThreads / 32));
+    int *zmap = reinterpret_cast<int *>(Ws + (size_t)n * kZq);
     fft_load_tables(P, L.tw, L.tab);
     for (int e = threadIdx.x; e < n; e += blockDim.x) zmap[e] = mm_map_z(e, g.Z, g.zpad, g.Zp);
     __syncthreads();
     const long long plane = (long long)g.P * g.H;
-    const long long q0 = (long long)blockIdx.x * nq;
+    const long long q0 = (long long)blockIdx.x * kZq;
+    int wpsf = -1;
     for (int t0 = 0; t0 < g.nt; t0 += tg) {
+        // with several spectra a group is one tile (tg == 1); with one spectrum
+        // the chunk is staged once and reused by every group
+        const int psf = g.npsf == 1 ? 0 : g.t0 + t0;
+        if (psf != wpsf) {
+            for (int it = threadIdx.x; it < kZq * n; it += blockDim.x) {
+                const int qo = it & (kZq - 1), e = it >> lnq;
+                if (q0 + qo < plane)
+                    cp_async8(&Ws[e * kZq + qo], &W[(long long)psf * wstride + e * plane + q0 + qo]);
+                else
+                    Ws[e * kZq + qo] = make_float2(0.f, 0.f);
+            }
+            wpsf = psf;
+        }
         for (int it = threadIdx.x; it < nl * n; it += blockDim.x) {
             const int l = it & (nl - 1), e = it >> lnl;
             const int t = t0 + (l >> lnq);
-            const long long q = q0 + (l & (nq - 1));
+            const long long q = q0 + (l & (kZq - 1));
             const int src = zmap[e];
             if (src >= 0 && t < g.nt && q < plane)
                 cp_async8(&L.A[sidx(e, l, nl)], &S[((long long)t * g.Z + src) * plane + q]);
@@ -50,21 +67,14 @@ k_zpass(TileGeom g, float2 *__restrict__ S, const float2 *__restrict__ W, long l
         float2 *R = fft_lines<false, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
         for (int it = threadIdx.x; it < nl * n; it += blockDim.x) {
             const int l = it & (nl - 1), e = it >> lnl;
-            const int t = t0 + (l >> lnq);
-            const long long q = q0 + (l & (nq - 1));
-            float2 w = make_float2(0.f, 0.f);
-            if (t < g.nt && q < plane) {
-                const TileDesc d = mm_tile_desc(g, g.t0 + t);
-                w = __ldg(&W[(long long)d.psf * wstride + e * plane + q]);
-            }
-            R[sidx(e, l, nl)] = cmul(R[sidx(e, l, nl)], w);
+            R[sidx(e, l, nl)] = cmul(R[sidx(e, l, nl)], Ws[e * kZq + (l & (kZq - 1))]);
         }
         __syncthreads();
         float2 *R2 = fft_lines<true, LMAX>(R, R == L.A ? L.B : L.A, nl, P, L.tw, L.tab, L.scr);
         for (int it = threadIdx.x; it < nl * g.Z; it += blockDim.x) {
             const int l = it & (nl - 1), z = it >> lnl;
             const int t = t0 + (l >> lnq);
-            const long long q = q0 + (l & (nq - 1));
+            const long long q = q0 + (l & (kZq - 1));
             if (t < g.nt && q < plane) S[((long long)t * g.Z + z) * plane + q] = R2[sidx(g.zpad + z, l, nl)];
         }
         __syncthreads();
@@ -102,17 +112,19 @@ int mm_launch_zpass(const TileGeom &g, float2 *S, const float2 *W, long long wst
     FftPlan P;
     int rc = mm_fft_plan_get(g.Zp, &P);
     if (rc) return rc;
-    // lines per CTA: 64 when they fit, tiles per group up to 4 (a power of two)
+    // lines per CTA: kZq positions of tg tiles (tg up to 4, one tile when each
+    // tile has its own spectrum), fewer positions' worth of tiles if too large
     auto bytes = [&](int l) {
-        return fft_smem_bytes(P.n, P.ntab, l, kZThreads / 32) + sizeof(int) * (size_t)P.n;
+        return fft_smem_bytes(P.n, P.ntab, l, kZThreads / 32) + sizeof(float2) * (size_t)P.n * kZq +
+               sizeof(int) * (size_t)P.n;
     };
-    int nl = 64;
-    while (nl > 1 && bytes(nl) > (size_t)kSmemLimit) nl >>= 1;
     int tg = 1;
-    while (tg < 4 && tg * 2 <= g.nt && tg * 2 <= nl) tg *= 2;
-    const int nq = nl / tg;
+    if (g.npsf == 1)
+        while (tg < 4 && tg * 2 <= g.nt && bytes(kZq * tg * 2) <= (size_t)kSmemLimit) tg *= 2;
+    int nl = kZq * tg;
+    MM_REQUIRE(bytes(nl) <= (size_t)kSmemLimit, "padded depth %d too large for the z pass", g.Zp);
     size_t sm = bytes(nl);
-    dim3 grid(mm_cdiv((long)g.P * g.H, nq));
+    dim3 grid(mm_cdiv((long)g.P * g.H, kZq));
     TileGeom ga = g;
     void *args[] = {&ga, &S, &W, &wstride, &P, &nl, &tg};
     const void *fn = MM_BY_CLASS(P, k_zpass, );

@@ -16,8 +16,8 @@
 // k_fit      one warp per spot: gathers the sphere |d|^2 <= delta_fit^2 in the
 //            reference's (dz, dx, dy) order (first 600 in-range samples,
 //            maxima.cu:148, 190-232) and forms every output of
-//            delta_fit_cross_corr from moment sums (float32 per lane on
-//            centre-shifted values, double across the warp):
+//            delta_fit_cross_corr from moment sums (float32 on centre-shifted
+//            values, statistics in double):
 //              bg = min v;  centroid = sum (c+d)(v-bg) / sum (v-bg)  (fallback c);
 //              hn = cov(v, G) / (std'(v) std(G));  a = cov(raw, G) / (std'(raw) std(G))
 //            with std' = std, or 1 where std == 0 (maxima.cu:233-341).  std(G) == 0
@@ -172,19 +172,41 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
     }
 }
 
-__device__ __forceinline__ double wsum(double v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
+// Sums 16 per-lane values over the warp with a reduce-scatter (16 + 15
+// shuffles instead of 16 x 5): afterwards lane 0 holds all 16 totals.
+__device__ __forceinline__ void warp_sum16(float (&v)[16], unsigned lane) {
+#pragma unroll
+    for (int w = 8, off = 16; w >= 1; w >>= 1, off >>= 1) {
+        const bool up = lane & off;
+#pragma unroll
+        for (int j = 0; j < w; ++j) {
+            const float send = up ? v[j] : v[j + w];
+            const float keep = up ? v[j + w] : v[j];
+            v[j] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+        }
+    }
+    // lane L now holds in v[0] the sum over lanes sharing bit 0 of value
+    // index idx(L) = bits 4..1 of L read as (b4 b3 b2 b1) -> 8*b4 + 4*b3 + 2*b2 + b1
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+    const float mine = v[0];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        const int src = ((i >> 3) & 1) << 4 | ((i >> 2) & 1) << 3 | ((i >> 1) & 1) << 2 | (i & 1) << 1;
+        v[i] = __shfl_sync(0xffffffffu, mine, src);
+    }
 }
 
 // Per-spot fit.  Each lane sums its samples in float32 after shifting the
 // image and raw values by the centre voxel's (every moment used below is
-// shift-invariant, so the shift removes the cancellation); the warp reduction
-// and the final statistics are double precision.
+// shift-invariant, so the shift removes the cancellation); the warp adds the
+// lanes' sums and lane 0 forms the statistics in double precision.  The
+// Gaussian weights depend only on the offset and the sigmas, so a block
+// tabulates them once.
 __global__ void __launch_bounds__(256)
 k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand, unsigned cap, int delta_fit,
       float sigmaZ, float sigmaXY, Xform t, float *__restrict__ out, unsigned out_cap,
       unsigned *__restrict__ out_count, int keep_filter) {
+    __shared__ float gtab[kSphereCap];
     t = xf_resolve(t);
     const unsigned lane = threadIdx.x & 31;
     const unsigned nc = min(*ncand, cap);
@@ -193,6 +215,12 @@ k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand
     const int nsamp = table ? g_fit_sphere_n[delta_fit] : side * side * side;
     const int df2 = delta_fit * delta_fit;
     const float gz = 2 * sigmaZ * sigmaZ, gxy = 2 * sigmaXY * sigmaXY;
+    if (table)
+        for (int i = threadIdx.x; i < nsamp; i += blockDim.x) {
+            const char4 o = g_fit_sphere[delta_fit][i];
+            gtab[i] = expf(-(o.x * o.x / gz + o.y * o.y / gxy + o.z * o.z / gxy));
+        }
+    __syncthreads();
     for (unsigned s = (blockIdx.x * blockDim.x + threadIdx.x) / 32; s < nc; s += gridDim.x * blockDim.x / 32) {
         uint2 c = cand[s];
         const int z0 = c.x & 0xffff, x0 = c.x >> 16, y0 = c.y & 0xffff, vi = c.y >> 16;
@@ -203,8 +231,10 @@ k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand
         const float *img = V.img + vi * V.ivol;
         const float cv = xf(img[z0 * V.isz + x0 * V.isx + y0], t);
         const float crw = raw_at(V, vi, d, z0, x0, y0);
-        float n = 0, sv = 0, svv = 0, sg = 0, sgg = 0, svg = 0, sr = 0, srr = 0, srg = 0;
-        float sdz = 0, sdx = 0, sdy = 0, svdz = 0, svdx = 0, svdy = 0;
+        // n, sv, svv, sg, sgg, svg, sr, srr, srg, sdz, sdx, sdy, svdz, svdx, svdy, (unused)
+        float acc[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) acc[i] = 0.f;
         float vmin = 1e20f;
         int taken = 0;  // in-range samples before this chunk (cap 600, maxima.cu:194)
         for (int c0 = 0; c0 < nsamp && taken < 600; c0 += 32) {
@@ -237,23 +267,24 @@ k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand
             if (ok && rank < 600) {
                 const float v = xf(img[zz * V.isz + xx * V.isx + yy], t);
                 const float r = raw_at(V, vi, d, zz, xx, yy);
-                const float g = expf(-(dz * dz / gz + dx * dx / gxy + dy * dy / gxy));
+                const float g = table ? gtab[ci] : expf(-(dz * dz / gz + dx * dx / gxy + dy * dy / gxy));
                 const float dv = v - cv, dr = r - crw;
-                n += 1.f;
-                sv += dv; svv += dv * dv;
-                sg += g; sgg += g * g; svg += dv * g;
-                sr += dr; srr += dr * dr; srg += dr * g;
-                sdz += (float)dz; sdx += (float)dx; sdy += (float)dy;
-                svdz += dv * dz; svdx += dv * dx; svdy += dv * dy;
+                acc[0] += 1.f;
+                acc[1] += dv; acc[2] += dv * dv;
+                acc[3] += g; acc[4] += g * g; acc[5] += dv * g;
+                acc[6] += dr; acc[7] += dr * dr; acc[8] += dr * g;
+                acc[9] += (float)dz; acc[10] += (float)dx; acc[11] += (float)dy;
+                acc[12] += dv * dz; acc[13] += dv * dx; acc[14] += dv * dy;
                 vmin = fminf(vmin, v);
             }
         }
-        const double N = wsum(n), Sv = wsum(sv), Svv = wsum(svv), Sg = wsum(sg), Sgg = wsum(sgg), Svg = wsum(svg);
-        const double Sr = wsum(sr), Srr = wsum(srr), Srg = wsum(srg);
-        const double Sdz = wsum(sdz), Sdx = wsum(sdx), Sdy = wsum(sdy);
-        const double Svdz = wsum(svdz), Svdx = wsum(svdx), Svdy = wsum(svdy);
+        warp_sum16(acc, lane);
         for (int o = 16; o > 0; o >>= 1) vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
+        const double N = acc[0];
         if (lane != 0 || N == 0) continue;
+        const double Sv = acc[1], Svv = acc[2], Sg = acc[3], Sgg = acc[4], Svg = acc[5];
+        const double Sr = acc[6], Srr = acc[7], Srg = acc[8];
+        const double Sdz = acc[9], Sdx = acc[10], Sdy = acc[11], Svdz = acc[12], Svdx = acc[13], Svdy = acc[14];
         const double mg = Sg / N, mv = Sv / N, mr = Sr / N;
         const double varg = fmax(Sgg / N - mg * mg, 0.0);
         const double varv = fmax(Svv / N - mv * mv, 0.0);
