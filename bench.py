@@ -271,10 +271,18 @@ def gpu_arm(args, rank, world, local):
     peak_src = "measured" if peak else "fallback"
     peak = peak or 6800.0
     achieved = (dbytes / dl) / ((dms / dl) / 1e3) / 1e9
+    # DRAM traffic of the dominant kernel per launch: ncu's bytes per tile on
+    # the quad workload, scaled by the tiles one launch of this run processes
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    tp = os.path.join(ROOT, "profiles", "dram_traffic_quad.json")
     if os.path.exists(tp):
-        traffic = json.load(open(tp)).get(dom)
+        e = json.load(open(tp))["stages"].get(dom)
+        if e:
+            shape = (w["Z"], w["X"], w["Y"])
+            tiles = len(s["dec_h"].tile_boxes(shape)) * w["colours"]
+            if s["dec_d"] is not None:
+                tiles += len(s["dec_d"].tile_boxes(shape))
+            traffic = e["per_tile"] * tiles * args.steps / dl + e["per_launch"]
     stage_share = {k: round(v[0] / sum(x[0] for x in stages.values()), 4) for k, v in stages.items()}
 
     line = {
@@ -300,6 +308,7 @@ def gpu_arm(args, rank, world, local):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+                     "traffic_source": "profiles/dram_traffic_quad.json scaled by tiles per launch" if traffic else None,
                      "bytes_per_launch": dbytes / dl, "ms_per_launch": dms / dl,
                      "stage_share": stage_share},
         "clocks": clk.summary(),

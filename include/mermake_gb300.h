@@ -72,6 +72,12 @@ int mm_subtract_u16(const uint16_t *x, const int64_t *x_strides, const uint16_t 
                     uint16_t *z, const int64_t *z_strides, int ndim, const int64_t *shape, int mode,
                     void *stream);
 
+/* cp.median of a float32 array as load_flats uses it (mermake/io.py:42-54):
+ * writes the median to *median (host) -- the mean in float32 of the two middle
+ * values when n is even -- and, when out is not NULL, out[i] = x[i] / median
+ * (io.py:52).  Synchronises the stream. */
+int mm_median_f32(mm_ctx *ctx, const float *x, int64_t n, float *median, float *out, void *stream);
+
 /* Deconvolver.__init__ for one PSF (mermake/deconvolver.py:48-75 with
  * center_psf 238-270 and laplacian_3d 24-36): writes the Wiener spectrum
  * conj(H)/(|H|^2 + beta |L|^2), pre-divided by Zp*P*P, as the half spectrum

@@ -61,6 +61,7 @@ _SIGS = {
                        _i32, _i32, _f32, _f32, _i32, _vp, _vp, _u32, _pu32, _vp, _u32, _pu32, _pf32, _vp], _i32),
     "mm_tile_geometry": ([_i32] * 8 + [_vp] * 4, _i32),
     "mm_fft_c2c": ([_vp, _i32, _i32, _i32, _vp], _i32),
+    "mm_median_f32": ([_vp, _vp, _i64, _pf32, _vp, _vp], _i32),
     "mm_aligner_create": ([_vp, _i32, _i32, _i64, _f32, _i32, _i32, C.POINTER(_vp), _vp], _i32),
     "mm_aligner_translation": ([_vp, _vp, _i32, _i32, _i64, _f32, _pf32, C.POINTER(_i32), _vp], _i32),
     "mm_aligner_info": ([_vp, C.POINTER(_i32), C.POINTER(_i32), C.POINTER(_i32)], _i32),

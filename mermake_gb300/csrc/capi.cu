@@ -12,7 +12,7 @@
 namespace {
 thread_local char g_err[1024] = "";
 
-enum Slot { WS_SPEC = 0, WS_RES, WS_TMP, WS_VOL, WS_CAND, WS_SMALL, WS_N };
+enum Slot { WS_SPEC = 0, WS_RES, WS_TMP, WS_VOL, WS_CAND, WS_SMALL, WS_SELECT, WS_N };
 }  // namespace
 
 static std::atomic<unsigned long long> g_launches{0};
@@ -571,3 +571,21 @@ extern "C" int mm_profile_read(mm_ctx *c, int nmax, double *ms, double *bytes, i
 extern "C" const char *mm_stage_name(int i) { return (i >= 0 && i < ST_N) ? kStageNames[i] : ""; }
 
 extern "C" uint64_t mm_launch_count(void) { return mm_launch_counter_get(); }
+
+int mm_median_impl(const float *x, long long n, unsigned *scratch, float *med_dev, float *out, cudaStream_t st);
+
+extern "C" int mm_median_f32(mm_ctx *c, const float *x, int64_t n, float *median, float *out, void *stream) {
+    MM_REQUIRE(c && x && median, "null argument");
+    MM_REQUIRE(n > 0, "median of an empty array");
+    std::lock_guard<std::mutex> lock(c->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    void *scr;
+    int rc;
+    if ((rc = ws_get(c, WS_SELECT, sizeof(unsigned) * 272, &scr))) return rc;
+    float *med_dev = reinterpret_cast<float *>(static_cast<unsigned *>(scr) + 264);
+    if ((rc = mm_median_impl(x, n, static_cast<unsigned *>(scr), med_dev, out, st))) return rc;
+    MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters + 8, med_dev, sizeof(float), cudaMemcpyDeviceToHost, st));
+    MM_CUDA_TRY(cudaStreamSynchronize(st));
+    memcpy(median, c->h_counters + 8, sizeof(float));
+    return MM_OK;
+}

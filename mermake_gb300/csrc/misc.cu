@@ -185,3 +185,99 @@ int mm_launch_rms_div(const double *sumsq, long long n, float *div, cudaStream_t
     MM_CHECK_LAUNCH();
     return MM_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Median of a float32 array (cp.median in mermake/io.py:52): the k-th smallest
+// value by radix selection over the order-preserving bit pattern of the floats,
+// four 8-bit digits, one histogram per digit; an even count averages the two
+// middle values in float32 ((a + b) / 2), as the reference's mean does.
+// ---------------------------------------------------------------------------
+namespace {
+
+__device__ __forceinline__ unsigned f2key(float f) {
+    const unsigned u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float key2f(unsigned k) {
+    const unsigned u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(u);
+}
+
+// state: [0] prefix, [1] mask, [2] rank still to skip inside the prefix
+__global__ void k_select_hist(const float *__restrict__ x, long long n, const unsigned *__restrict__ state,
+                              int shift, unsigned *__restrict__ hist) {
+    __shared__ unsigned h[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    const unsigned prefix = state[0], mask = state[1];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const unsigned k = f2key(x[i]);
+        if ((k & mask) == prefix) atomicAdd(&h[(k >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 256; i += blockDim.x)
+        if (h[i]) atomicAdd(&hist[i], h[i]);
+}
+
+__global__ void k_select_pick(unsigned *__restrict__ state, unsigned *__restrict__ hist, int shift) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    unsigned r = state[2];
+    int b = 0;
+    for (; b < 255; ++b) {
+        if (r < hist[b]) break;
+        r -= hist[b];
+    }
+    state[0] |= (unsigned)b << shift;
+    state[1] |= 255u << shift;
+    state[2] = r;
+    for (int i = 0; i < 256; ++i) hist[i] = 0;
+}
+
+__global__ void k_select_init(unsigned *__restrict__ state, unsigned long long rank, unsigned *__restrict__ hist) {
+    state[0] = 0;
+    state[1] = 0;
+    state[2] = (unsigned)rank;
+    for (int i = 0; i < 256; ++i) hist[i] = 0;
+}
+
+__global__ void k_median_finish(const unsigned *__restrict__ s_lo, const unsigned *__restrict__ s_hi, int even,
+                                float *__restrict__ med) {
+    const float a = key2f(s_lo[0]);
+    med[0] = even ? (a + key2f(s_hi[0])) / 2.0f : a;
+}
+
+__global__ void k_divide(const float *__restrict__ x, long long n, const float *__restrict__ d, float *__restrict__ out) {
+    const float dv = d[0];
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = __fdiv_rn(x[i], dv);
+}
+
+int select_kth(const float *x, long long n, unsigned long long k, unsigned *state, unsigned *hist, cudaStream_t st) {
+    k_select_init<<<1, 1, 0, st>>>(state, k, hist);
+    MM_CHECK_LAUNCH();
+    for (int shift = 24; shift >= 0; shift -= 8) {
+        k_select_hist<<<grid_for(n), 256, 0, st>>>(x, n, state, shift, hist);
+        MM_CHECK_LAUNCH();
+        k_select_pick<<<1, 1, 0, st>>>(state, hist, shift);
+        MM_CHECK_LAUNCH();
+    }
+    return MM_OK;
+}
+
+}  // namespace
+
+int mm_median_impl(const float *x, long long n, unsigned *scratch, float *med_dev, float *out, cudaStream_t st) {
+    // scratch: 2 x 4 state words + 256 histogram words
+    unsigned *s_lo = scratch, *s_hi = scratch + 4, *hist = scratch + 8;
+    int rc;
+    const int even = (n % 2) == 0;
+    if ((rc = select_kth(x, n, even ? n / 2 - 1 : n / 2, s_lo, hist, st))) return rc;
+    if (even && (rc = select_kth(x, n, n / 2, s_hi, hist, st))) return rc;
+    k_median_finish<<<1, 1, 0, st>>>(s_lo, s_hi, even, med_dev);
+    MM_CHECK_LAUNCH();
+    if (out) {
+        k_divide<<<grid_for(n), 256, 0, st>>>(x, n, med_dev, out);
+        MM_CHECK_LAUNCH();
+    }
+    return MM_OK;
+}
