@@ -86,11 +86,24 @@ int mm_median_f32(mm_ctx *ctx, const float *x, int64_t n, float *median, float *
 int mm_wiener_spectrum(mm_ctx *ctx, const float *psf, int pz, int px, int py, int tile_height, int tile_size,
                        int zpad, int overlap, float beta, void *W, void *stream);
 
+/* The z step of tile_wise for one spectrum as a matrix per frequency
+ * (mermake/deconvolver.py:139-157: z padding by reflection, FFT over Zp, times
+ * W, inverse FFT, keep planes [zpad, zpad + Z)).  No counterpart in the
+ * reference, which transforms every tile over the padded depth.  Writes zop,
+ * (Z, Z, P, P/2+1) complex64 (8 Z^2 P (P/2+1) bytes, 4.6 GB at Z = 50,
+ * P = 678), from W as made by mm_wiener_spectrum with the same geometry.
+ * Passing zop to mm_deconv_tiles / mm_hyb_spots / mm_dapi_spots replaces the
+ * two padded-depth transforms by one complex matrix product per frequency over
+ * the tiles of a batch.  Z <= 128 and Zp <= 400 (MM_EINVAL beyond). */
+int mm_wiener_zop(mm_ctx *ctx, const void *W, int tile_height, int zpad, int tile_size, int overlap, void *zop,
+                  void *stream);
+
 /* Deconvolver.tile_wise / apply (mermake/deconvolver.py:98-184) for tiles
  * [tile_begin, tile_begin + tile_count) of the x-major tile grid of a
  * (Z, X, Y) channel, uint16 or float32 (image_dtype; strides isz, isx, 1).  flat: float32 (X, Y) with row stride fsx, or NULL.
  * W: npsf spectra as made by mm_wiener_spectrum (tile i uses spectrum i when
- * npsf > 1).  blur_radius < 0: no background subtraction.
+ * npsf > 1).  zop: NULL, or the z operator of W made by mm_wiener_zop
+ * (npsf == 1 only).  blur_radius < 0: no background subtraction.
  * Outputs (any may be NULL):
  *   res_out    (tile_count, Z, P, P) float32: tile_res after blur subtraction;
  *              the yielded view is [:, :xend, :yend]
@@ -99,8 +112,8 @@ int mm_wiener_spectrum(mm_ctx *ctx, const float *psf, int pz, int px, int py, in
  *   stitch_out (Z, X, Y) float32 with strides (osz, osx, 1): tile centres
  *              written as Deconvolver.apply does (deconvolver.py:179-183). */
 int mm_deconv_tiles(mm_ctx *ctx, const void *image, int image_dtype, int Z, int X, int Y, int64_t isz, int64_t isx,
-                    const float *flat, int64_t fsx, const void *W, int npsf, int tile_size, int zpad,
-                    int overlap, int tile_begin, int tile_count, int blur_radius, float *res_out, float *raw_out,
+                    const float *flat, int64_t fsx, const void *W, int npsf, const void *zop, int tile_size,
+                    int zpad, int overlap, int tile_begin, int tile_count, int blur_radius, float *res_out, float *raw_out,
                     float *stitch_out, int64_t osz, int64_t osx, void *stream);
 
 /* find_local_maxima (mermake/maxima.py:17-98; kernels local_maxima_count,
@@ -141,9 +154,9 @@ int mm_find_local_maxima_noalloc(const float *image, int Z, int X, int Y, int64_
  * specified, as in the reference); *count = total rows; MM_EOVERFLOW if it
  * exceeds out_cap. */
 int mm_hyb_spots(mm_ctx *ctx, const uint16_t *image, int Z, int X, int Y, int64_t isz, int64_t isx,
-                 const float *flat, int64_t fsx, const void *W, int npsf, int tile_size, int zpad, int overlap,
-                 int blur_radius, float threshold, int delta, int delta_fit, float sigmaZ, float sigmaXY,
-                 int batch, float *out, uint32_t out_cap, uint32_t *count, void *stream);
+                 const float *flat, int64_t fsx, const void *W, int npsf, const void *zop, int tile_size,
+                 int zpad, int overlap, int blur_radius, float threshold, int delta, int delta_fit, float sigmaZ,
+                 float sigmaXY, int batch, float *out, uint32_t out_cap, uint32_t *count, void *stream);
 
 /* The DAPI block (mermake/__main__.py:215-225): Deconvolver.apply into `buffer`
  * (Z, X, Y) float32, divide by the RMS, find_local_maxima (+), negate,
@@ -151,9 +164,9 @@ int mm_hyb_spots(mm_ctx *ctx, const uint16_t *image, int Z, int X, int Y, int64_
  * and negation are applied on read; `buffer` keeps the un-normalised result.
  * *rms receives the divisor used (float). */
 int mm_dapi_spots(mm_ctx *ctx, const uint16_t *image, int Z, int X, int Y, int64_t isz, int64_t isx,
-                  const float *flat, int64_t fsx, const void *W, int npsf, int tile_size, int zpad, int overlap,
-                  int blur_radius, float threshold, int delta, int delta_fit, float sigmaZ, float sigmaXY,
-                  int batch, float *buffer, float *out_plus, uint32_t cap_plus, uint32_t *count_plus,
+                  const float *flat, int64_t fsx, const void *W, int npsf, const void *zop, int tile_size,
+                  int zpad, int overlap, int blur_radius, float threshold, int delta, int delta_fit, float sigmaZ,
+                  float sigmaXY, int batch, float *buffer, float *out_plus, uint32_t cap_plus, uint32_t *count_plus,
                   float *out_minus, uint32_t cap_minus, uint32_t *count_minus, float *rms, void *stream);
 
 /* Tile layout of Deconvolver.tiled / tile_wise (mermake/deconvolver.py:117-148,

@@ -49,16 +49,17 @@ _SIGS = {
     "mm_box_1d_f32": ([_vp, _pi64, _vp, _pi64, _i32, _i32, _i32, _i32, _i32, _vp], _i32),
     "mm_subtract_u16": ([_vp, _pi64, _vp, _pi64, _vp, _pi64, _i32, _pi64, _i32, _vp], _i32),
     "mm_wiener_spectrum": ([_vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _i32, _f32, _vp, _vp], _i32),
-    "mm_deconv_tiles": ([_vp, _vp, _i32, _i32, _i32, _i32, _i64, _i64, _vp, _i64, _vp] + [_i32] * 7
+    "mm_wiener_zop": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp], _i32),
+    "mm_deconv_tiles": ([_vp, _vp, _i32, _i32, _i32, _i32, _i64, _i64, _vp, _i64, _vp, _i32, _vp] + [_i32] * 6
                         + [_vp, _vp, _vp, _i64, _i64, _vp], _i32),
     "mm_find_local_maxima": ([_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i32, _i64, _i64, _f32, _i32, _i32,
                               _f32, _f32, _f32, _i32, _vp, _u32, _pu32, _vp], _i32),
     "mm_find_local_maxima_noalloc": ([_vp, _i32, _i32, _i32, _i64, _i64, _vp, _i32, _i64, _i64, _f32, _i32, _i32,
                                       _f32, _f32, _f32, _i32, _vp, _u32, _pu32, _vp], _i32),
-    "mm_hyb_spots": ([_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i64, _vp, _i32, _i32, _i32, _i32, _i32, _f32,
+    "mm_hyb_spots": ([_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i64, _vp, _i32, _vp, _i32, _i32, _i32, _i32, _f32,
                       _i32, _i32, _f32, _f32, _i32, _vp, _u32, _pu32, _vp], _i32),
-    "mm_dapi_spots": ([_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i64, _vp, _i32, _i32, _i32, _i32, _i32, _f32,
-                       _i32, _i32, _f32, _f32, _i32, _vp, _vp, _u32, _pu32, _vp, _u32, _pu32, _pf32, _vp], _i32),
+    "mm_dapi_spots": ([_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i64, _vp, _i32, _vp, _i32, _i32, _i32, _i32,
+                       _f32, _i32, _i32, _f32, _f32, _i32, _vp, _vp, _u32, _pu32, _vp, _u32, _pu32, _pf32, _vp], _i32),
     "mm_tile_geometry": ([_i32] * 8 + [_vp] * 4, _i32),
     "mm_fft_c2c": ([_vp, _i32, _i32, _i32, _vp], _i32),
     "mm_median_f32": ([_vp, _vp, _i64, _pf32, _vp, _vp], _i32),

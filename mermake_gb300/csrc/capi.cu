@@ -173,8 +173,9 @@ int fill_geom(TileGeom &g, int Z, int X, int Y, long long isz, long long isx, lo
 
 
 // tile_wise core for tiles [g.t0, g.t0 + g.nt)
-int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *flat, const float2 *W, int blur_radius,
-              float *res_out, float *raw_out, float *stitch, long long osz, long long osx, cudaStream_t st) {
+int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *flat, const float2 *W,
+              const float2 *zop, int blur_radius, float *res_out, float *raw_out, float *stitch, long long osz,
+              long long osx, cudaStream_t st) {
     const long long plane_c = (long long)g.P * g.H;
     const long long tile_c = (long long)g.Z * plane_c;
     const long long tile_r = (long long)g.Z * g.P * g.P;
@@ -201,7 +202,11 @@ int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *
         StageTimer t(c, ST_COLS_FWD, 2 * spec_b, st);
         if ((rc = mm_launch_cols(S, g.P, g.H, g.H, plane_c, g.nt * g.Z, false, st))) return rc;
     }
-    {
+    if (zop) {
+        // the z operator (Z x Z per frequency) is read once per batch
+        StageTimer t(c, ST_ZPASS, 2 * spec_b + 8.0 * g.Z * g.Z * plane_c, st);
+        if ((rc = mm_launch_zop_apply(S, zop, g.Z, plane_c, g.nt, st))) return rc;
+    } else {
         StageTimer t(c, ST_ZPASS, 2 * spec_b + w_b, st);
         if ((rc = mm_launch_zpass(g, S, W, wstride, st))) return rc;
     }
@@ -291,14 +296,30 @@ int mm_wiener_spectrum(mm_ctx *c, const float *psf, int pz, int px, int py, int 
                                 (float *)vol, (float2 *)spec, &sm->sumsq, st);
 }
 
+int mm_wiener_zop(mm_ctx *c, const void *W, int tile_height, int zpad, int tile_size, int overlap, void *zop,
+                  void *stream) {
+    MM_REQUIRE(c && W && zop, "null argument");
+    MM_REQUIRE(tile_height > 0 && tile_size > 0 && zpad >= 0 && overlap >= 0, "bad tile geometry");
+    std::lock_guard<std::mutex> lock(c->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    const int Z = tile_height, Zp = tile_height + 2 * zpad, P = tile_size + 2 * overlap;
+    const long long plane = (long long)P * (P / 2 + 1);
+    void *E;
+    int rc;
+    if ((rc = ws_get(c, WS_VOL, mm_zop_coef_bytes(Z, Zp), &E))) return rc;
+    StageTimer tm(c, ST_WIENER, 8.0 * Zp * plane + 8.0 * Z * Z * plane, st);
+    return mm_zop_build_impl((const float2 *)W, Z, zpad, Zp, plane, (float2 *)E, (float2 *)zop, st);
+}
+
 int mm_deconv_tiles(mm_ctx *c, const void *image, int image_dtype, int Z, int X, int Y, int64_t isz, int64_t isx,
-                    const float *flat, int64_t fsx, const void *W, int npsf, int tile_size, int zpad, int overlap,
-                    int tile_begin, int tile_count, int blur_radius, float *res_out, float *raw_out,
+                    const float *flat, int64_t fsx, const void *W, int npsf, const void *zop, int tile_size, int zpad,
+                    int overlap, int tile_begin, int tile_count, int blur_radius, float *res_out, float *raw_out,
                     float *stitch_out, int64_t osz, int64_t osx, void *stream) {
     MM_REQUIRE(c && image && W, "null argument");
     TileGeom g;
     int rc = fill_geom(g, Z, X, Y, isz, isx, fsx, tile_size, zpad, overlap, npsf);
     if (rc) return rc;
+    MM_REQUIRE(!zop || npsf == 1, "a z operator needs a single spectrum (npsf == 1)");
     const int nt = ntiles_of(g);
     MM_REQUIRE(tile_begin >= 0 && tile_count >= 0 && tile_begin + tile_count <= nt,
                "tiles [%d, %d) outside the %d tiles of the channel", tile_begin, tile_begin + tile_count, nt);
@@ -308,8 +329,8 @@ int mm_deconv_tiles(mm_ctx *c, const void *image, int image_dtype, int Z, int X,
     g.t0 = tile_begin;
     g.nt = tile_count;
     std::lock_guard<std::mutex> lock(c->mu);
-    return run_tiles(c, g, image, image_dtype, flat, (const float2 *)W, blur_radius, res_out, raw_out, stitch_out, osz, osx,
-                     (cudaStream_t)stream);
+    return run_tiles(c, g, image, image_dtype, flat, (const float2 *)W, (const float2 *)zop, blur_radius, res_out,
+                     raw_out, stitch_out, osz, osx, (cudaStream_t)stream);
 }
 
 int mm_find_local_maxima(mm_ctx *c, const float *image, int Z, int X, int Y, int64_t isz, int64_t isx,
@@ -358,15 +379,16 @@ int mm_find_local_maxima(mm_ctx *c, const float *image, int Z, int X, int Y, int
 }
 
 int mm_hyb_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t isz, int64_t isx,
-                 const float *flat, int64_t fsx, const void *W, int npsf, int tile_size, int zpad, int overlap,
-                 int blur_radius, float threshold, int delta, int delta_fit, float sigmaZ, float sigmaXY, int batch,
-                 float *out, uint32_t out_cap, uint32_t *count, void *stream) {
+                 const float *flat, int64_t fsx, const void *W, int npsf, const void *zop, int tile_size, int zpad,
+                 int overlap, int blur_radius, float threshold, int delta, int delta_fit, float sigmaZ, float sigmaXY,
+                 int batch, float *out, uint32_t out_cap, uint32_t *count, void *stream) {
     MM_REQUIRE(c && image && W && count, "null argument");
     MM_REQUIRE(delta <= 5, "Delta must be an less than or equal to 5 due to MAX_KERNEL_POINTS");
     MM_REQUIRE(delta >= 0 && delta_fit >= 0, "negative delta");
     TileGeom g;
     int rc = fill_geom(g, Z, X, Y, isz, isx, fsx, tile_size, zpad, overlap, npsf);
     if (rc) return rc;
+    MM_REQUIRE(!zop || npsf == 1, "a z operator needs a single spectrum (npsf == 1)");
     const int nt = ntiles_of(g);
     if (batch <= 0) batch = nt;
     std::lock_guard<std::mutex> lock(c->mu);
@@ -385,8 +407,8 @@ int mm_hyb_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t 
             TileGeom gb = g;
             gb.t0 = t0;
             gb.nt = (t0 + batch <= nt) ? batch : nt - t0;
-            if ((rc = run_tiles(c, gb, image, MM_DTYPE_U16, flat, (const float2 *)W, blur_radius, nullptr, nullptr,
-                                nullptr, 0, 0, st)))
+            if ((rc = run_tiles(c, gb, image, MM_DTYPE_U16, flat, (const float2 *)W, (const float2 *)zop, blur_radius,
+                                nullptr, nullptr, nullptr, 0, 0, st)))
                 return rc;
             MaximaArgs a = {};
             a.img = (const float *)c->ws[WS_RES];
@@ -425,8 +447,8 @@ int mm_hyb_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t 
 }
 
 int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t isz, int64_t isx,
-                  const float *flat, int64_t fsx, const void *W, int npsf, int tile_size, int zpad, int overlap,
-                  int blur_radius, float threshold, int delta, int delta_fit, float sigmaZ, float sigmaXY,
+                  const float *flat, int64_t fsx, const void *W, int npsf, const void *zop, int tile_size, int zpad,
+                  int overlap, int blur_radius, float threshold, int delta, int delta_fit, float sigmaZ, float sigmaXY,
                   int batch, float *buffer, float *out_plus, uint32_t cap_plus, uint32_t *count_plus,
                   float *out_minus, uint32_t cap_minus, uint32_t *count_minus, float *rms, void *stream) {
     MM_REQUIRE(c && image && W && buffer && count_plus && count_minus, "null argument");
@@ -436,6 +458,7 @@ int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t
     TileGeom g;
     int rc = fill_geom(g, Z, X, Y, isz, isx, fsx, tile_size, zpad, overlap, npsf);
     if (rc) return rc;
+    MM_REQUIRE(!zop || npsf == 1, "a z operator needs a single spectrum (npsf == 1)");
     const int nt = ntiles_of(g);
     if (batch <= 0) batch = nt;
     std::lock_guard<std::mutex> lock(c->mu);
@@ -448,8 +471,8 @@ int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t
         TileGeom gb = g;
         gb.t0 = t0;
         gb.nt = (t0 + batch <= nt) ? batch : nt - t0;
-        if ((rc = run_tiles(c, gb, image, MM_DTYPE_U16, flat, (const float2 *)W, blur_radius, nullptr, nullptr, buffer,
-                            (long long)X * Y, Y, st)))
+        if ((rc = run_tiles(c, gb, image, MM_DTYPE_U16, flat, (const float2 *)W, (const float2 *)zop, blur_radius,
+                            nullptr, nullptr, buffer, (long long)X * Y, Y, st)))
             return rc;
     }
     {

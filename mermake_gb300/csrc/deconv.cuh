@@ -115,6 +115,14 @@ int mm_launch_rows_fwd_f32(const float *vol, int nrows, int P, float2 *S, cudaSt
 int mm_launch_cols(float2 *S, int n, long long se, int nlines, long long plane_stride, int nplanes,
                    bool inv, cudaStream_t st);
 int mm_launch_zpass(const TileGeom &g, float2 *S, const float2 *W, long long wstride, cudaStream_t st);
+
+// z pass as a matrix per frequency (zop.cu), single spectrum only.
+#define MM_ZOP_MAX_Z 128
+#define MM_ZOP_MAX_ZP 400
+size_t mm_zop_coef_bytes(int Z, int Zp);
+int mm_zop_build_impl(const float2 *W, int Z, int zpad, int Zp, long long plane, float2 *E, float2 *M,
+                      cudaStream_t st);
+int mm_launch_zop_apply(float2 *S, const float2 *M, int Z, long long plane, int nt, cudaStream_t st);
 int mm_launch_zfwd(float2 *S, int Zp, int plane, cudaStream_t st);
 int mm_launch_rows_inv(const float2 *S, int nrows, int P, int H, float *out, float *blur, int delta,
                        cudaStream_t st);

@@ -96,10 +96,35 @@ class Deconvolver:
             _lib.check(L.mm_wiener_spectrum(ctx, _lib.ptr(pd), *pd.shape, self.tile_height, self.tile_size,
                                             self.zpad, self.overlap, self.beta, _lib.ptr(self.psf_fft[i]), st))
         self.psf_fft = torch.view_as_complex(self.psf_fft)
+        self.z_operator = None
+        if self._want_z_operator(kwargs.get("z_operator")):
+            self.z_operator = torch.empty((self.tile_height, self.tile_height, self.P, self.H), dtype=torch.complex64,
+                                          device="cuda")
+            _lib.check(L.mm_wiener_zop(ctx, _lib.ptr(self.psf_fft), self.tile_height, self.zpad, self.tile_size,
+                                       self.overlap, _lib.ptr(self.z_operator), st))
         if self.tile_size:
             shape = (self.tile_height, self.P, self.P)
             self.tile_res = torch.empty(shape, dtype=torch.float32, device="cuda")
             self.tile_raw = torch.empty(shape, dtype=torch.float32, device="cuda")
+
+    # z operator: with one PSF, the z step of every tile is the same Z x Z
+    # complex matrix per (x, y) frequency (csrc/zop.cu); it is kept resident
+    # (8 Z^2 P (P/2+1) bytes) and replaces the padded-depth transforms.
+    Z_OPERATOR_MAX_BYTES = 16 << 30
+
+    def _want_z_operator(self, request):
+        if request is False or self.psf_fft.shape[0] != 1 or not self.tile_size:
+            return False
+        nbytes = 8 * self.tile_height ** 2 * self.P * self.H
+        ok = self.tile_height <= 128 and self.Zp <= 400
+        if request is True:
+            if not ok:
+                raise ValueError("z_operator needs tile height <= 128 and padded depth <= 400")
+            return True
+        if not ok or nbytes > self.Z_OPERATOR_MAX_BYTES:
+            return False
+        free, _ = torch.cuda.mem_get_info()
+        return nbytes <= free // 4
 
     # -- geometry ------------------------------------------------------------
     def tile_boxes(self, shape):
@@ -136,8 +161,8 @@ class Deconvolver:
         _lib.check(L.mm_deconv_tiles(
             _lib.ctx(), _lib.ptr(img), dt, Z, X, Y, img.stride(0), img.stride(1), _lib.ptr(flat),
             flat.stride(0) if flat is not None else 0, _lib.ptr(self.psf_fft), self.psf_fft.shape[0],
-            self.tile_size, self.zpad, self.overlap, t0, nt, br, _lib.ptr(res_out), _lib.ptr(raw_out),
-            _lib.ptr(stitch), stitch.stride(0) if stitch is not None else 0,
+            _lib.ptr(self.z_operator), self.tile_size, self.zpad, self.overlap, t0, nt, br, _lib.ptr(res_out),
+            _lib.ptr(raw_out), _lib.ptr(stitch), stitch.stride(0) if stitch is not None else 0,
             stitch.stride(1) if stitch is not None else 0, _lib.stream_ptr(stream)))
 
     def _check_image(self, img):

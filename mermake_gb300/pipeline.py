@@ -63,9 +63,9 @@ def hyb_spots(dec, image, flat_field=None, *, threshold=None, delta=1, delta_fit
         n = C.c_uint32(0)
         rc = L.mm_hyb_spots(_lib.ctx(img.device.index), _lib.ptr(img), Z, X, Y, img.stride(0), img.stride(1),
                             _lib.ptr(fl), fl.stride(0) if fl is not None else 0, _lib.ptr(dec.psf_fft),
-                            dec.psf_fft.shape[0], dec.tile_size, dec.zpad, dec.overlap, br, th, int(delta),
-                            int(delta_fit), float(sigmaZ), float(sigmaXY), int(batch), _lib.ptr(out), cap,
-                            C.byref(n), _lib.stream_ptr(stream))
+                            dec.psf_fft.shape[0], _lib.ptr(dec.z_operator), dec.tile_size, dec.zpad, dec.overlap,
+                            br, th, int(delta), int(delta_fit), float(sigmaZ), float(sigmaXY), int(batch),
+                            _lib.ptr(out), cap, C.byref(n), _lib.stream_ptr(stream))
         if rc == _lib.MM_EOVERFLOW:
             cap = int(n.value)
             continue
@@ -95,9 +95,9 @@ def dapi_spots(dec, image, flat_field=None, *, threshold=None, delta=1, delta_fi
         n_p, n_m, rms = C.c_uint32(0), C.c_uint32(0), C.c_float(0)
         rc = L.mm_dapi_spots(_lib.ctx(img.device.index), _lib.ptr(img), Z, X, Y, img.stride(0), img.stride(1),
                              _lib.ptr(fl), fl.stride(0) if fl is not None else 0, _lib.ptr(dec.psf_fft),
-                             dec.psf_fft.shape[0], dec.tile_size, dec.zpad, dec.overlap, br, th, int(delta),
-                             int(delta_fit), float(sigmaZ), float(sigmaXY), int(batch), _lib.ptr(buffer),
-                             _lib.ptr(op), cp, C.byref(n_p), _lib.ptr(om), cm, C.byref(n_m), C.byref(rms),
+                             dec.psf_fft.shape[0], _lib.ptr(dec.z_operator), dec.tile_size, dec.zpad,
+                             dec.overlap, br, th, int(delta), int(delta_fit), float(sigmaZ), float(sigmaXY),
+                             int(batch), _lib.ptr(buffer), _lib.ptr(op), cp, C.byref(n_p), _lib.ptr(om), cm, C.byref(n_m), C.byref(rms),
                              _lib.stream_ptr(stream))
         if rc == _lib.MM_EOVERFLOW:
             cp, cm = max(cp, int(n_p.value)), max(cm, int(n_m.value))

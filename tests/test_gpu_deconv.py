@@ -37,8 +37,9 @@ def test_wiener_spectrum_matches_oracle(dc, golden_dir):
     assert err < 1e-5, err
 
 
+@pytest.mark.parametrize("zop", [True, False])
 @pytest.mark.parametrize("k", [0, 1, 2])
-def test_deconv_tiles_match_golden_and_oracle(dc, golden_dir, k):
+def test_deconv_tiles_match_golden_and_oracle(dc, golden_dir, k, zop):
     """test_deconvolver.py:422-434 on the stored tiles: Deconvolver.apply of the
     tile's input crop, against the reference's float16 goldens and the FP64 oracle."""
     t = load_tile(golden_dir, k)
@@ -46,7 +47,8 @@ def test_deconv_tiles_match_golden_and_oracle(dc, golden_dir, k):
     Z, ts, ov = t["Z"], t["ts"], t["ov"]
     x, y, x0, x1, y0, y1 = t["box"]
     img = u16(t["img"])
-    d = dc.Deconvolver(psf, img.shape, tile_size=ts, zpad=Z, overlap=ov, beta=1e-3)
+    d = dc.Deconvolver(psf, img.shape, tile_size=ts, zpad=Z, overlap=ov, beta=1e-3, z_operator=zop)
+    assert (d.z_operator is not None) == zop
     tiles = d.tile_boxes(img.shape)
     ti = tiles.index(tuple(t["box"]))
     res = torch.empty((1, Z, d.P, d.P), device="cuda")
@@ -77,13 +79,15 @@ def small_case(seed=0, Z=10, X=50, Y=50, flat=True):
     return img, psf, fl
 
 
+@pytest.mark.parametrize("zop", [True, False])
 @pytest.mark.parametrize("ts,zpad,ov,blur", [(30, 5, 5, None), (30, 5, 5, 8), (20, 3, 7, 5), (64, 9, 11, 30),
-                                             (17, 4, 3, None)])
-def test_tile_wise_matches_oracle(dc, ts, zpad, ov, blur):
+                                             (17, 4, 3, None), (15, 4, 3, 4)])
+def test_tile_wise_matches_oracle(dc, ts, zpad, ov, blur, zop):
     """Every yielded tile and raw view of tile_wise (deconvolver.py:98-170)
-    with a flat field and optional blur subtraction."""
+    with a flat field and optional blur subtraction, with the z operator and
+    with the padded-depth transforms (P = 21: an odd plane of 21 x 11)."""
     img, psf, fl = small_case(ts + zpad)
-    d = dc.Deconvolver(psf, img.shape, tile_size=ts, zpad=zpad, overlap=ov, beta=0.01)
+    d = dc.Deconvolver(psf, img.shape, tile_size=ts, zpad=zpad, overlap=ov, beta=0.01, z_operator=zop)
     o = od.Deconvolver(psf, img.shape, tile_size=ts, zpad=zpad, overlap=ov, beta=0.01)
     n = 0
     for (x, y, res, raw), (xo, yo, rres, rraw) in zip(d.tile_wise(u16(img), torch.from_numpy(fl).cuda(), blur),
@@ -153,3 +157,28 @@ def test_apply_stitch_order_matches_reference(dc, npsf):
     ok = ~np.isnan(want)
     np.testing.assert_array_equal(got_all[ok], got_one[ok])
     assert np.abs(got_all[ok] - want[ok]).max() <= REL * np.abs(want[ok]).max()
+
+
+@pytest.mark.parametrize("Z,zpad,ts,ov", [(13, 12, 10, 3), (100, 49, 10, 3), (50, 24, 30, 9), (7, 2, 15, 3)])
+def test_z_operator_matches_padded_transforms(dc, Z, zpad, ts, ov):
+    """The z operator (one Z x Z matrix per frequency) against the FFT z pass
+    over the padded depth, on whole batches: Z not a multiple of the 10-plane
+    chunks, a batch of 25 tiles split into two tile chunks at Z = 100, and an
+    odd frequency plane (P = 21)."""
+    rng = np.random.default_rng(Z)
+    X = Y = 5 * ts
+    img = rng.integers(100, 5000, (Z, X, Y)).astype(np.uint16)
+    psf = np.zeros((5, 5, 5), np.float32)
+    psf[2, 2, 2] = 1.0
+    psf[1:4, 1:4, 1:4] += 0.1 * rng.random((3, 3, 3)).astype(np.float32)
+    args = dict(tile_size=ts, zpad=zpad, overlap=ov, beta=0.01)
+    a = dc.Deconvolver(psf, img.shape, z_operator=True, **args)
+    b = dc.Deconvolver(psf, img.shape, z_operator=False, **args)
+    nt = len(a.tile_boxes(img.shape))
+    assert nt == 25
+    ra = torch.empty((nt, Z, a.P, a.P), device="cuda")
+    rb = torch.empty_like(ra)
+    a._call(u16(img), dc.MM_DTYPE_U16, None, 0, nt, 6, res_out=ra)
+    b._call(u16(img), dc.MM_DTYPE_U16, None, 0, nt, 6, res_out=rb)
+    err = float((ra - rb).abs().max() / rb.abs().max())
+    assert err < 2e-5, err
