@@ -2,7 +2,7 @@
 """Benchmark of the per-FOV image path (deconv + blur + maxima + fit).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mermake_gb300|reference]
-                    [--workload fov3c|tile] [--form batched|plain]
+                    [--workload fov3c|quad|grid25|tile] [--form batched|plain]
 
 A step is one FOV of the workload, inputs resident in HBM:
 
@@ -13,6 +13,8 @@ A step is one FOV of the workload, inputs resident in HBM:
   threshold 3.0, delta 5, fit 5, zpad 24.
 * ``quad``: one colour of 50 x 1000 x 1000 (2 x 2 tiles), 10,000 puncta, flat
   field: the small case for profiler captures (spectra larger than L2).
+* ``grid25``: one colour of 50 x 1000 x 1000 in 5 x 5 tiles of 200 (padded
+  378): a 25-tile batch, like a colour of ``fov3c``, in a few GB.
 * ``tile``: one smFISH tile, uint16 40 x 500 x 500, 2,000 puncta, no flat field.
 
 ``value`` is FOV input voxels per second (all channels) of the batched form
@@ -49,6 +51,9 @@ WORKLOADS = {
     "quad": dict(Z=50, X=1000, Y=1000, colours=1, puncta=10000, flat=True, dapi=False, nuclei=0,
                  hyb=dict(tile_size=500, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
                           delta_fit=3, sigmaZ=1, sigmaXY=1.5)),
+    "grid25": dict(Z=50, X=1000, Y=1000, colours=1, puncta=10000, flat=True, dapi=False, nuclei=0,
+                   hyb=dict(tile_size=200, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
+                            delta_fit=3, sigmaZ=1, sigmaXY=1.5)),
     "tile": dict(Z=40, X=500, Y=500, colours=1, puncta=2000, flat=False, dapi=False, nuclei=0,
                  hyb=dict(tile_size=500, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
                           delta_fit=3, sigmaZ=1, sigmaXY=1.5)),

@@ -89,12 +89,14 @@ int mm_wiener_spectrum(mm_ctx *ctx, const float *psf, int pz, int px, int py, in
 /* The z step of tile_wise for one spectrum as a matrix per frequency
  * (mermake/deconvolver.py:139-157: z padding by reflection, FFT over Zp, times
  * W, inverse FFT, keep planes [zpad, zpad + Z)).  No counterpart in the
- * reference, which transforms every tile over the padded depth.  Writes zop,
- * (Z, Z, P, P/2+1) complex64 (8 Z^2 P (P/2+1) bytes, 4.6 GB at Z = 50,
- * P = 678), from W as made by mm_wiener_spectrum with the same geometry.
- * Passing zop to mm_deconv_tiles / mm_hyb_spots / mm_dapi_spots replaces the
- * two padded-depth transforms by one complex matrix product per frequency over
- * the tiles of a batch.  Z <= 128 and Zp <= 400 (MM_EINVAL beyond). */
+ * reference, which transforms every tile over the padded depth.  Writes the
+ * z kernel zop, (Zp, P, P/2+1) complex64 like W: the inverse DFT of W along
+ * z, from which every entry of the Z x Z matrix of a frequency is a sum of at
+ * most four samples.  Passing zop to mm_deconv_tiles / mm_hyb_spots /
+ * mm_dapi_spots replaces the two padded-depth transforms of each tile by one
+ * complex matrix product per frequency over the tiles of a batch.
+ * tile_height <= 64 and Zp <= 400, and no plane copied more than four times
+ * by the z padding (MM_EINVAL otherwise). */
 int mm_wiener_zop(mm_ctx *ctx, const void *W, int tile_height, int zpad, int tile_size, int overlap, void *zop,
                   void *stream);
 

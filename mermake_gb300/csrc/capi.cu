@@ -203,9 +203,9 @@ int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *
         if ((rc = mm_launch_cols(S, g.P, g.H, g.H, plane_c, g.nt * g.Z, false, st))) return rc;
     }
     if (zop) {
-        // the z operator (Z x Z per frequency) is read once per batch
-        StageTimer t(c, ST_ZPASS, 2 * spec_b + 8.0 * g.Z * g.Z * plane_c, st);
-        if ((rc = mm_launch_zop_apply(S, zop, g.Z, plane_c, g.nt, st))) return rc;
+        // the z kernel (Zp per frequency, the size of W) is read once per batch
+        StageTimer t(c, ST_ZPASS, 2 * spec_b + 8.0 * wstride, st);
+        if ((rc = mm_launch_zop_apply(S, zop, g.Z, g.zpad, g.Zp, plane_c, g.nt, st))) return rc;
     } else {
         StageTimer t(c, ST_ZPASS, 2 * spec_b + w_b, st);
         if ((rc = mm_launch_zpass(g, S, W, wstride, st))) return rc;
@@ -300,15 +300,13 @@ int mm_wiener_zop(mm_ctx *c, const void *W, int tile_height, int zpad, int tile_
                   void *stream) {
     MM_REQUIRE(c && W && zop, "null argument");
     MM_REQUIRE(tile_height > 0 && tile_size > 0 && zpad >= 0 && overlap >= 0, "bad tile geometry");
+    MM_REQUIRE(tile_height <= MM_ZOP_MAX_Z, "z operator needs tile height <= %d", MM_ZOP_MAX_Z);
     std::lock_guard<std::mutex> lock(c->mu);
     cudaStream_t st = (cudaStream_t)stream;
-    const int Z = tile_height, Zp = tile_height + 2 * zpad, P = tile_size + 2 * overlap;
+    const int Zp = tile_height + 2 * zpad, P = tile_size + 2 * overlap;
     const long long plane = (long long)P * (P / 2 + 1);
-    void *E;
-    int rc;
-    if ((rc = ws_get(c, WS_VOL, mm_zop_coef_bytes(Z, Zp), &E))) return rc;
-    StageTimer tm(c, ST_WIENER, 8.0 * Zp * plane + 8.0 * Z * Z * plane, st);
-    return mm_zop_build_impl((const float2 *)W, Z, zpad, Zp, plane, (float2 *)E, (float2 *)zop, st);
+    StageTimer tm(c, ST_WIENER, 16.0 * Zp * plane, st);
+    return mm_zker_build_impl((const float2 *)W, Zp, plane, (float2 *)zop, st);
 }
 
 int mm_deconv_tiles(mm_ctx *c, const void *image, int image_dtype, int Z, int X, int Y, int64_t isz, int64_t isx,

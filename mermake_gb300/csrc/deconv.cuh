@@ -116,13 +116,15 @@ int mm_launch_cols(float2 *S, int n, long long se, int nlines, long long plane_s
                    bool inv, cudaStream_t st);
 int mm_launch_zpass(const TileGeom &g, float2 *S, const float2 *W, long long wstride, cudaStream_t st);
 
-// z pass as a matrix per frequency (zop.cu), single spectrum only.
-#define MM_ZOP_MAX_Z 128
+// z pass as a matrix per frequency (zop.cu), single spectrum only: the z
+// kernel w (Zp, P, P/2+1) is the inverse DFT of W along z.
+#define MM_ZOP_MAX_Z 64
 #define MM_ZOP_MAX_ZP 400
-size_t mm_zop_coef_bytes(int Z, int Zp);
-int mm_zop_build_impl(const float2 *W, int Z, int zpad, int Zp, long long plane, float2 *E, float2 *M,
-                      cudaStream_t st);
-int mm_launch_zop_apply(float2 *S, const float2 *M, int Z, long long plane, int nt, cudaStream_t st);
+#define MM_ZOP_MAX_COPIES 4
+int mm_zop_supported(int Z, int zpad);
+int mm_zker_build_impl(const float2 *W, int Zp, long long plane, float2 *w, cudaStream_t st);
+int mm_launch_zop_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, long long plane, int nt,
+                        cudaStream_t st);
 int mm_launch_zfwd(float2 *S, int Zp, int plane, cudaStream_t st);
 int mm_launch_rows_inv(const float2 *S, int nrows, int P, int H, float *out, float *blur, int delta,
                        cudaStream_t st);

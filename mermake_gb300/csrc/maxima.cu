@@ -124,6 +124,10 @@ __device__ __forceinline__ float raw_at(const Vols &V, int vi, const TileDesc &d
     return v;
 }
 
+// A warp per (z, x) row, lanes along y: every row index is split once, loads
+// are coalesced, and each lane keeps kMaxY values of the row in flight.
+constexpr int kMaxY = 4;
+
 __global__ void __launch_bounds__(256)
 k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigned cap,
          unsigned *__restrict__ count) {
@@ -133,41 +137,51 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
     TileDesc d;
     vol_dims(V, vi, X, Y, d);
     const int Z = V.Z;
-    const long long total = (long long)Z * X * Y;
+    const int rows = Z * X;
     const float *img = V.img + vi * V.ivol;
     const int nn = g_sphere_n[delta];
     const char4 *sph = g_sphere[delta];
     const unsigned lane = threadIdx.x & 31;
-    for (long long base = (long long)blockIdx.x * blockDim.x; base < total; base += (long long)gridDim.x * blockDim.x) {
-        long long i = base + threadIdx.x;
-        bool is_max = false;
-        int z = 0, x = 0, y = 0;
-        if (i < total) {
-            z = (int)(i / ((long long)X * Y));
-            x = (int)((i / Y) % X);
-            y = (int)(i % Y);
-            float v = xf(img[z * V.isz + x * V.isx + y], t);
-            if (!(v <= th)) {  // maxima.cu:19 (a NaN threshold admits every voxel)
-                is_max = true;
-                for (int k = 0; k < nn; ++k) {
-                    char4 o = sph[k];
-                    int nz = refl(z + o.x, Z), nx = refl(x + o.y, X), ny = refl(y + o.z, Y);
-                    if (nz < 0 || nz >= Z || nx < 0 || nx >= X || ny < 0 || ny >= Y) continue;
-                    if (v < xf(img[nz * V.isz + nx * V.isx + ny], t)) {
-                        is_max = false;
-                        break;
+    const int wpb = blockDim.x >> 5;
+    for (int row = blockIdx.x * wpb + (int)(threadIdx.x >> 5); row < rows; row += gridDim.x * wpb) {
+        const int z = row / X, x = row - z * X;
+        const float *rp = img + z * V.isz + x * V.isx;
+        for (int y0 = 0; y0 < Y; y0 += 32 * kMaxY) {
+            float vals[kMaxY];
+#pragma unroll
+            for (int k = 0; k < kMaxY; ++k) {
+                const int y = y0 + 32 * k + (int)lane;
+                vals[k] = y < Y ? rp[y] : 0.f;
+            }
+#pragma unroll
+            for (int k = 0; k < kMaxY; ++k) {
+                const int y = y0 + 32 * k + (int)lane;
+                bool is_max = false;
+                if (y < Y) {
+                    const float v = xf(vals[k], t);
+                    if (!(v <= th)) {  // maxima.cu:19 (a NaN threshold admits every voxel)
+                        is_max = true;
+                        for (int q = 0; q < nn; ++q) {
+                            const char4 o = sph[q];
+                            const int nz = refl(z + o.x, Z), nx = refl(x + o.y, X), ny = refl(y + o.z, Y);
+                            if (nz < 0 || nz >= Z || nx < 0 || nx >= X || ny < 0 || ny >= Y) continue;
+                            if (v < xf(img[nz * V.isz + nx * V.isx + ny], t)) {
+                                is_max = false;
+                                break;
+                            }
+                        }
                     }
                 }
+                const unsigned m = __ballot_sync(0xffffffffu, is_max);
+                if (m) {
+                    unsigned slot = 0;
+                    const int leader = __ffs(m) - 1;
+                    if ((int)lane == leader) slot = atomicAdd(count, __popc(m));
+                    slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(m & ((1u << lane) - 1));
+                    if (is_max && slot < cap)
+                        cand[slot] = make_uint2((unsigned)z | ((unsigned)x << 16), (unsigned)y | ((unsigned)vi << 16));
+                }
             }
-        }
-        unsigned m = __ballot_sync(0xffffffffu, is_max);
-        if (m) {
-            unsigned slot = 0;
-            int leader = __ffs(m) - 1;
-            if ((int)lane == leader) slot = atomicAdd(count, __popc(m));
-            slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(m & ((1u << lane) - 1));
-            if (is_max && slot < cap)
-                cand[slot] = make_uint2((unsigned)z | ((unsigned)x << 16), (unsigned)y | ((unsigned)vi << 16));
         }
     }
 }
@@ -369,8 +383,9 @@ int mm_launch_maxima_fit(const MaximaArgs &a, uint2 *cand, unsigned cand_cap, un
     Xform t = {a.div, a.neg, a.divp};
     MM_CUDA_TRY(cudaMemsetAsync(ncand, 0, sizeof(unsigned), st));
     if (out_count && zero_out_count) MM_CUDA_TRY(cudaMemsetAsync(out_count, 0, sizeof(unsigned), st));
-    long long per = (long long)a.Z * (a.tiles ? (long long)a.tiles->P * a.tiles->P : (long long)a.X * a.Y);
-    int gx = (int)((per + 255) / 256);
+    // a warp per (z, x) row, 8 rows per CTA
+    long long rows = (long long)a.Z * (a.tiles ? (long long)a.tiles->P : (long long)a.X);
+    int gx = (int)((rows + 7) / 8);
     if (gx > 152 * 16) gx = 152 * 16;
     if (gx < 1) gx = 1;
     dim3 grid(gx, a.nvol);

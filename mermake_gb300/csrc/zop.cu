@@ -5,18 +5,19 @@
 // values, one per real plane.  The reference pads them to Zp planes (reflect
 // at zpad and zpad+Z-1, mm_map_z), transforms over Zp, multiplies by W, and
 // transforms back, then keeps planes [zpad, zpad+Z).  That is a linear map of
-// the Z values:
+// the Z values, Y[i] = sum_j M_p[i][j] X[j], and because padding only copies
+// planes, every entry is a sum of samples of one vector per frequency:
 //
-//   Y[i] = sum_j M_p[i][j] X[j],
-//   M_p[i][j] = sum_kz E[i][j][kz] W[kz][p],
-//   E[i][j][kz] = sum_{z : map_z(z) = j} exp(+2 pi i kz (zpad + i - z) / Zp)
+//   M_p[i][j] = sum_{z : map_z(z) = j} w_p[(zpad + i - z) mod Zp],
+//   w_p[d]    = sum_kz W[kz][p] exp(+2 pi i kz d / Zp)
 //
-// (W already holds the 1 / (Zp P P) normalisation of both inverse transforms).
-// With one spectrum every tile of a batch uses the same M_p, so the z pass of
-// nt tiles becomes, per p, a (Z x Z) by (Z x nt) complex product: regular FP32
-// FMA work with register blocking, in place of two transforms over the padded
-// depth.  M is built once per spectrum (k_zop_coef, k_zop_build) and kept
-// resident, (Z, Z, P, P/2+1) complex64.
+// (w_p is the unnormalised inverse DFT of W along z; W already holds the
+// 1 / (Zp P P) normalisation).  At most four z map to one j.  The "z kernel" w
+// (Zp, P, P/2+1) complex64, the size of W, is built once per spectrum
+// (k_zker_build) and kept resident.  With one spectrum every tile of a batch
+// uses the same M_p, so the z pass of nt tiles is, per p, a (Z x Z) by
+// (Z x nt) complex product: regular FP32 FMA work with register blocking, in
+// place of two transforms over the padded depth.
 #include "deconv.cuh"
 
 namespace {
@@ -31,76 +32,77 @@ __device__ __forceinline__ void cp_async_wait_group() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-// E[i][j][kz] in double precision from exact integer phases, rounded once.
-__global__ void k_zop_coef(float2 *__restrict__ E, int Z, int zpad, int Zp) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long total = (long long)Z * Z * Zp;
-    if (idx >= total) return;
-    const int kz = (int)(idx % Zp);
-    const long long r = idx / Zp;
-    const int j = (int)(r % Z), i = (int)(r / Z);
-    double re = 0.0, im = 0.0;
-    for (int z = 0; z < Zp; ++z) {
-        if (mm_map_z(z, Z, zpad, Zp) != j) continue;
-        long long e = ((long long)kz * (zpad + i - z)) % Zp;
-        if (e < 0) e += Zp;
-        double s, c;
-        sincospi(2.0 * (double)e / (double)Zp, &s, &c);
-        re += c;
-        im += s;
-    }
-    E[idx] = make_float2((float)re, (float)im);
-}
-
-// M[i][j][p] = sum_kz E[i][j][kz] W[kz][p]: a CTA stages W for kBuildP
-// consecutive p; a warp per (i, j) pair, two p per lane.
+// w[d][p] = sum_kz W[kz][p] e^{+2 pi i kz d / Zp}: a CTA stages W for kBuildP
+// consecutive p and the Zp roots of unity (double precision, rounded once);
+// a warp per d, two p per lane.
 constexpr int kBuildP = 64;
 constexpr int kBuildThreads = 256;
 
 __global__ void __launch_bounds__(kBuildThreads)
-k_zop_build(const float2 *__restrict__ W, const float2 *__restrict__ E, float2 *__restrict__ M, int Z, int Zp,
-            long long plane) {
-    extern __shared__ __align__(16) float2 Ws[];  // Zp x kBuildP
+k_zker_build(const float2 *__restrict__ W, float2 *__restrict__ w, int Zp, long long plane) {
+    extern __shared__ __align__(16) float2 Ws[];  // Zp x kBuildP, then Zp roots
+    float2 *root = Ws + (size_t)Zp * kBuildP;
     const long long p0 = (long long)blockIdx.x * kBuildP;
     for (int it = threadIdx.x; it < Zp * kBuildP; it += blockDim.x) {
         const int kz = it / kBuildP, pp = it - kz * kBuildP;
         Ws[it] = p0 + pp < plane ? W[(long long)kz * plane + p0 + pp] : make_float2(0.f, 0.f);
     }
+    for (int k = threadIdx.x; k < Zp; k += blockDim.x) {
+        double s, c;
+        sincospi(2.0 * (double)k / (double)Zp, &s, &c);
+        root[k] = make_float2((float)c, (float)s);
+    }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    for (int ij = warp; ij < Z * Z; ij += nw) {
-        const float2 *e = E + (long long)ij * Zp;
+    for (int d = warp; d < Zp; d += nw) {
         float ax = 0.f, ay = 0.f, bx = 0.f, by = 0.f;
+        int e = 0;
         for (int kz = 0; kz < Zp; ++kz) {
-            const float2 c = __ldg(e + kz);
+            const float2 c = root[e];
             const float2 w0 = Ws[kz * kBuildP + lane], w1 = Ws[kz * kBuildP + 32 + lane];
             ax = fmaf(c.x, w0.x, fmaf(-c.y, w0.y, ax));
             ay = fmaf(c.x, w0.y, fmaf(c.y, w0.x, ay));
             bx = fmaf(c.x, w1.x, fmaf(-c.y, w1.y, bx));
             by = fmaf(c.x, w1.y, fmaf(c.y, w1.x, by));
+            e += d;
+            if (e >= Zp) e -= Zp;
         }
-        const long long base = (long long)ij * plane + p0;
-        if (p0 + lane < plane) M[base + lane] = make_float2(ax, ay);
-        if (p0 + 32 + lane < plane) M[base + 32 + lane] = make_float2(bx, by);
+        const long long base = (long long)d * plane + p0;
+        if (p0 + lane < plane) w[base + lane] = make_float2(ax, ay);
+        if (p0 + 32 + lane < plane) w[base + 32 + lane] = make_float2(bx, by);
     }
 }
 
 // ---------------------------------------------------------------------------
-// Apply: Y[t][i][p] = sum_j M[i][j][p] X[t][j][p] in place on the batch
-// spectrum S (nt, Z, plane).  A CTA owns kPB consecutive p and walks j in
-// chunks of kJC, staging M (Z rows) and X (TC tile rows) of the chunk in
-// shared memory with cp.async, double-buffered.  Thread (p, ig, tg) keeps the
-// TI x TT block of outputs i in [ig TI, ig TI + TI), t in [tg TT, tg TT + TT)
-// in registers.  Shared rows are kMS float2 apart (kJC * kPB + 4): the four
-// i-groups a warp reads fall on different bank windows.  The tiles go in
-// chunks of TC = tgn * TT; every read of a chunk's rows precedes its writes,
+// Apply: Y[t][i][p] = sum_j M_p[i][j] X[t][j][p] in place on the batch
+// spectrum S (nt, Z, plane).  A CTA owns kPB consecutive p.  It stages their
+// z kernel and sums all of M (Z x Z x kPB) into shared memory once, with a
+// thread per (j, p) walking i (the kernel index of each copy of plane j just
+// advances by one per i).  Then it walks j in chunks of kJC with the chunk of
+// X (TC tile rows) staged by cp.async into a ring of three buffers, so a
+// single barrier per chunk both publishes chunk c and frees the buffer of
+// chunk c - 1 for chunk c + 2.  Thread (p, ig, tg) keeps the TI x TT block of
+// outputs i in [ig TI, ig TI + TI), t in [tg TT, tg TT + TT) in registers.
+// Row strides (Z kPB + 4 for M, kJC kPB + 4 for X, in float2) put the i-groups
+// a warp reads on bank windows that overlap at most twice, the minimum for
+// 256 bytes.  With Z = 50 and 25 tiles a CTA has 200 threads and 110 KB, so
+// two run on an SM and one's barrier waits overlap the other's FMAs.  Tiles go
+// in chunks of TC = tgn TT; every read of a chunk's rows precedes its writes,
 // and chunks touch disjoint rows, so the update is in place.
 // ---------------------------------------------------------------------------
-constexpr int kPB = 8;
+constexpr int kPB = 4;
 constexpr int kJC = 10;
-constexpr int kMS = kJC * kPB + 4;
+constexpr int kXS = kJC * kPB + 4;
 constexpr int kTI = 5, kTT = 5;
-constexpr int kApplyMaxThreads = 640;
+constexpr int kNBuf = 3;
+constexpr int kApplyMaxThreads = 256;
+
+// for each real plane j: how many padded planes copy it, and the kernel index
+// (zpad - z) mod Zp of each copy z (at most MM_ZOP_MAX_COPIES)
+struct ZopTab {
+    int n[MM_ZOP_MAX_Z];
+    int off[MM_ZOP_MAX_Z][MM_ZOP_MAX_COPIES];
+};
 
 __device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {
     c.x = fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x));
@@ -109,88 +111,130 @@ __device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {
 }
 
 template <bool V16>
-__global__ void __launch_bounds__(kApplyMaxThreads, 1)
-k_zop_apply(float2 *__restrict__ S, const float2 *__restrict__ M, int Z, long long plane, int nt, int ign,
-            int tgn) {
+__global__ void __launch_bounds__(kApplyMaxThreads, 2)
+k_zop_apply(float2 *__restrict__ S, const float2 *__restrict__ w, int Z, int Zp, long long plane, int nt, int ign,
+            int tgn, const ZopTab tab) {
     extern __shared__ __align__(16) float2 sm[];
     const int rowsM = ign * kTI, TC = tgn * kTT;
-    const int stage = (rowsM + TC) * kMS;
-    const int tid = threadIdx.x;
-    const int p = tid & (kPB - 1);
-    const int rest = tid >> 3;
+    const int msw = Z * kPB + 4;       // M row stride
+    float2 *ws = sm;                   // Zp x kPB
+    float2 *Ms = ws + Zp * kPB;        // rowsM x msw
+    float2 *Xb = Ms + rowsM * msw;     // kNBuf x TC x kXS
+    const int tid = threadIdx.x, nth = blockDim.x;
+    const int p = tid % kPB;
+    const int rest = tid / kPB;
     const int ig = rest % ign, tg = rest / ign;
     const long long p0 = (long long)blockIdx.x * kPB;
     const int nch = (Z + kJC - 1) / kJC;
-    const int nM = Z * kJC * (kPB / 2);  // 16-byte units of a chunk's M rows
-    const int nU = nM + TC * kJC * (kPB / 2);
+
+    auto load_x = [&](int tc0, int c, int buf) {
+        float2 *Xs = Xb + buf * TC * kXS;
+        const int j0 = c * kJC;
+        for (int u = tid; u < TC * kJC * (kPB / 2); u += nth) {
+            const int pp = (u % (kPB / 2)) * 2;
+            const int r = u / (kPB / 2);
+            const int jj = r % kJC, row = r / kJC;
+            const int j = j0 + jj;
+            float2 *dst = Xs + row * kXS + jj * kPB + pp;
+            const long long pg = p0 + pp;
+            const bool ok = j < Z && tc0 + row < nt;
+            const float2 *src = S + ((long long)(tc0 + row) * Z + j) * plane + pg;
+            if (V16) {
+                // plane is even here, so pg < plane implies pg + 1 < plane
+                if (ok && pg < plane)
+                    cp_async16(dst, src);
+                else
+                    *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
+            } else {
+                if (ok && pg < plane)
+                    cp_async8(dst, src);
+                else
+                    dst[0] = make_float2(0.f, 0.f);
+                if (ok && pg + 1 < plane)
+                    cp_async8(dst + 1, src + 1);
+                else
+                    dst[1] = make_float2(0.f, 0.f);
+            }
+        }
+        cp_async_commit();
+    };
+
+    // the z kernel of this CTA's p, and the first two X chunks
+    for (int e = tid; e < Zp * kPB; e += nth) {
+        const int d = e / kPB, pp = e - d * kPB;
+        if (p0 + pp < plane)
+            cp_async8(&ws[e], &w[(long long)d * plane + p0 + pp]);
+        else
+            ws[e] = make_float2(0.f, 0.f);
+    }
+    cp_async_commit();
+    load_x(0, 0, 0);
+    if (nch > 1) {
+        load_x(0, 1, 1);
+        cp_async_wait_group<2>();
+    } else {
+        cp_async_wait_group<1>();
+    }
+    __syncthreads();
+    // M[i][j] = sum over the copies of plane j of ws[(i + off) mod Zp]
+    for (int q = tid; q < Z * kPB; q += nth) {
+        const int j = q / kPB, pp = q - j * kPB;
+        const int n = tab.n[j];
+        int d[MM_ZOP_MAX_COPIES];
+#pragma unroll
+        for (int k = 0; k < MM_ZOP_MAX_COPIES; ++k) d[k] = tab.off[j][k];
+        float2 *col = Ms + j * kPB + pp;
+        for (int i = 0; i < Z; ++i) {
+            float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < MM_ZOP_MAX_COPIES; ++k) {
+                if (k < n) {
+                    const float2 t = ws[d[k] * kPB + pp];
+                    v.x += t.x;
+                    v.y += t.y;
+                }
+                d[k] = d[k] + 1 == Zp ? 0 : d[k] + 1;
+            }
+            col[i * msw] = v;
+        }
+    }
 
     for (int tc0 = 0; tc0 < nt; tc0 += TC) {
-        auto load = [&](int c, int buf) {
-            float2 *Ms = sm + buf * stage, *Xs = Ms + rowsM * kMS;
-            const int j0 = c * kJC;
-            for (int u = tid; u < nU; u += blockDim.x) {
-                const bool isM = u < nM;
-                const int v = isM ? u : u - nM;
-                const int pp = (v & (kPB / 2 - 1)) * 2;
-                const int r = v / (kPB / 2);
-                const int jj = r % kJC, row = r / kJC;
-                const int j = j0 + jj;
-                float2 *dst = (isM ? Ms : Xs) + row * kMS + jj * kPB + pp;
-                const long long pg = p0 + pp;
-                const bool ok = j < Z && (isM || tc0 + row < nt);
-                const float2 *src = isM ? M + ((long long)row * Z + j) * plane + pg
-                                        : S + ((long long)(tc0 + row) * Z + j) * plane + pg;
-                if (V16) {
-                    // plane is even here, so pg < plane implies pg + 1 < plane
-                    if (ok && pg < plane)
-                        cp_async16(dst, src);
-                    else
-                        *reinterpret_cast<float4 *>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
-                } else {
-                    if (ok && pg < plane)
-                        cp_async8(dst, src);
-                    else
-                        dst[0] = make_float2(0.f, 0.f);
-                    if (ok && pg + 1 < plane)
-                        cp_async8(dst + 1, src + 1);
-                    else
-                        dst[1] = make_float2(0.f, 0.f);
-                }
-            }
-            cp_async_commit();
-        };
-
+        if (tc0 > 0) {
+            __syncthreads();  // every read of the previous tile chunk's buffers is done
+            load_x(tc0, 0, 0);
+            if (nch > 1) load_x(tc0, 1, 1);
+        }
         float2 acc[kTI][kTT];
 #pragma unroll
         for (int a = 0; a < kTI; ++a)
 #pragma unroll
             for (int b = 0; b < kTT; ++b) acc[a][b] = make_float2(0.f, 0.f);
 
-        load(0, 0);
         for (int c = 0; c < nch; ++c) {
-            if (c + 1 < nch) {
-                load(c + 1, (c + 1) & 1);
+            if (c + 1 < nch)
                 cp_async_wait_group<1>();
-            } else {
+            else
                 cp_async_wait_group<0>();
-            }
-            __syncthreads();
-            const float2 *Ms = sm + (c & 1) * stage, *Xs = Ms + rowsM * kMS;
-            const float2 *mr = Ms + (ig * kTI) * kMS + p;
-            const float2 *xr = Xs + (tg * kTT) * kMS + p;
+            __syncthreads();  // chunk c (and M) visible; chunk c - 1's buffer free
+            if (c + 2 < nch) load_x(tc0, c + 2, (c + 2) % kNBuf);
+            const int j0 = c * kJC;
+            const int jn = Z - j0 < kJC ? Z - j0 : kJC;
+            const float2 *mr = Ms + (ig * kTI) * msw + j0 * kPB + p;
+            const float2 *xr = Xb + (c % kNBuf) * TC * kXS + (tg * kTT) * kXS + p;
 #pragma unroll
             for (int jj = 0; jj < kJC; ++jj) {
+                if (jj >= jn) break;
                 float2 m[kTI], x[kTT];
 #pragma unroll
-                for (int a = 0; a < kTI; ++a) m[a] = mr[a * kMS + jj * kPB];
+                for (int a = 0; a < kTI; ++a) m[a] = mr[a * msw + jj * kPB];
 #pragma unroll
-                for (int b = 0; b < kTT; ++b) x[b] = xr[b * kMS + jj * kPB];
+                for (int b = 0; b < kTT; ++b) x[b] = xr[b * kXS + jj * kPB];
 #pragma unroll
                 for (int a = 0; a < kTI; ++a)
 #pragma unroll
                     for (int b = 0; b < kTT; ++b) acc[a][b] = cfma(m[a], x[b], acc[a][b]);
             }
-            __syncthreads();
         }
         if (p0 + p < plane) {
 #pragma unroll
@@ -209,35 +253,51 @@ k_zop_apply(float2 *__restrict__ S, const float2 *__restrict__ M, int Z, long lo
 
 }  // namespace
 
-size_t mm_zop_coef_bytes(int Z, int Zp) { return sizeof(float2) * (size_t)Z * Z * Zp; }
-
-int mm_zop_build_impl(const float2 *W, int Z, int zpad, int Zp, long long plane, float2 *E, float2 *M,
-                      cudaStream_t st) {
-    MM_REQUIRE(Z >= 1 && Z <= MM_ZOP_MAX_Z, "z operator needs 1 <= Z <= %d (got %d)", MM_ZOP_MAX_Z, Z);
-    MM_REQUIRE(Zp <= MM_ZOP_MAX_ZP, "z operator needs Zp <= %d (got %d)", MM_ZOP_MAX_ZP, Zp);
-    const long long ne = (long long)Z * Z * Zp;
-    k_zop_coef<<<(unsigned)((ne + 255) / 256), 256, 0, st>>>(E, Z, zpad, Zp);
-    MM_CHECK_LAUNCH();
-    const size_t sm = sizeof(float2) * (size_t)Zp * kBuildP;
-    MM_CUDA_TRY(cudaFuncSetAttribute(k_zop_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_zop_build<<<(unsigned)((plane + kBuildP - 1) / kBuildP), kBuildThreads, sm, st>>>(W, E, M, Z, Zp, plane);
+int mm_zker_build_impl(const float2 *W, int Zp, long long plane, float2 *w, cudaStream_t st) {
+    MM_REQUIRE(Zp >= 1 && Zp <= MM_ZOP_MAX_ZP, "z kernel needs 1 <= Zp <= %d (got %d)", MM_ZOP_MAX_ZP, Zp);
+    const size_t sm = sizeof(float2) * (size_t)Zp * (kBuildP + 1);
+    MM_CUDA_TRY(cudaFuncSetAttribute(k_zker_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_zker_build<<<(unsigned)((plane + kBuildP - 1) / kBuildP), kBuildThreads, sm, st>>>(W, w, Zp, plane);
     MM_CHECK_LAUNCH();
     return MM_OK;
 }
 
-int mm_launch_zop_apply(float2 *S, const float2 *M, int Z, long long plane, int nt, cudaStream_t st) {
-    MM_REQUIRE(Z >= 1 && Z <= MM_ZOP_MAX_Z, "z operator needs 1 <= Z <= %d (got %d)", MM_ZOP_MAX_Z, Z);
+int mm_zop_supported(int Z, int zpad) {
+    const int Zp = Z + 2 * zpad;
+    if (Z < 1 || Z > MM_ZOP_MAX_Z || zpad < 1 || Zp > MM_ZOP_MAX_ZP) return 0;
+    for (int j = 0; j < Z; ++j) {
+        int n = 0;
+        for (int z = 0; z < Zp; ++z) n += mm_map_z(z, Z, zpad, Zp) == j;
+        if (n > MM_ZOP_MAX_COPIES) return 0;
+    }
+    return 1;
+}
+
+int mm_launch_zop_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, long long plane, int nt,
+                        cudaStream_t st) {
+    MM_REQUIRE(Zp == Z + 2 * zpad && mm_zop_supported(Z, zpad),
+               "z operator needs Z <= %d, Zp <= %d and at most %d copies of a plane (Z %d, zpad %d)", MM_ZOP_MAX_Z,
+               MM_ZOP_MAX_ZP, MM_ZOP_MAX_COPIES, Z, zpad);
     if (nt <= 0) return MM_OK;
+    ZopTab tab = {};
+    for (int j = 0; j < Z; ++j)
+        for (int z = 0; z < Zp; ++z)
+            if (mm_map_z(z, Z, zpad, Zp) == j) {
+                const int o = ((zpad - z) % Zp + Zp) % Zp;
+                tab.off[j][tab.n[j]++] = o;
+            }
     int ign = (Z + kTI - 1) / kTI;
     const int tmax = kApplyMaxThreads / (kPB * ign);
     int tgn = (nt + kTT - 1) / kTT;
     if (tgn > tmax) tgn = tmax;
     const int threads = kPB * ign * tgn;
-    const size_t sm = sizeof(float2) * 2 * (size_t)(ign * kTI + tgn * kTT) * kMS;
+    const size_t sm = sizeof(float2) * ((size_t)Zp * kPB + (size_t)ign * kTI * (Z * kPB + 4) +
+                                        (size_t)kNBuf * tgn * kTT * kXS);
+    MM_REQUIRE(sm <= 227 * 1024, "z operator shared memory %zu bytes exceeds the limit", sm);
     const void *fn = (plane % 2 == 0) ? (const void *)k_zop_apply<true> : (const void *)k_zop_apply<false>;
     MM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     dim3 grid((unsigned)((plane + kPB - 1) / kPB));
-    void *args[] = {&S, &M, &Z, &plane, &nt, &ign, &tgn};
+    void *args[] = {&S, &w, &Z, &Zp, &plane, &nt, &ign, &tgn, &tab};
     MM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(threads), args, sm, st));
     mm_launch_counter_add();
     return MM_OK;

@@ -98,8 +98,7 @@ class Deconvolver:
         self.psf_fft = torch.view_as_complex(self.psf_fft)
         self.z_operator = None
         if self._want_z_operator(kwargs.get("z_operator")):
-            self.z_operator = torch.empty((self.tile_height, self.tile_height, self.P, self.H), dtype=torch.complex64,
-                                          device="cuda")
+            self.z_operator = torch.empty((self.Zp, self.P, self.H), dtype=torch.complex64, device="cuda")
             _lib.check(L.mm_wiener_zop(ctx, _lib.ptr(self.psf_fft), self.tile_height, self.zpad, self.tile_size,
                                        self.overlap, _lib.ptr(self.z_operator), st))
         if self.tile_size:
@@ -108,23 +107,23 @@ class Deconvolver:
             self.tile_raw = torch.empty(shape, dtype=torch.float32, device="cuda")
 
     # z operator: with one PSF, the z step of every tile is the same Z x Z
-    # complex matrix per (x, y) frequency (csrc/zop.cu); it is kept resident
-    # (8 Z^2 P (P/2+1) bytes) and replaces the padded-depth transforms.
-    Z_OPERATOR_MAX_BYTES = 16 << 30
-
+    # complex matrix per (x, y) frequency, summed from the inverse DFT of the
+    # spectrum along z (csrc/zop.cu).  That kernel has the size of psf_fft and
+    # is kept beside it.
     def _want_z_operator(self, request):
-        if request is False or self.psf_fft.shape[0] != 1 or not self.tile_size:
+        if request is False or self.psf_fft.shape[0] != 1 or not self.tile_size or self.zpad < 1:
             return False
-        nbytes = 8 * self.tile_height ** 2 * self.P * self.H
-        ok = self.tile_height <= 128 and self.Zp <= 400
-        if request is True:
-            if not ok:
-                raise ValueError("z_operator needs tile height <= 128 and padded depth <= 400")
-            return True
-        if not ok or nbytes > self.Z_OPERATOR_MAX_BYTES:
-            return False
-        free, _ = torch.cuda.mem_get_info()
-        return nbytes <= free // 4
+        ok = self.tile_height <= 64 and self.Zp <= 400
+        if ok:
+            # every real plane is copied by at most four padded planes
+            mz = np.zeros(self.Zp, dtype=np.int32)
+            _lib.check(_lib.lib().mm_tile_geometry(self.tile_height, self.tile_size, self.tile_size, self.tile_size,
+                                                   self.zpad, self.overlap, 1, 0, None, mz.ctypes.data, None, None))
+            ok = np.bincount(mz[mz >= 0], minlength=1).max() <= 4
+        if request is True and not ok:
+            raise ValueError("z_operator needs tile height <= 64, padded depth <= 400 and at most four copies "
+                             "of a plane in the z padding")
+        return ok
 
     # -- geometry ------------------------------------------------------------
     def tile_boxes(self, shape):

@@ -159,12 +159,14 @@ def test_apply_stitch_order_matches_reference(dc, npsf):
     assert np.abs(got_all[ok] - want[ok]).max() <= REL * np.abs(want[ok]).max()
 
 
-@pytest.mark.parametrize("Z,zpad,ts,ov", [(13, 12, 10, 3), (100, 49, 10, 3), (50, 24, 30, 9), (7, 2, 15, 3)])
+@pytest.mark.parametrize("Z,zpad,ts,ov", [(13, 12, 10, 3), (64, 63, 10, 3), (50, 24, 30, 9), (7, 2, 15, 3),
+                                          (5, 9, 10, 3)])
 def test_z_operator_matches_padded_transforms(dc, Z, zpad, ts, ov):
-    """The z operator (one Z x Z matrix per frequency) against the FFT z pass
-    over the padded depth, on whole batches: Z not a multiple of the 10-plane
-    chunks, a batch of 25 tiles split into two tile chunks at Z = 100, and an
-    odd frequency plane (P = 21)."""
+    """The z operator (one Z x Z matrix per frequency, summed from the z
+    kernel) against the FFT z pass over the padded depth, on whole batches: Z
+    not a multiple of the 10-plane chunks, a batch of 25 tiles split into two
+    tile chunks at Z = 64, an odd frequency plane (P = 21), and zpad > Z
+    (four padded planes copy one real plane)."""
     rng = np.random.default_rng(Z)
     X = Y = 5 * ts
     img = rng.integers(100, 5000, (Z, X, Y)).astype(np.uint16)
