@@ -412,6 +412,145 @@ __device__ __noinline__ void stage_lane(const float2 *__restrict__ src, float2 *
     }
 }
 
+// GEMM form of a large odd prime stage, for CTAs of at least 512 threads.
+// With u_r = x_r + x_{R-r}, v_r = x_r - x_{R-r} (twiddled) and H = (R-1)/2:
+//   A_k = sum_{r=1..H} cos(2 pi r k / R) u_r   (k = 0..H; A_0 = sum u_r)
+//   B_k = sum_{r=1..H} sin(2 pi r k / R) v_r   (k = 1..H)
+//   forward X[k] = x_0 + A_k - i B_k, X[R-k] = x_0 + A_k + i B_k, X[0] = x_0 + A_0
+//   (inverse: the sign of B swaps).
+// Over the m * nl butterflies of the CTA these are two real matrix products
+// with constant matrices, computed register-blocked: a thread keeps 8 rows k
+// x 3 butterflies, reads its 8 coefficients of a column r as two broadcast
+// float4 and its 3 inputs, 48 FMA per 5 shared loads (the lane stage needs 4
+// FMA per load).  Phase 1 writes U and V over dst (2 H nb < n nl values),
+// phase 2 multiplies, then A and B go over dst ((2H + 1) nb = n nl values) and
+// phase 3 combines them into src: the stage's output is left in src.
+// Coefficients and x_0 live in the lane-stage scratch (scr_all).
+template <int R>
+struct GemmStage {
+    static constexpr int H = (R - 1) / 2;
+    static constexpr int KA = (H + 1 + 7) / 8 * 8;  // rows k = 0..H of A, padded to 8
+    static constexpr int KB = (H + 7) / 8 * 8;      // rows k = 1..H of B, padded to 8
+    static __device__ __host__ constexpr size_t scr_floats(int nb) { return (size_t)H * (KA + KB) + 2 * nb; }
+    static __device__ __host__ constexpr int threads(int nb) { return (KA / 8 + KB / 8) * ((nb + 2) / 3); }
+};
+
+template <int R, bool INV>
+__device__ __noinline__ void stage_gemm(float2 *__restrict__ src, float2 *__restrict__ dst, int n, int nl, int Ns,
+                                        const float2 *__restrict__ tw, const float2 *__restrict__ cs,
+                                        float4 *__restrict__ scr_all) {
+    using G = GemmStage<R>;
+    constexpr int H = G::H, KA = G::KA, KB = G::KB;
+    const int m = n / R, nb = m * nl;
+    const int tstep = n / (Ns * R);
+    const int lnl = log2_pow2(nl);
+    const float invNs = 1.0f / (float)Ns;
+    float *Ct = reinterpret_cast<float *>(scr_all);     // [r][k], k = 0..KA-1
+    float *St = Ct + H * KA;                            // [r][k - 1], k = 1..KB
+    float2 *x0s = reinterpret_cast<float2 *>(St + H * KB);
+    float2 *U = dst, *V = dst + H * nb;
+
+    for (int e = threadIdx.x; e < H * KA; e += blockDim.x) {
+        const int r = e / KA + 1, k = e % KA;
+        Ct[e] = k <= H ? cs[(r * k) % R].x : 0.f;
+    }
+    for (int e = threadIdx.x; e < H * KB; e += blockDim.x) {
+        const int r = e / KB + 1, k = e % KB + 1;
+        St[e] = k <= H ? -cs[(r * k) % R].y : 0.f;  // the table holds (cos, -sin)
+    }
+    // phase 1: x_0, U, V
+    for (int e = threadIdx.x; e < nb * (H + 1); e += blockDim.x) {
+        const int r = e / nb, b = e - r * nb;
+        const int l = b & (nl - 1), j = b >> lnl;
+        if (r == 0) {
+            x0s[b] = src[sidx(j, l, nl)];
+            continue;
+        }
+        float2 u = src[sidx(j + r * m, l, nl)], v = src[sidx(j + (R - r) * m, l, nl)];
+        if (Ns > 1) {
+            const int kk = j - fdiv_i(j, Ns, invNs) * Ns;
+            const float2 wu = tw[kk * r * tstep], wv = tw[kk * (R - r) * tstep];
+            u = INV ? cmulc(u, wu) : cmul(u, wu);
+            v = INV ? cmulc(v, wv) : cmul(v, wv);
+        }
+        U[(r - 1) * nb + b] = cadd(u, v);
+        V[(r - 1) * nb + b] = csub(u, v);
+    }
+    __syncthreads();
+    // phase 2: thread = (part, 8 rows, 3 butterflies)
+    const int nbb = (nb + 2) / 3;
+    const int itemsA = (KA / 8) * nbb;
+    const int it = threadIdx.x;
+    const bool active = it < itemsA + (KB / 8) * nbb;
+    const bool partB = it >= itemsA;
+    const int rel = partB ? it - itemsA : it;
+    const int kb = rel / nbb, b0 = (rel - kb * nbb) * 3;
+    float2 acc[8][3];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+#pragma unroll
+        for (int i = 0; i < 3; ++i) acc[q][i] = make_float2(0.f, 0.f);
+    if (active) {
+        const int cstride = partB ? KB : KA;
+        const float *cp = (partB ? St : Ct) + kb * 8;
+        const float2 *ip = (partB ? V : U) + b0;
+#pragma unroll 4
+        for (int r = 0; r < H; ++r) {
+            const float4 c0 = *reinterpret_cast<const float4 *>(cp + r * cstride);
+            const float4 c1 = *reinterpret_cast<const float4 *>(cp + r * cstride + 4);
+            const float c[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+            float2 in[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) in[i] = ip[r * nb + i];  // reads past nb stay inside dst
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    acc[q][i].x = fmaf(c[q], in[i].x, acc[q][i].x);
+                    acc[q][i].y = fmaf(c[q], in[i].y, acc[q][i].y);
+                }
+        }
+    }
+    __syncthreads();
+    // A rows k = 0..H at dst[k nb + b], B rows k = 1..H at dst[(H + k) nb + b]
+    if (active) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int k = kb * 8 + q + (partB ? 1 : 0);
+            if (k > H) break;
+            float2 *row = dst + (size_t)(partB ? H + k : k) * nb;
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+                if (b0 + i < nb) row[b0 + i] = acc[q][i];
+        }
+    }
+    __syncthreads();
+    // phase 3: combine into src
+    for (int e = threadIdx.x; e < nb * (H + 1); e += blockDim.x) {
+        const int k = e / nb, b = e - k * nb;
+        const int l = b & (nl - 1), j = b >> lnl;
+        const int kk = Ns > 1 ? j - fdiv_i(j, Ns, invNs) * Ns : 0;
+        const int d = (j - kk) * R + kk;
+        const float2 x0 = x0s[b];
+        const float2 a = cadd(dst[(size_t)k * nb + b], x0);
+        if (k == 0) {
+            src[sidx(d, l, nl)] = a;
+            continue;
+        }
+        const float2 bv = dst[(size_t)(H + k) * nb + b];
+        float2 o1, o2;
+        if (!INV) {
+            o1 = make_float2(a.x + bv.y, a.y - bv.x);
+            o2 = make_float2(a.x - bv.y, a.y + bv.x);
+        } else {
+            o1 = make_float2(a.x - bv.y, a.y + bv.x);
+            o2 = make_float2(a.x + bv.y, a.y - bv.x);
+        }
+        src[sidx(d + k * Ns, l, nl)] = o1;
+        src[sidx(d + (R - k) * Ns, l, nl)] = o2;
+    }
+}
+
 template <int R, bool INV>
 __device__ __forceinline__ void stage_small(const float2 *__restrict__ src, float2 *__restrict__ dst,
                                             int n, int nl, int Ns, const float2 *tw) {
@@ -527,6 +666,17 @@ __device__ float2 *fft_lines(float2 *A, float2 *B, int nl, const FftPlan &P,
     float2 *src = A, *dst = B;
     for (int st = 0; st < P.nst; ++st) {
         const int R = P.rad[st], Ns = P.ns[st];
+        if constexpr (LMAX >= 113) {
+            // 113 in GEMM form when the CTA has the threads and the scratch
+            const int nb = P.n / 113 * nl;
+            if (R == 113 && (int)blockDim.x >= GemmStage<113>::threads(nb) &&
+                GemmStage<113>::scr_floats(nb) * sizeof(float) <=
+                    sizeof(float4) * MM_FFT_SCR_PER_WARP * (blockDim.x >> 5)) {
+                stage_gemm<113, INV>(src, dst, P.n, nl, Ns, tw_s, tab_s + P.ptab[st], scr);
+                __syncthreads();
+                continue;  // output left in src
+            }
+        }
         switch (R) {
             case 2: stage_small<2, INV>(src, dst, P.n, nl, Ns, tw_s); break;
             case 3: stage_small<3, INV>(src, dst, P.n, nl, Ns, tw_s); break;
