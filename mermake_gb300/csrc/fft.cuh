@@ -425,7 +425,8 @@ __device__ __noinline__ void stage_lane(const float2 *__restrict__ src, float2 *
 // FMA per load).  Phase 1 writes U and V over dst (2 H nb < n nl values),
 // phase 2 multiplies, then A and B go over dst ((2H + 1) nb = n nl values) and
 // phase 3 combines them into src: the stage's output is left in src.
-// Coefficients and x_0 live in the lane-stage scratch (scr_all).
+// The coefficient tables live in the lane-stage scratch (scr_all), written by
+// fft_gemm_tables at the start of the kernel, followed by x_0.
 template <int R>
 struct GemmStage {
     static constexpr int H = (R - 1) / 2;
@@ -434,6 +435,49 @@ struct GemmStage {
     static __device__ __host__ constexpr size_t scr_floats(int nb) { return (size_t)H * (KA + KB) + 2 * nb; }
     static __device__ __host__ constexpr int threads(int nb) { return (KA / 8 + KB / 8) * ((nb + 2) / 3); }
 };
+
+// The plan can use the GEMM form: one 113 stage, no lane stage (which would
+// reuse the scratch holding the coefficients), and enough threads and scratch.
+__device__ __forceinline__ bool fft_gemm_ok(const FftPlan &P, int nl) {
+    bool has = false;
+    for (int st = 0; st < P.nst; ++st) {
+        if (P.rad[st] == 113)
+            has = true;
+        else if (P.rad[st] > 37)
+            return false;
+    }
+    if (!has) return false;
+    const int nb = P.n / 113 * nl;
+    return (int)blockDim.x >= GemmStage<113>::threads(nb) &&
+           GemmStage<113>::scr_floats(nb) * sizeof(float) <=
+               sizeof(float4) * MM_FFT_SCR_PER_WARP * (blockDim.x >> 5);
+}
+
+// Coefficient tables of the GEMM stage (cos and sin of 2 pi r k / 113 from the
+// plan's table in global memory); called by every thread of a kernel that
+// runs fft_lines, before the barrier that precedes it, so that the work
+// overlaps the kernel's own loads.
+template <int LMAX>
+__device__ __forceinline__ void fft_gemm_tables(const FftPlan &P, int nl, float4 *scr_all) {
+    if constexpr (LMAX >= 113) {
+        if (!fft_gemm_ok(P, nl)) return;
+        using G = GemmStage<113>;
+        int pt = 0;
+        for (int st = 0; st < P.nst; ++st)
+            if (P.rad[st] == 113) pt = P.ptab[st];
+        const float2 *cs = P.tab + pt;
+        float *Ct = reinterpret_cast<float *>(scr_all);
+        float *St = Ct + G::H * G::KA;
+        for (int e = threadIdx.x; e < G::H * G::KA; e += blockDim.x) {
+            const int r = e / G::KA + 1, k = e % G::KA;
+            Ct[e] = k <= G::H ? cs[(r * k) % 113].x : 0.f;
+        }
+        for (int e = threadIdx.x; e < G::H * G::KB; e += blockDim.x) {
+            const int r = e / G::KB + 1, k = e % G::KB + 1;
+            St[e] = k <= G::H ? -cs[(r * k) % 113].y : 0.f;  // the table holds (cos, -sin)
+        }
+    }
+}
 
 template <int R, bool INV>
 __device__ __noinline__ void stage_gemm(float2 *__restrict__ src, float2 *__restrict__ dst, int n, int nl, int Ns,
@@ -450,17 +494,10 @@ __device__ __noinline__ void stage_gemm(float2 *__restrict__ src, float2 *__rest
     float2 *x0s = reinterpret_cast<float2 *>(St + H * KB);
     float2 *U = dst, *V = dst + H * nb;
 
-    for (int e = threadIdx.x; e < H * KA; e += blockDim.x) {
-        const int r = e / KA + 1, k = e % KA;
-        Ct[e] = k <= H ? cs[(r * k) % R].x : 0.f;
-    }
-    for (int e = threadIdx.x; e < H * KB; e += blockDim.x) {
-        const int r = e / KB + 1, k = e % KB + 1;
-        St[e] = k <= H ? -cs[(r * k) % R].y : 0.f;  // the table holds (cos, -sin)
-    }
+    const float invnb = 1.0f / (float)nb;
     // phase 1: x_0, U, V
     for (int e = threadIdx.x; e < nb * (H + 1); e += blockDim.x) {
-        const int r = e / nb, b = e - r * nb;
+        const int r = fdiv_i(e, nb, invnb), b = e - r * nb;
         const int l = b & (nl - 1), j = b >> lnl;
         if (r == 0) {
             x0s[b] = src[sidx(j, l, nl)];
@@ -527,7 +564,7 @@ __device__ __noinline__ void stage_gemm(float2 *__restrict__ src, float2 *__rest
     __syncthreads();
     // phase 3: combine into src
     for (int e = threadIdx.x; e < nb * (H + 1); e += blockDim.x) {
-        const int k = e / nb, b = e - k * nb;
+        const int k = fdiv_i(e, nb, invnb), b = e - k * nb;
         const int l = b & (nl - 1), j = b >> lnl;
         const int kk = Ns > 1 ? j - fdiv_i(j, Ns, invNs) * Ns : 0;
         const int d = (j - kk) * R + kk;
@@ -667,11 +704,8 @@ __device__ float2 *fft_lines(float2 *A, float2 *B, int nl, const FftPlan &P,
     for (int st = 0; st < P.nst; ++st) {
         const int R = P.rad[st], Ns = P.ns[st];
         if constexpr (LMAX >= 113) {
-            // 113 in GEMM form when the CTA has the threads and the scratch
-            const int nb = P.n / 113 * nl;
-            if (R == 113 && (int)blockDim.x >= GemmStage<113>::threads(nb) &&
-                GemmStage<113>::scr_floats(nb) * sizeof(float) <=
-                    sizeof(float4) * MM_FFT_SCR_PER_WARP * (blockDim.x >> 5)) {
+            // 113 in GEMM form (tables from fft_gemm_tables)
+            if (R == 113 && fft_gemm_ok(P, nl)) {
                 stage_gemm<113, INV>(src, dst, P.n, nl, Ns, tw_s, tab_s + P.ptab[st], scr);
                 __syncthreads();
                 continue;  // output left in src
