@@ -50,6 +50,10 @@ k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ 
     const long long row0 = (long long)blockIdx.x * 2 * nl;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     float *Af = reinterpret_cast<float *>(L.A);
+    // the y map of the tile (same for every row), after the scratch
+    int *ymap = reinterpret_cast<int *>(L.scr + MM_FFT_SCR_PER_WARP * nw);
+    for (int e = threadIdx.x; e < n; e += blockDim.x) ymap[e] = mm_map_xy(e, d.y == 0, d.yd, g.P, g.ov);
+    __syncthreads();
     for (int q = warp; q < 2 * nl; q += nw) {
         const long long row = row0 + q;
         const int l = q >> 1, comp = q & 1;
@@ -71,7 +75,7 @@ k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ 
                 const int e = e0 + 32 * u;
                 v[u] = 0.f;
                 if (src && e < n) {
-                    const int sy = mm_map_xy(e, d.y == 0, d.yd, g.P, g.ov);
+                    const int sy = ymap[e];
                     if (sy >= 0) {
                         // transform input: the fast division is within 2 ulp; the raw
                         // view (k_make_raw) keeps the reference's IEEE quotient
@@ -193,6 +197,9 @@ k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restri
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     // odd segment length: the 32 lanes' strided reads fall in distinct banks
     const int seg = ((n + 31) / 32) | 1;
+    // mean = sum x (1 / count): the full window's reciprocal is computed once
+    const int full = 2 * delta + 1;
+    const float inv_full = 1.0f / (float)full;
     for (int q = warp; q < 2 * nl; q += nw) {
         const int l = q >> 1, comp = q & 1;
         const int s0 = lane * seg, s1 = min(s0 + seg, n);
@@ -207,7 +214,7 @@ k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restri
                     if (drop >= 0) sum -= Rf[2 * sidx(drop, l, nl) + comp];
                 }
                 const int cnt = min(e + delta, n - 1) - max(e - delta, 0) + 1;
-                Bf[q * n + e] = sum / (float)cnt;
+                Bf[q * n + e] = sum * (cnt == full ? inv_full : 1.0f / (float)cnt);
             }
         }
         __syncwarp();
@@ -248,6 +255,8 @@ k_blur_x_sub(TileGeom g, const float *__restrict__ res, const float *__restrict_
     }
     const int seg = (P + nw - 1) / nw;
     const int x0 = warp * seg, x1 = min(x0 + seg, P);
+    const int full = 2 * delta + 1;
+    const float inv_full = 1.0f / (float)(full > 0 ? full : 1);
     float sum = 0.f;
     if (delta >= 0 && x0 < P) {
         const int lo = max(x0 - delta, 0), hi = min(x0 + delta, P - 1);
@@ -272,7 +281,7 @@ k_blur_x_sub(TileGeom g, const float *__restrict__ res, const float *__restrict_
             float val = v[u];
             if (delta >= 0) {
                 const int cnt = min(x + delta, P - 1) - max(x - delta, 0) + 1;
-                val = val - sum / (float)cnt;
+                val = val - sum * (cnt == full ? inv_full : 1.0f / (float)cnt);
             }
             if (res_out) res_out[pbase + (long long)x * P + y] = val;
             if (stitch && x >= g.ov && x < d.xend - g.ov && y >= g.ov && y < d.yend - g.ov) {
@@ -327,8 +336,10 @@ int mm_launch_rows_fwd_img(const TileGeom &g, const void *img, int dtype, const 
     FftPlan P;
     int rc = mm_fft_plan_get(g.P, &P);
     if (rc) return rc;
-    int nl = pick_nl(P, 16);
-    size_t sm = fft_smem(P, nl);
+    // lines per CTA, with room for the y map (P ints) after the scratch
+    int nl = 16;
+    while (nl > 1 && fft_smem(P, nl) + sizeof(int) * P.n > (size_t)kSmemLimit) nl >>= 1;
+    size_t sm = fft_smem(P, nl) + sizeof(int) * P.n;
     dim3 grid(mm_cdiv((long)g.Z * g.P, 2 * nl), g.nt);
     TileGeom ga = g;
     const void *imga = img;
