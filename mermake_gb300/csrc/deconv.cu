@@ -31,9 +31,13 @@ int set_smem(K *kernel, size_t bytes) {
 }
 
 // ---------------------------------------------------------------------------
-// y pass, forward, tile source (u16 or f32) through the pad maps.  One warp
-// gathers one padded row at a time (row-level map and addresses computed once,
-// lanes over the row), eight loads in flight per lane.
+// y pass, forward, tile source (u16 or f32) through the pad maps.  A CTA takes
+// 2 nl padded rows in x-major, z-minor order, so its rows share few flat-field
+// rows.  uint16 tiles: the CTA first stages its raw rows (4-byte cp.async
+// words) and their flat rows into the idle ping-pong buffer, all in flight at
+// once, then builds the lines from shared memory through the y map (divided by
+// the flat), so the gathers do not stall on global latency row by row.
+// float32 tiles gather straight from global memory.
 // ---------------------------------------------------------------------------
 template <typename T, int LMAX>
 __global__ void __launch_bounds__(kThreads)
@@ -47,47 +51,111 @@ k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ 
     const int ti = g.t0 + blockIdx.y;
     const TileDesc d = mm_tile_desc(g, ti);
     const long long nrows = (long long)g.Z * g.P;
-    const long long row0 = (long long)blockIdx.x * 2 * nl;
+    const long long row0 = (long long)blockIdx.x * 2 * nl;  // in (x, z) order
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     float *Af = reinterpret_cast<float *>(L.A);
     // the y map of the tile (same for every row), after the scratch
     int *ymap = reinterpret_cast<int *>(L.scr + MM_FFT_SCR_PER_WARP * nw);
     for (int e = threadIdx.x; e < n; e += blockDim.x) ymap[e] = mm_map_xy(e, d.y == 0, d.yd, g.P, g.ov);
-    __syncthreads();
-    for (int q = warp; q < 2 * nl; q += nw) {
-        const long long row = row0 + q;
-        const int l = q >> 1, comp = q & 1;
-        const T *src = nullptr;
-        const float *fsrc = nullptr;
-        if (row < nrows) {
-            const int z = (int)(row / g.P), xp = (int)(row % g.P);
+
+    if constexpr (sizeof(T) == 2) {
+        const int rs = (d.yd + 3) & ~1;  // staged row length (even, room for one leading element)
+        uint16_t *Bu = reinterpret_cast<uint16_t *>(L.B);
+        float *Bfl = reinterpret_cast<float *>(Bu + 2 * nl * rs);
+        const long long rlast = min(row0 + 2 * nl, nrows) - 1;
+        const int xpa = (int)(row0 / g.Z), xpb = (int)(rlast / g.Z);
+        const int nfx = xpb - xpa + 1;
+        const bool fstage = flat && (size_t)2 * nl * rs * sizeof(uint16_t) + (size_t)nfx * d.yd * sizeof(float) <=
+                                        (size_t)n * nl * sizeof(float2);
+        for (int q = warp; q < 2 * nl; q += nw) {
+            const long long r = row0 + q;
+            if (r >= nrows) continue;
+            const int xp = (int)(r / g.Z), z = (int)(r - (long long)xp * g.Z);
             const int sx = mm_map_xy(xp, d.x == 0, d.xd, g.P, g.ov);
-            if (sx >= 0) {
-                src = img + z * g.isz + (long long)(d.x0 + sx) * g.isx + d.y0;
-                if (flat) fsrc = flat + (long long)(d.x0 + sx) * g.fsx + d.y0;
-            }
+            if (sx < 0) continue;
+            const uint16_t *src = reinterpret_cast<const uint16_t *>(img) + z * g.isz +
+                                  (long long)(d.x0 + sx) * g.isx + d.y0;
+            // a row starting 2 bytes past a word boundary is copied from the
+            // element before it (inside the same allocation, which is aligned)
+            const int off = (int)((reinterpret_cast<uintptr_t>(src) >> 1) & 1);
+            const uint16_t *a = src - off;
+            uint16_t *dst = Bu + q * rs;
+            const int nwords = (d.yd + off) >> 1;
+            for (int w = lane; w < nwords; w += 32) cp_async4(dst + 2 * w, a + 2 * w);
+            if (((d.yd + off) & 1) && lane == 0) dst[d.yd - 1 + off] = src[d.yd - 1];
         }
-        constexpr int U = 24;  // a whole padded row (up to 768) in flight per warp
-        for (int e0 = lane; e0 < n; e0 += 32 * U) {
-            float v[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int e = e0 + 32 * u;
-                v[u] = 0.f;
-                if (src && e < n) {
-                    const int sy = ymap[e];
-                    if (sy >= 0) {
-                        // transform input: the fast division is within 2 ulp; the raw
-                        // view (k_make_raw) keeps the reference's IEEE quotient
-                        v[u] = (float)src[sy];
-                        if (fsrc) v[u] = __fdividef(v[u], fsrc[sy]);
-                    }
+        if (fstage)
+            for (int it = threadIdx.x; it < nfx * d.yd; it += blockDim.x) {
+                const int fx = it / d.yd, y = it - fx * d.yd;
+                const int sx = mm_map_xy(xpa + fx, d.x == 0, d.xd, g.P, g.ov);
+                if (sx >= 0) cp_async4(&Bfl[it], &flat[(long long)(d.x0 + sx) * g.fsx + d.y0 + y]);
+            }
+        cp_async_wait_all();
+        __syncthreads();
+        for (int q = warp; q < 2 * nl; q += nw) {
+            const long long r = row0 + q;
+            const int l = q >> 1, comp = q & 1;
+            int sx = -1, off = 0;
+            const float *frow = nullptr;
+            if (r < nrows) {
+                const int xp = (int)(r / g.Z), z = (int)(r - (long long)xp * g.Z);
+                sx = mm_map_xy(xp, d.x == 0, d.xd, g.P, g.ov);
+                if (sx >= 0) {
+                    const uint16_t *src = reinterpret_cast<const uint16_t *>(img) + z * g.isz +
+                                          (long long)(d.x0 + sx) * g.isx + d.y0;
+                    off = (int)((reinterpret_cast<uintptr_t>(src) >> 1) & 1);
+                    if (flat)
+                        frow = fstage ? Bfl + (xp - xpa) * d.yd : flat + (long long)(d.x0 + sx) * g.fsx + d.y0;
                 }
             }
+            const uint16_t *rowp = Bu + q * rs + off;
+            for (int e = lane; e < n; e += 32) {
+                float v = 0.f;
+                const int sy = ymap[e];
+                if (sx >= 0 && sy >= 0) {
+                    // the fast division is within 2 ulp; the raw view (k_make_raw)
+                    // keeps the reference's IEEE quotient
+                    v = (float)rowp[sy];
+                    if (frow) v = __fdividef(v, frow[sy]);
+                }
+                Af[2 * sidx(e, l, nl) + comp] = v;
+            }
+        }
+    } else {
+        __syncthreads();
+        for (int q = warp; q < 2 * nl; q += nw) {
+            const long long r = row0 + q;
+            const int l = q >> 1, comp = q & 1;
+            const T *src = nullptr;
+            const float *fsrc = nullptr;
+            if (r < nrows) {
+                const int xp = (int)(r / g.Z), z = (int)(r - (long long)xp * g.Z);
+                const int sx = mm_map_xy(xp, d.x == 0, d.xd, g.P, g.ov);
+                if (sx >= 0) {
+                    src = img + z * g.isz + (long long)(d.x0 + sx) * g.isx + d.y0;
+                    if (flat) fsrc = flat + (long long)(d.x0 + sx) * g.fsx + d.y0;
+                }
+            }
+            constexpr int U = 24;  // a whole padded row (up to 768) in flight per warp
+            for (int e0 = lane; e0 < n; e0 += 32 * U) {
+                float v[U];
 #pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int e = e0 + 32 * u;
-                if (e < n) Af[2 * sidx(e, l, nl) + comp] = v[u];
+                for (int u = 0; u < U; ++u) {
+                    const int e = e0 + 32 * u;
+                    v[u] = 0.f;
+                    if (src && e < n) {
+                        const int sy = ymap[e];
+                        if (sy >= 0) {
+                            v[u] = (float)src[sy];
+                            if (fsrc) v[u] = __fdividef(v[u], fsrc[sy]);
+                        }
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    const int e = e0 + 32 * u;
+                    if (e < n) Af[2 * sidx(e, l, nl) + comp] = v[u];
+                }
             }
         }
     }
@@ -95,16 +163,23 @@ k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ 
     __syncthreads();
     float2 *R = fft_lines<false, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
 
+    // unpack the two real rows of each line into their spectrum rows z P + x
     const int H = g.H;
     const float invH = 1.0f / (float)H;
     float2 *Sb = S + (long long)blockIdx.y * nrows * H;
     for (int it = threadIdx.x; it < nl * H; it += blockDim.x) {
         const int l = fdiv_i(it, H, invH), k = it - l * H;
-        const long long r0 = row0 + 2 * l;
+        const long long r0 = row0 + 2 * l, r1 = r0 + 1;
         const float2 ck = R[sidx(k, l, nl)];
         const float2 cn = R[sidx((n - k) % n, l, nl)];
-        if (r0 < nrows) Sb[r0 * H + k] = make_float2(0.5f * (ck.x + cn.x), 0.5f * (ck.y - cn.y));
-        if (r0 + 1 < nrows) Sb[(r0 + 1) * H + k] = make_float2(0.5f * (ck.y + cn.y), -0.5f * (ck.x - cn.x));
+        if (r0 < nrows) {
+            const long long xp = r0 / g.Z;
+            Sb[((r0 - xp * g.Z) * g.P + xp) * H + k] = make_float2(0.5f * (ck.x + cn.x), 0.5f * (ck.y - cn.y));
+        }
+        if (r1 < nrows) {
+            const long long xp = r1 / g.Z;
+            Sb[((r1 - xp * g.Z) * g.P + xp) * H + k] = make_float2(0.5f * (ck.y + cn.y), -0.5f * (ck.x - cn.x));
+        }
     }
 }
 
