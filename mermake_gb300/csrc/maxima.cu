@@ -17,7 +17,7 @@
 //            reference's (dz, dx, dy) order (first 600 in-range samples,
 //            maxima.cu:148, 190-232) and forms every output of
 //            delta_fit_cross_corr from moment sums (float32 on centre-shifted
-//            values, statistics in double):
+//            values; the variances and covariances in double, the rest in float):
 //              bg = min v;  centroid = sum (c+d)(v-bg) / sum (v-bg)  (fallback c);
 //              hn = cov(v, G) / (std'(v) std(G));  a = cov(raw, G) / (std'(raw) std(G))
 //            with std' = std, or 1 where std == 0 (maxima.cu:233-341).  std(G) == 0
@@ -118,6 +118,8 @@ __device__ __forceinline__ float raw_at(const Vols &V, int vi, const TileDesc &d
     float v = V.raw_kind == 2 ? (float)static_cast<const uint16_t *>(V.chan)[ci] : static_cast<const float *>(V.chan)[ci];
     if (V.flat) {
         float f = V.flat[gx * g.fsx + gy];
+        // the reference's IEEE quotient: the batched fit reads the same raw
+        // values as a fit on the materialised raw view
         v = __fdiv_rn(v, f);
         if (x >= d.xs && x < d.xs + d.xd && y >= d.ys && y < d.ys + d.yd) v = __fmul_rn(v, f);
     }
@@ -125,12 +127,18 @@ __device__ __forceinline__ float raw_at(const Vols &V, int vi, const TileDesc &d
 }
 
 // A warp per (z, x) row, lanes along y: every row index is split once, loads
-// are coalesced, and each lane keeps kMaxY values of the row in flight.
+// are coalesced, and each lane keeps kMaxY values of the row in flight.  The
+// voxels above the threshold (a few percent) are queued per warp in shared
+// memory and their neighbourhoods tested one voxel per lane, so the test does
+// not run with most lanes idle.
 constexpr int kMaxY = 4;
+constexpr int kMaxWarps = 8;
 
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(32 * kMaxWarps)
 k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigned cap,
          unsigned *__restrict__ count) {
+    __shared__ int qy[kMaxWarps][32 * kMaxY];
+    __shared__ float qv[kMaxWarps][32 * kMaxY];
     t = xf_resolve(t);
     const int vi = blockIdx.y;
     int X, Y;
@@ -142,8 +150,10 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
     const int nn = g_sphere_n[delta];
     const char4 *sph = g_sphere[delta];
     const unsigned lane = threadIdx.x & 31;
-    const int wpb = blockDim.x >> 5;
-    for (int row = blockIdx.x * wpb + (int)(threadIdx.x >> 5); row < rows; row += gridDim.x * wpb) {
+    const int warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    int *my_y = qy[warp];
+    float *my_v = qv[warp];
+    for (int row = blockIdx.x * wpb + warp; row < rows; row += gridDim.x * wpb) {
         const int z = row / X, x = row - z * X;
         const float *rp = img + z * V.isz + x * V.isx;
         for (int y0 = 0; y0 < Y; y0 += 32 * kMaxY) {
@@ -153,22 +163,38 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
                 const int y = y0 + 32 * k + (int)lane;
                 vals[k] = y < Y ? rp[y] : 0.f;
             }
+            // queue the voxels above the threshold (maxima.cu:19; a NaN
+            // threshold admits every voxel)
+            int qn = 0;
 #pragma unroll
             for (int k = 0; k < kMaxY; ++k) {
                 const int y = y0 + 32 * k + (int)lane;
+                const float v = xf(vals[k], t);
+                const bool up = y < Y && !(v <= th);
+                const unsigned m = __ballot_sync(0xffffffffu, up);
+                if (up) {
+                    const int at = qn + __popc(m & ((1u << lane) - 1));
+                    my_y[at] = y;
+                    my_v[at] = v;
+                }
+                qn += __popc(m);
+            }
+            __syncwarp();
+            for (int q0 = 0; q0 < qn; q0 += 32) {
+                const int qi = q0 + (int)lane;
                 bool is_max = false;
-                if (y < Y) {
-                    const float v = xf(vals[k], t);
-                    if (!(v <= th)) {  // maxima.cu:19 (a NaN threshold admits every voxel)
-                        is_max = true;
-                        for (int q = 0; q < nn; ++q) {
-                            const char4 o = sph[q];
-                            const int nz = refl(z + o.x, Z), nx = refl(x + o.y, X), ny = refl(y + o.z, Y);
-                            if (nz < 0 || nz >= Z || nx < 0 || nx >= X || ny < 0 || ny >= Y) continue;
-                            if (v < xf(img[nz * V.isz + nx * V.isx + ny], t)) {
-                                is_max = false;
-                                break;
-                            }
+                int y = 0;
+                if (qi < qn) {
+                    y = my_y[qi];
+                    const float v = my_v[qi];
+                    is_max = true;
+                    for (int q = 0; q < nn; ++q) {
+                        const char4 o = sph[q];
+                        const int nz = refl(z + o.x, Z), nx = refl(x + o.y, X), ny = refl(y + o.z, Y);
+                        if (nz < 0 || nz >= Z || nx < 0 || nx >= X || ny < 0 || ny >= Y) continue;
+                        if (v < xf(img[nz * V.isz + nx * V.isx + ny], t)) {
+                            is_max = false;
+                            break;
                         }
                     }
                 }
@@ -182,6 +208,7 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
                         cand[slot] = make_uint2((unsigned)z | ((unsigned)x << 16), (unsigned)y | ((unsigned)vi << 16));
                 }
             }
+            __syncwarp();
         }
     }
 }
@@ -213,7 +240,8 @@ __device__ __forceinline__ void warp_sum16(float (&v)[16], unsigned lane) {
 // Per-spot fit.  Each lane sums its samples in float32 after shifting the
 // image and raw values by the centre voxel's (every moment used below is
 // shift-invariant, so the shift removes the cancellation); the warp adds the
-// lanes' sums and lane 0 forms the statistics in double precision.  The
+// lanes' sums and lane 0 forms the statistics (the cancelling terms in double
+// precision, the quotients and roots in float, as the reference).  The
 // Gaussian weights depend only on the offset and the sigmas, so a block
 // tabulates them once.
 __global__ void __launch_bounds__(256)
@@ -221,6 +249,7 @@ k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand
       float sigmaZ, float sigmaXY, Xform t, float *__restrict__ out, unsigned out_cap,
       unsigned *__restrict__ out_count, int keep_filter) {
     __shared__ float gtab[kSphereCap];
+    __shared__ char4 otab[kSphereCap];
     t = xf_resolve(t);
     const unsigned lane = threadIdx.x & 31;
     const unsigned nc = min(*ncand, cap);
@@ -232,6 +261,7 @@ k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand
     if (table)
         for (int i = threadIdx.x; i < nsamp; i += blockDim.x) {
             const char4 o = g_fit_sphere[delta_fit][i];
+            otab[i] = o;
             gtab[i] = expf(-(o.x * o.x / gz + o.y * o.y / gxy + o.z * o.z / gxy));
         }
     __syncthreads();
@@ -259,7 +289,7 @@ k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand
             if (ci < nsamp) {
                 bool in;
                 if (table) {
-                    const char4 o = g_fit_sphere[delta_fit][ci];
+                    const char4 o = otab[ci];
                     dz = o.x; dx = o.y; dy = o.z;
                     in = true;
                 } else {
@@ -294,37 +324,39 @@ k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand
         }
         warp_sum16(acc, lane);
         for (int o = 16; o > 0; o >>= 1) vmin = fminf(vmin, __shfl_xor_sync(0xffffffffu, vmin, o));
-        const double N = acc[0];
-        if (lane != 0 || N == 0) continue;
-        const double Sv = acc[1], Svv = acc[2], Sg = acc[3], Sgg = acc[4], Svg = acc[5];
-        const double Sr = acc[6], Srr = acc[7], Srg = acc[8];
-        const double Sdz = acc[9], Sdx = acc[10], Sdy = acc[11], Svdz = acc[12], Svdx = acc[13], Svdy = acc[14];
-        const double mg = Sg / N, mv = Sv / N, mr = Sr / N;
-        const double varg = fmax(Sgg / N - mg * mg, 0.0);
-        const double varv = fmax(Svv / N - mv * mv, 0.0);
-        const double varr = fmax(Srr / N - mr * mr, 0.0);
-        const double stdg = sqrt(varg);
-        double stdv = sqrt(varv), stdr = sqrt(varr);
-        if (!(stdv > 0)) stdv = 1.0;
-        if (!(stdr > 0)) stdr = 1.0;
-        const double hn = (Svg / N - mv * mg) / (stdv * stdg);
-        const double a = (Srg / N - mr * mg) / (stdr * stdg);
+        if (lane != 0 || acc[0] == 0.f) continue;
+        // Only the variances and covariances cancel (mean square minus squared
+        // mean of the shifted values): they are formed in double precision; the
+        // quotients, roots and the centroid in float, as the reference does.
+        const double N = acc[0], invN = 1.0 / N;
+        const double mg = acc[3] * invN, mv = acc[1] * invN, mr = acc[6] * invN;
+        const float varg = (float)fmax(acc[4] * invN - mg * mg, 0.0);
+        const float varv = (float)fmax(acc[2] * invN - mv * mv, 0.0);
+        const float varr = (float)fmax(acc[7] * invN - mr * mr, 0.0);
+        const float covg_v = (float)(acc[5] * invN - mv * mg);
+        const float covg_r = (float)(acc[8] * invN - mr * mg);
+        const float stdg = sqrtf(varg);
+        float stdv = sqrtf(varv), stdr = sqrtf(varr);
+        if (!(stdv > 0.f)) stdv = 1.f;
+        if (!(stdr > 0.f)) stdr = 1.f;
+        const float hn = covg_v / (stdv * stdg);
+        const float a = covg_r / (stdr * stdg);
         // sum (c + d)(v - bg) / sum (v - bg), with v - bg = dv + (cv - bg)
-        const double shift = (double)cv - (double)vmin;
-        const double sw = Sv + N * shift;
-        double zc, xc, yc;
-        if (sw > 0) {
-            zc = z0 + (Svdz + shift * Sdz) / sw;
-            xc = x0 + (Svdx + shift * Sdx) / sw;
-            yc = y0 + (Svdy + shift * Sdy) / sw;
+        const float shift = cv - vmin;
+        const float sw = acc[1] + acc[0] * shift;
+        float zc, xc, yc;
+        if (sw > 0.f) {
+            zc = z0 + (acc[12] + shift * acc[9]) / sw;
+            xc = x0 + (acc[13] + shift * acc[10]) / sw;
+            yc = y0 + (acc[14] + shift * acc[11]) / sw;
         } else {
             zc = z0; xc = x0; yc = y0;
         }
         float row[8];
-        row[0] = (float)zc; row[1] = (float)xc; row[2] = (float)yc; row[3] = vmin;
-        row[4] = (float)a;
+        row[0] = zc; row[1] = xc; row[2] = yc; row[3] = vmin;
+        row[4] = a;
         row[5] = crw;
-        row[6] = (float)hn;
+        row[6] = hn;
         row[7] = cv;
         unsigned o;
         if (keep_filter) {
@@ -389,7 +421,7 @@ int mm_launch_maxima_fit(const MaximaArgs &a, uint2 *cand, unsigned cand_cap, un
     if (gx > 152 * 16) gx = 152 * 16;
     if (gx < 1) gx = 1;
     dim3 grid(gx, a.nvol);
-    k_maxima<<<grid, 256, 0, st>>>(V, a.th, a.delta, t, cand, cand_cap, ncand);
+    k_maxima<<<grid, 32 * kMaxWarps, 0, st>>>(V, a.th, a.delta, t, cand, cand_cap, ncand);
     MM_CHECK_LAUNCH();
     k_fit<<<152 * 8, 256, 0, st>>>(V, cand, ncand, cand_cap, a.delta_fit, a.sigmaZ, a.sigmaXY, t, out, out_cap,
                                    out_count, a.keep_filter);
