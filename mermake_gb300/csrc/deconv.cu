@@ -159,7 +159,6 @@ k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ 
             }
         }
     }
-    fft_gemm_tables<LMAX>(P, nl, L.scr);
     __syncthreads();
     float2 *R = fft_lines<false, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
 
@@ -199,7 +198,6 @@ k_rows_fwd_f32(const float *__restrict__ vol, long long nrows, float2 *__restric
         const long long row = row0 + q;
         Af[2 * sidx(e, q >> 1, nl) + (q & 1)] = row < nrows ? vol[row * n + e] : 0.f;
     }
-    fft_gemm_tables<LMAX>(P, nl, L.scr);
     __syncthreads();
     float2 *R = fft_lines<false, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
     for (int it = threadIdx.x; it < nl * H; it += blockDim.x) {
@@ -257,7 +255,6 @@ k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restri
             }
         }
     }
-    fft_gemm_tables<LMAX>(P, nl, L.scr);
     __syncthreads();
     float2 *R = fft_lines<true, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
     const float *Rf = reinterpret_cast<const float *>(R);

@@ -3,19 +3,22 @@
 // The deconvolution needs transforms at the exact padded tile lengths of the
 // reference (deconvolver.py:86-90, 155-157), which carry large prime factors
 // (678 = 2*3*113, 478 = 2*239, 148 = 4*37, 118 = 2*59, ...).  A length is
-// factored into stages of three kinds:
+// factored into stages of four kinds:
 //   * radix 2/3/4/5/6/7 and the odd primes 11..37: one thread per butterfly,
 //     values in registers;
-//   * primes 41..61, 79, 89 and 113 ("lane" stage; with 59, 79, 89 and 113
-//     the primes of the reference's padded lengths such as 118 = 2*59 and
-//     678 = 2*3*113): one warp per butterfly and one lane per
-//     output pair (k, R-k); each lane keeps its column of the DFT matrix in
-//     registers for the whole stage, and the warp reads the paired inputs
-//     a_r = x_r + x_{R-r}, b_r = x_r - x_{R-r} as shared-memory broadcasts
-//     (one 16-byte load per 4 FMAs);
+//   * 113 (678 = 6*113): Rader's algorithm, the 113-point DFT as a cyclic
+//     convolution of length 112 = 16*7 done with small register DFTs
+//     (stage_rader113);
+//   * primes 41..61, 79 and 89 ("lane" stage; 59, 79 and 89 are the primes of
+//     the reference's padded depths such as 118 = 2*59): one warp per
+//     butterfly and one lane per output pair (k, R-k); each lane keeps its
+//     column of the DFT matrix in registers for the whole stage, and the warp
+//     reads the paired inputs a_r = x_r + x_{R-r}, b_r = x_r - x_{R-r} as
+//     shared-memory broadcasts (one 16-byte load per 4 FMAs);
 //   * any other prime: a direct DFT with table look-ups ("generic" stage).
 // The lane and generic stages pair x[r] with x[R-r], halving the multiplies of a
-// plain DFT, and run first, where the Stockham twiddles are all 1.
+// plain DFT.  The large-prime stages run first, where the Stockham twiddles are
+// all 1.
 //
 // Layout: a CTA holds `nl` lines (a power of two); element e of line l is at
 // s[sidx(e, l, nl)] = s[e*nl + (l ^ (e & (nl-1)))]: lines are interleaved
@@ -263,7 +266,7 @@ __device__ __noinline__ void stage_odd_tab(const float2 *__restrict__ src, float
     }
 }
 
-// Lane stage (primes 41..113, see top): warps per butterfly, lane per output
+// Lane stage (primes 41..89, see top): warps per butterfly, lane per output
 // pair.  For H = (R-1)/2 <= 32 one warp covers all pairs and keeps the whole
 // DFT column (2H values) in registers.  For 32 < H <= 64 two k-groups of lanes
 // are needed, and the r range is split in halves between two warps as well, so
@@ -412,179 +415,120 @@ __device__ __noinline__ void stage_lane(const float2 *__restrict__ src, float2 *
     }
 }
 
-// GEMM form of a large odd prime stage, for CTAs of at least 512 threads.
-// With u_r = x_r + x_{R-r}, v_r = x_r - x_{R-r} (twiddled) and H = (R-1)/2:
-//   A_k = sum_{r=1..H} cos(2 pi r k / R) u_r   (k = 0..H; A_0 = sum u_r)
-//   B_k = sum_{r=1..H} sin(2 pi r k / R) v_r   (k = 1..H)
-//   forward X[k] = x_0 + A_k - i B_k, X[R-k] = x_0 + A_k + i B_k, X[0] = x_0 + A_0
-//   (inverse: the sign of B swaps).
-// Over the m * nl butterflies of the CTA these are two real matrix products
-// with constant matrices, computed register-blocked: a thread keeps 8 rows k
-// x 3 butterflies, reads its 8 coefficients of a column r as two broadcast
-// float4 and its 3 inputs, 48 FMA per 5 shared loads (the lane stage needs 4
-// FMA per load).  Phase 1 writes U and V over dst (2 H nb < n nl values),
-// phase 2 multiplies, then A and B go over dst ((2H + 1) nb = n nl values) and
-// phase 3 combines them into src: the stage's output is left in src.
-// The coefficient tables live in the lane-stage scratch (scr_all), written by
-// fft_gemm_tables at the start of the kernel, followed by x_0.
-template <int R>
-struct GemmStage {
-    static constexpr int H = (R - 1) / 2;
-    static constexpr int KA = (H + 1 + 7) / 8 * 8;  // rows k = 0..H of A, padded to 8
-    static constexpr int KB = (H + 7) / 8 * 8;      // rows k = 1..H of B, padded to 8
-    static __device__ __host__ constexpr size_t scr_floats(int nb) { return (size_t)H * (KA + KB) + 2 * nb; }
-    static __device__ __host__ constexpr int threads(int nb) { return (KA / 8 + KB / 8) * ((nb + 2) / 3); }
-};
-
-// The plan can use the GEMM form: one 113 stage, no lane stage (which would
-// reuse the scratch holding the coefficients), and enough threads and scratch.
-__device__ __forceinline__ bool fft_gemm_ok(const FftPlan &P, int nl) {
-    bool has = false;
-    for (int st = 0; st < P.nst; ++st) {
-        if (P.rad[st] == 113)
-            has = true;
-        else if (P.rad[st] > 37)
-            return false;
+// 16-point DFT in registers (n = n1 + 4 n2, k = k1 + 4 k2: 4-point DFTs over
+// n2, twiddles w16^(n1 k1), 4-point DFTs over n1), natural order in and out.
+template <bool INV>
+__device__ __forceinline__ void dft16(float2 *v) {
+    const float c1 = 0.92387953251128675613f, s1 = 0.38268343236508977173f, r2 = 0.70710678118654752440f;
+    // w16^e for e = 1, 2, 3, 4, 6, 9 (forward: exp(-2 pi i e / 16))
+    const float sg = INV ? 1.f : -1.f;
+    const float2 w1 = make_float2(c1, sg * s1), w2 = make_float2(r2, sg * r2), w3 = make_float2(s1, sg * c1);
+    const float2 w6 = make_float2(-r2, sg * r2), w9 = make_float2(-c1, -sg * s1);
+    float2 a[4][4];
+#pragma unroll
+    for (int n1 = 0; n1 < 4; ++n1) {
+        float2 t[4] = {v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]};
+        dft4<INV>(t);
+#pragma unroll
+        for (int k1 = 0; k1 < 4; ++k1) a[n1][k1] = t[k1];
     }
-    if (!has) return false;
-    const int nb = P.n / 113 * nl;
-    return (int)blockDim.x >= GemmStage<113>::threads(nb) &&
-           GemmStage<113>::scr_floats(nb) * sizeof(float) <=
-               sizeof(float4) * MM_FFT_SCR_PER_WARP * (blockDim.x >> 5);
-}
-
-// Coefficient tables of the GEMM stage (cos and sin of 2 pi r k / 113 from the
-// plan's table in global memory); called by every thread of a kernel that
-// runs fft_lines, before the barrier that precedes it, so that the work
-// overlaps the kernel's own loads.
-template <int LMAX>
-__device__ __forceinline__ void fft_gemm_tables(const FftPlan &P, int nl, float4 *scr_all) {
-    if constexpr (LMAX >= 113) {
-        if (!fft_gemm_ok(P, nl)) return;
-        using G = GemmStage<113>;
-        int pt = 0;
-        for (int st = 0; st < P.nst; ++st)
-            if (P.rad[st] == 113) pt = P.ptab[st];
-        const float2 *cs = P.tab + pt;
-        float *Ct = reinterpret_cast<float *>(scr_all);
-        float *St = Ct + G::H * G::KA;
-        for (int e = threadIdx.x; e < G::H * G::KA; e += blockDim.x) {
-            const int r = e / G::KA + 1, k = e % G::KA;
-            Ct[e] = k <= G::H ? cs[(r * k) % 113].x : 0.f;
-        }
-        for (int e = threadIdx.x; e < G::H * G::KB; e += blockDim.x) {
-            const int r = e / G::KB + 1, k = e % G::KB + 1;
-            St[e] = k <= G::H ? -cs[(r * k) % 113].y : 0.f;  // the table holds (cos, -sin)
-        }
+    a[1][1] = cmul(a[1][1], w1);
+    a[1][2] = cmul(a[1][2], w2);
+    a[1][3] = cmul(a[1][3], w3);
+    a[2][1] = cmul(a[2][1], w2);
+    a[2][2] = mul_i<INV>(a[2][2]);  // w16^4 = -+i
+    a[2][3] = cmul(a[2][3], w6);
+    a[3][1] = cmul(a[3][1], w3);
+    a[3][2] = cmul(a[3][2], w6);
+    a[3][3] = cmul(a[3][3], w9);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+        float2 t[4] = {a[0][k1], a[1][k1], a[2][k1], a[3][k1]};
+        dft4<INV>(t);
+#pragma unroll
+        for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = t[k2];
     }
 }
 
-template <int R, bool INV>
-__device__ __noinline__ void stage_gemm(float2 *__restrict__ src, float2 *__restrict__ dst, int n, int nl, int Ns,
-                                        const float2 *__restrict__ tw, const float2 *__restrict__ cs,
-                                        float4 *__restrict__ scr_all) {
-    using G = GemmStage<R>;
-    constexpr int H = G::H, KA = G::KA, KB = G::KB;
+// The 113-point stage by Rader's algorithm.  With g = 3 a primitive root,
+// X[g^m] = x_0 + sum_q u[q] h[(m - q) mod 112], u[q] = x[g^-q],
+// h[s] = w113^(g^s), and X[0] = x_0 + sum u: a cyclic convolution of length
+// 112 = 16 x 7, done as FFT-112, a product with the precomputed FFT of h
+// (already divided by 112), and an inverse FFT-112, in three passes over the
+// CTA's m * nl butterflies held in dst as T[q1 * 7 + k2][b]:
+//   1. gather u[q1 + 16 q2] (twiddled), 7-point DFT over q2, times w112^(q1 k2);
+//   2. per (k2, b): 16-point DFT over q1, product with H[k2 + 7 k1], inverse
+//      16-point DFT over k1, times w112^-(q1 k2), all in registers;
+//   3. inverse 7-point DFT over k2, then X[g^(q1 + 16 q2)] = x_0 + c into src.
+// About three times fewer arithmetic instructions than the direct DFT.  The
+// stage's output is left in src; x_0 and sum u go through scr_all.
+// tb: the stage's table (cos/sin, then the Rader tables of fft_plan.cu).
+template <bool INV>
+__device__ __noinline__ void stage_rader113(float2 *__restrict__ src, float2 *__restrict__ dst, int n, int nl,
+                                            int Ns, const float2 *__restrict__ tw, const float2 *__restrict__ tb,
+                                            float4 *__restrict__ scr_all) {
+    constexpr int R = 113;
     const int m = n / R, nb = m * nl;
     const int tstep = n / (Ns * R);
     const int lnl = log2_pow2(nl);
-    const float invNs = 1.0f / (float)Ns;
-    float *Ct = reinterpret_cast<float *>(scr_all);     // [r][k], k = 0..KA-1
-    float *St = Ct + H * KA;                            // [r][k - 1], k = 1..KB
-    float2 *x0s = reinterpret_cast<float2 *>(St + H * KB);
-    float2 *U = dst, *V = dst + H * nb;
+    const float invNs = 1.0f / (float)Ns, invnb = 1.0f / (float)nb;
+    const float2 *Hh = tb + R + (INV ? 112 : 0);
+    const float2 *w112 = tb + R + 224;
+    const int2 *gq = reinterpret_cast<const int2 *>(tb + R + 336);  // (g^-q, g^q)
+    float2 *x0s = reinterpret_cast<float2 *>(scr_all);
+    float2 *s0s = x0s + nb;
+    float2 *T = dst;
 
-    const float invnb = 1.0f / (float)nb;
-    // phase 1: x_0, U, V
-    for (int e = threadIdx.x; e < nb * (H + 1); e += blockDim.x) {
-        const int r = fdiv_i(e, nb, invnb), b = e - r * nb;
+    for (int e = threadIdx.x; e < 16 * nb; e += blockDim.x) {
+        const int q1 = fdiv_i(e, nb, invnb), b = e - q1 * nb;
         const int l = b & (nl - 1), j = b >> lnl;
-        if (r == 0) {
-            x0s[b] = src[sidx(j, l, nl)];
-            continue;
+        const int kk = Ns > 1 ? j - fdiv_i(j, Ns, invNs) * Ns : 0;
+        float2 v[7];
+#pragma unroll
+        for (int q2 = 0; q2 < 7; ++q2) {
+            const int r = gq[q1 + 16 * q2].x;
+            float2 x = src[sidx(j + r * m, l, nl)];
+            if (Ns > 1) {
+                const float2 w = tw[kk * r * tstep];
+                x = INV ? cmulc(x, w) : cmul(x, w);
+            }
+            v[q2] = x;
         }
-        float2 u = src[sidx(j + r * m, l, nl)], v = src[sidx(j + (R - r) * m, l, nl)];
-        if (Ns > 1) {
-            const int kk = j - fdiv_i(j, Ns, invNs) * Ns;
-            const float2 wu = tw[kk * r * tstep], wv = tw[kk * (R - r) * tstep];
-            u = INV ? cmulc(u, wu) : cmul(u, wu);
-            v = INV ? cmulc(v, wv) : cmul(v, wv);
-        }
-        U[(r - 1) * nb + b] = cadd(u, v);
-        V[(r - 1) * nb + b] = csub(u, v);
+        if (q1 == 0) x0s[b] = src[sidx(j, l, nl)];
+        dft_small<7, false>(v);
+        T[(q1 * 7) * nb + b] = v[0];
+#pragma unroll
+        for (int k2 = 1; k2 < 7; ++k2) T[(q1 * 7 + k2) * nb + b] = cmul(v[k2], w112[q1 * k2]);
     }
     __syncthreads();
-    // phase 2: thread = (part, 8 rows, 3 butterflies)
-    const int nbb = (nb + 2) / 3;
-    const int itemsA = (KA / 8) * nbb;
-    const int it = threadIdx.x;
-    const bool active = it < itemsA + (KB / 8) * nbb;
-    const bool partB = it >= itemsA;
-    const int rel = partB ? it - itemsA : it;
-    const int kb = rel / nbb, b0 = (rel - kb * nbb) * 3;
-    float2 acc[8][3];
+    for (int e = threadIdx.x; e < 7 * nb; e += blockDim.x) {
+        const int k2 = fdiv_i(e, nb, invnb), b = e - k2 * nb;
+        float2 v[16];
 #pragma unroll
-    for (int q = 0; q < 8; ++q)
+        for (int q1 = 0; q1 < 16; ++q1) v[q1] = T[(q1 * 7 + k2) * nb + b];
+        dft16<false>(v);
+        if (k2 == 0) s0s[b] = v[0];
 #pragma unroll
-        for (int i = 0; i < 3; ++i) acc[q][i] = make_float2(0.f, 0.f);
-    if (active) {
-        const int cstride = partB ? KB : KA;
-        const float *cp = (partB ? St : Ct) + kb * 8;
-        const float2 *ip = (partB ? V : U) + b0;
-#pragma unroll 4
-        for (int r = 0; r < H; ++r) {
-            const float4 c0 = *reinterpret_cast<const float4 *>(cp + r * cstride);
-            const float4 c1 = *reinterpret_cast<const float4 *>(cp + r * cstride + 4);
-            const float c[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
-            float2 in[3];
+        for (int k1 = 0; k1 < 16; ++k1) v[k1] = cmul(v[k1], Hh[k2 + 7 * k1]);
+        dft16<true>(v);
+        T[k2 * nb + b] = v[0];
 #pragma unroll
-            for (int i = 0; i < 3; ++i) in[i] = ip[r * nb + i];  // reads past nb stay inside dst
-#pragma unroll
-            for (int q = 0; q < 8; ++q)
-#pragma unroll
-                for (int i = 0; i < 3; ++i) {
-                    acc[q][i].x = fmaf(c[q], in[i].x, acc[q][i].x);
-                    acc[q][i].y = fmaf(c[q], in[i].y, acc[q][i].y);
-                }
-        }
+        for (int q1 = 1; q1 < 16; ++q1) T[(q1 * 7 + k2) * nb + b] = cmulc(v[q1], w112[q1 * k2]);
     }
     __syncthreads();
-    // A rows k = 0..H at dst[k nb + b], B rows k = 1..H at dst[(H + k) nb + b]
-    if (active) {
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-            const int k = kb * 8 + q + (partB ? 1 : 0);
-            if (k > H) break;
-            float2 *row = dst + (size_t)(partB ? H + k : k) * nb;
-#pragma unroll
-            for (int i = 0; i < 3; ++i)
-                if (b0 + i < nb) row[b0 + i] = acc[q][i];
-        }
-    }
-    __syncthreads();
-    // phase 3: combine into src
-    for (int e = threadIdx.x; e < nb * (H + 1); e += blockDim.x) {
-        const int k = fdiv_i(e, nb, invnb), b = e - k * nb;
+    for (int e = threadIdx.x; e < 16 * nb; e += blockDim.x) {
+        const int q1 = fdiv_i(e, nb, invnb), b = e - q1 * nb;
         const int l = b & (nl - 1), j = b >> lnl;
         const int kk = Ns > 1 ? j - fdiv_i(j, Ns, invNs) * Ns : 0;
         const int d = (j - kk) * R + kk;
+        float2 v[7];
+#pragma unroll
+        for (int k2 = 0; k2 < 7; ++k2) v[k2] = T[(q1 * 7 + k2) * nb + b];
+        dft_small<7, true>(v);
         const float2 x0 = x0s[b];
-        const float2 a = cadd(dst[(size_t)k * nb + b], x0);
-        if (k == 0) {
-            src[sidx(d, l, nl)] = a;
-            continue;
-        }
-        const float2 bv = dst[(size_t)(H + k) * nb + b];
-        float2 o1, o2;
-        if (!INV) {
-            o1 = make_float2(a.x + bv.y, a.y - bv.x);
-            o2 = make_float2(a.x - bv.y, a.y + bv.x);
-        } else {
-            o1 = make_float2(a.x - bv.y, a.y + bv.x);
-            o2 = make_float2(a.x + bv.y, a.y - bv.x);
-        }
-        src[sidx(d + k * Ns, l, nl)] = o1;
-        src[sidx(d + (R - k) * Ns, l, nl)] = o2;
+#pragma unroll
+        for (int q2 = 0; q2 < 7; ++q2) src[sidx(d + gq[q1 + 16 * q2].y * Ns, l, nl)] = cadd(x0, v[q2]);
+        if (q1 == 0) src[sidx(d, l, nl)] = cadd(x0, s0s[b]);
     }
 }
 
@@ -694,8 +638,8 @@ __device__ void stage_generic(float2 *__restrict__ src, float2 *__restrict__ dst
 #define MM_ODD_CASE(R) \
     case R: stage_odd_tab<R, INV>(src, dst, P.n, nl, Ns, tw_s, tab_s + P.ptab[st]); break;
 
-// LMAX: the largest prime given a lane stage in this instantiation (0, 63 or
-// 127; the host picks the class of the plan, mm_fft_lane_class), so that
+// LMAX: the largest prime given a lane (or, at 127, the Rader) stage in this
+// instantiation (0, 63 or 127; the host picks the class of the plan), so that
 // kernels whose lengths only need small lane stages keep fewer registers.
 template <bool INV, int LMAX>
 __device__ float2 *fft_lines(float2 *A, float2 *B, int nl, const FftPlan &P,
@@ -704,11 +648,11 @@ __device__ float2 *fft_lines(float2 *A, float2 *B, int nl, const FftPlan &P,
     for (int st = 0; st < P.nst; ++st) {
         const int R = P.rad[st], Ns = P.ns[st];
         if constexpr (LMAX >= 113) {
-            // 113 in GEMM form (tables from fft_gemm_tables)
-            if (R == 113 && fft_gemm_ok(P, nl)) {
-                stage_gemm<113, INV>(src, dst, P.n, nl, Ns, tw_s, tab_s + P.ptab[st], scr);
+            // 113 by Rader's algorithm (output left in src)
+            if (R == 113) {
+                stage_rader113<INV>(src, dst, P.n, nl, Ns, tw_s, tab_s + P.ptab[st], scr);
                 __syncthreads();
-                continue;  // output left in src
+                continue;
             }
         }
         switch (R) {
@@ -721,7 +665,7 @@ __device__ float2 *fft_lines(float2 *A, float2 *B, int nl, const FftPlan &P,
             MM_ODD_CASE(11) MM_ODD_CASE(13) MM_ODD_CASE(17) MM_ODD_CASE(19) MM_ODD_CASE(23)
             MM_ODD_CASE(29) MM_ODD_CASE(31) MM_ODD_CASE(37)
             MM_LANE_CASE(41) MM_LANE_CASE(43) MM_LANE_CASE(47) MM_LANE_CASE(53) MM_LANE_CASE(59)
-            MM_LANE_CASE(61) MM_LANE_CASE(79) MM_LANE_CASE(89) MM_LANE_CASE(113)
+            MM_LANE_CASE(61) MM_LANE_CASE(79) MM_LANE_CASE(89)
             default: stage_generic<INV>(src, dst, P.n, nl, R, Ns, tw_s, tab_s + P.ptab[st]); break;
         }
         __syncthreads();

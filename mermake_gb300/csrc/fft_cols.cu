@@ -27,7 +27,6 @@ k_cols(float2 *__restrict__ S, long long se, int nlines, long long plane_stride,
         else
             L.A[sidx(e, l, nl)] = make_float2(0.f, 0.f);
     }
-    fft_gemm_tables<LMAX>(P, nl, L.scr);
     cp_async_wait_all();
     __syncthreads();
     float2 *R = fft_lines<INV, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);

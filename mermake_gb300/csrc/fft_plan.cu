@@ -2,6 +2,7 @@
 // (device, length) for the life of the process.
 #include <math.h>
 #include <stdlib.h>
+#include <string.h>
 
 #include <algorithm>
 #include <map>
@@ -39,6 +40,45 @@ void factor(int n, std::vector<int> &first, std::vector<int> &small) {
     // the table-driven odd stages go after the large ones, before the constant radices
     small.insert(small.begin(), mid.begin(), mid.end());
 }
+// Rader tables of the 113-point stage (stage_rader113 in fft.cuh), appended
+// after its cos/sin table: the FFT-112 of the Rader sequence
+// h[s] = exp(-+2 pi i g^s / 113) / 112 for the forward and the inverse
+// transform, the twiddles exp(-2 pi i m / 112), and the index pairs
+// (g^-q mod 113, g^q mod 113) stored as the bits of a float2; g = 3.
+void rader113_tables(std::vector<float2> &tab) {
+    constexpr int R = 113, M = 112, g = 3;
+    int gp[M], gi[M];
+    int ginv = 1;
+    for (int e = 0; e < R - 2; ++e) ginv = ginv * g % R;  // g^(R-2) = g^-1
+    gp[0] = gi[0] = 1;
+    for (int q = 1; q < M; ++q) {
+        gp[q] = gp[q - 1] * g % R;
+        gi[q] = gi[q - 1] * ginv % R;
+    }
+    for (int dir = 0; dir < 2; ++dir) {
+        const double sgn = dir == 0 ? -1.0 : 1.0;
+        for (int k = 0; k < M; ++k) {
+            double re = 0.0, im = 0.0;
+            for (int s = 0; s < M; ++s) {
+                const double a = sgn * 2.0 * M_PI * (double)gp[s] / (double)R;
+                const double b = -2.0 * M_PI * (double)((long)s * k % M) / (double)M;
+                re += cos(a + b);
+                im += sin(a + b);
+            }
+            tab.push_back(make_float2((float)(re / M), (float)(im / M)));
+        }
+    }
+    for (int m = 0; m < M; ++m) {
+        const double a = -2.0 * M_PI * (double)m / (double)M;
+        tab.push_back(make_float2((float)cos(a), (float)sin(a)));
+    }
+    for (int q = 0; q < M; ++q) {
+        float2 e;
+        memcpy(&e.x, &gi[q], sizeof(int));
+        memcpy(&e.y, &gp[q], sizeof(int));
+        tab.push_back(e);
+    }
+}
 }  // namespace
 
 int mm_fft_plan_get(int n, FftPlan *out) {
@@ -69,6 +109,7 @@ int mm_fft_plan_get(int n, FftPlan *out) {
             double a = -2.0 * M_PI * (double)m / (double)R;
             tab.push_back(make_float2((float)cos(a), (float)sin(a)));
         }
+        if (R == 113) rader113_tables(tab);
         Ns *= R;
         P.nst++;
     }
@@ -86,7 +127,8 @@ int mm_fft_plan_get(int n, FftPlan *out) {
         Ns *= R;
         P.nst++;
     }
-    // lane-stage class (fft.cuh): 0 none, 63 primes 41..61, 127 also 79, 89, 113
+    // stage class (fft.cuh): 0 none, 63 lane primes 41..61, 127 also the lane
+    // primes 79, 89 and the Rader stage 113
     P.lclass = 0;
     for (int i = 0; i < P.nst; ++i) {
         const int R = P.rad[i];

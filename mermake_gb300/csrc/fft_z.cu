@@ -34,7 +34,6 @@ k_zpass(TileGeom g, float2 *__restrict__ S, const float2 *__restrict__ W, long l
     int *zmap = reinterpret_cast<int *>(Ws + (size_t)n * kZq);
     fft_load_tables(P, L.tw, L.tab);
     for (int e = threadIdx.x; e < n; e += blockDim.x) zmap[e] = mm_map_z(e, g.Z, g.zpad, g.Zp);
-    fft_gemm_tables<LMAX>(P, nl, L.scr);
     __syncthreads();
     const long long plane = (long long)g.P * g.H;
     const long long q0 = (long long)blockIdx.x * kZq;
@@ -98,7 +97,6 @@ k_zfwd(float2 *__restrict__ S, long long plane, FftPlan P, int nl) {
         else
             L.A[sidx(e, l, nl)] = make_float2(0.f, 0.f);
     }
-    fft_gemm_tables<LMAX>(P, nl, L.scr);
     cp_async_wait_all();
     __syncthreads();
     float2 *R = fft_lines<false, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
