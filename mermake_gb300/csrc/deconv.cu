@@ -269,30 +269,35 @@ k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restri
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     // odd segment length: the 32 lanes' strided reads fall in distinct banks
     const int seg = ((n + 31) / 32) | 1;
-    // mean = sum x (1 / count): the full window's reciprocal is computed once
-    const int full = 2 * delta + 1;
-    const float inv_full = 1.0f / (float)full;
-    for (int q = warp; q < 2 * nl; q += nw) {
-        const int l = q >> 1, comp = q & 1;
+    // mean = sum x (1 / count), the reciprocals of the window counts from a
+    // table in the (now idle) scratch
+    float *rtab = reinterpret_cast<float *>(L.scr);
+    for (int c = threadIdx.x; c <= 2 * delta + 1; c += blockDim.x) rtab[c] = c ? 1.0f / (float)c : 0.f;
+    __syncthreads();
+    // a warp per line: both real rows of the line at once (float2 reads, all banks)
+    for (int l = warp; l < nl; l += nw) {
         const int s0 = lane * seg, s1 = min(s0 + seg, n);
         if (s0 < n) {
             int lo = max(s0 - delta, 0), hi = min(s0 + delta, n - 1);
-            float sum = 0.f;
-            for (int i = lo; i <= hi; ++i) sum += Rf[2 * sidx(i, l, nl) + comp];
+            float2 sum = make_float2(0.f, 0.f);
+            for (int i = lo; i <= hi; ++i) sum = cadd(sum, R[sidx(i, l, nl)]);
             for (int e = s0; e < s1; ++e) {
                 if (e > s0) {
                     const int add = e + delta, drop = e - delta - 1;
-                    if (add <= n - 1) sum += Rf[2 * sidx(add, l, nl) + comp];
-                    if (drop >= 0) sum -= Rf[2 * sidx(drop, l, nl) + comp];
+                    if (add <= n - 1) sum = cadd(sum, R[sidx(add, l, nl)]);
+                    if (drop >= 0) sum = csub(sum, R[sidx(drop, l, nl)]);
                 }
-                const int cnt = min(e + delta, n - 1) - max(e - delta, 0) + 1;
-                Bf[q * n + e] = sum * (cnt == full ? inv_full : 1.0f / (float)cnt);
+                const float rc = rtab[min(e + delta, n - 1) - max(e - delta, 0) + 1];
+                Bf[(2 * l) * n + e] = sum.x * rc;
+                Bf[(2 * l + 1) * n + e] = sum.y * rc;
             }
         }
         __syncwarp();
-        const long long row = row0 + q;
-        if (row < nrows)
-            for (int e = lane; e < n; e += 32) blur[row * n + e] = Bf[q * n + e];
+        for (int c = 0; c < 2; ++c) {
+            const long long row = row0 + 2 * l + c;
+            if (row < nrows)
+                for (int e = lane; e < n; e += 32) blur[row * n + e] = Bf[(2 * l + c) * n + e];
+        }
     }
 }
 
@@ -303,10 +308,11 @@ k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restri
 // consecutive y columns held in shared memory; each warp slides the window
 // down a segment of rows.  delta < 0: no blur (res copied).
 // ---------------------------------------------------------------------------
+template <bool STITCH>
 __global__ void __launch_bounds__(kThreads)
 k_blur_x_sub(TileGeom g, const float *__restrict__ res, const float *__restrict__ tmp, int delta,
              float *res_out, float *__restrict__ stitch, long long osz, long long osx) {
-    extern __shared__ __align__(16) float colbuf[];  // P x 32
+    extern __shared__ __align__(16) float colbuf[];  // P x 32, then the reciprocal table
     const int P = g.P;
     const int ti = g.t0 + blockIdx.z;
     const TileDesc d = mm_tile_desc(g, ti);
@@ -315,6 +321,7 @@ k_blur_x_sub(TileGeom g, const float *__restrict__ res, const float *__restrict_
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
     const int y = y0 + lane;
     const long long pbase = ((long long)blockIdx.z * g.Z + z) * P * P;
+    float *rtab = colbuf + P * 32;  // 1 / count for counts 0..2 delta + 1
     if (delta >= 0) {
         for (int x = warp; x < P; x += nw) {
             if (y < P)
@@ -322,41 +329,41 @@ k_blur_x_sub(TileGeom g, const float *__restrict__ res, const float *__restrict_
             else
                 colbuf[x * 32 + lane] = 0.f;
         }
+        for (int c = threadIdx.x; c <= 2 * delta + 1; c += blockDim.x) rtab[c] = c ? 1.0f / (float)c : 0.f;
         cp_async_wait_all();
         __syncthreads();
     }
     const int seg = (P + nw - 1) / nw;
     const int x0 = warp * seg, x1 = min(x0 + seg, P);
-    const int full = 2 * delta + 1;
-    const float inv_full = 1.0f / (float)(full > 0 ? full : 1);
     float sum = 0.f;
     if (delta >= 0 && x0 < P) {
         const int lo = max(x0 - delta, 0), hi = min(x0 + delta, P - 1);
         for (int i = lo; i <= hi; ++i) sum += colbuf[i * 32 + lane];
     }
+    const bool yok = y < P;
     constexpr int U = 8;  // rows of res loaded ahead of the in-place stores
     for (int xb = x0; xb < x1; xb += U) {
         float v[U];
 #pragma unroll
         for (int u = 0; u < U; ++u)
-            v[u] = (y < P && xb + u < x1) ? res[pbase + (long long)(xb + u) * P + y] : 0.f;
+            v[u] = (yok && xb + u < x1) ? res[pbase + (long long)(xb + u) * P + y] : 0.f;
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int x = xb + u;
             if (x >= x1) break;
-            if (delta >= 0 && x > x0) {
-                const int add = x + delta, drop = x - delta - 1;
-                if (add <= P - 1) sum += colbuf[add * 32 + lane];
-                if (drop >= 0) sum -= colbuf[drop * 32 + lane];
-            }
-            if (y >= P) continue;
             float val = v[u];
             if (delta >= 0) {
-                const int cnt = min(x + delta, P - 1) - max(x - delta, 0) + 1;
-                val = val - sum * (cnt == full ? inv_full : 1.0f / (float)cnt);
+                // x is the same for the whole warp: the branches do not diverge
+                if (x > x0) {
+                    const int add = x + delta, drop = x - delta - 1;
+                    if (add <= P - 1) sum += colbuf[add * 32 + lane];
+                    if (drop >= 0) sum -= colbuf[drop * 32 + lane];
+                }
+                val -= sum * rtab[min(x + delta, P - 1) - max(x - delta, 0) + 1];
             }
+            if (!yok) continue;
             if (res_out) res_out[pbase + (long long)x * P + y] = val;
-            if (stitch && x >= g.ov && x < d.xend - g.ov && y >= g.ov && y < d.yend - g.ov) {
+            if (STITCH && x >= g.ov && x < d.xend - g.ov && y >= g.ov && y < d.yend - g.ov) {
                 const int ox = d.x + x - g.ov, oy = d.y + y - g.ov;
                 // inside its own span a tile is the final writer; past it, ask who is
                 const bool own = ox < d.x + g.ts && oy < d.y + g.ts;
@@ -447,11 +454,17 @@ int mm_launch_rows_inv(const float2 *S, int nrows, int Pn, int H, float *out, fl
 
 int mm_launch_blur_x_sub(const TileGeom &g, const float *res, const float *tmp, int delta, float *res_out,
                          float *stitch, long long osz, long long osx, cudaStream_t st) {
-    size_t sm = delta >= 0 ? (size_t)g.P * 32 * sizeof(float) : 0;
+    size_t sm = delta >= 0 ? ((size_t)g.P * 32 + 2 * delta + 2) * sizeof(float) : 0;
+    MM_REQUIRE(sm <= (size_t)kSmemLimit, "blur radius %d too large for the tile", delta);
     int rc;
-    if ((rc = set_smem(k_blur_x_sub, sm > 0 ? sm : 1))) return rc;
     dim3 grid(mm_cdiv(g.P, 32), g.Z, g.nt);
-    k_blur_x_sub<<<grid, kThreads, sm, st>>>(g, res, tmp, delta, res_out, stitch, osz, osx);
+    if (stitch) {
+        if ((rc = set_smem(k_blur_x_sub<true>, sm > 0 ? sm : 1))) return rc;
+        k_blur_x_sub<true><<<grid, kThreads, sm, st>>>(g, res, tmp, delta, res_out, stitch, osz, osx);
+    } else {
+        if ((rc = set_smem(k_blur_x_sub<false>, sm > 0 ? sm : 1))) return rc;
+        k_blur_x_sub<false><<<grid, kThreads, sm, st>>>(g, res, tmp, delta, res_out, stitch, osz, osx);
+    }
     MM_CHECK_LAUNCH();
     return MM_OK;
 }

@@ -176,26 +176,41 @@ k_zop_apply(float2 *__restrict__ S, const float2 *__restrict__ w, int Z, int Zp,
         cp_async_wait_group<1>();
     }
     __syncthreads();
-    // M[i][j] = sum over the copies of plane j of ws[(i + off) mod Zp]
+    // M[i][j] = sum over the copies of plane j of ws[(i + off) mod Zp]: a thread
+    // per (j, p) adds each copy's run of the kernel, ten rows i at a time (the
+    // run wraps past Zp at most once, handled by the slow branch)
     for (int q = tid; q < Z * kPB; q += nth) {
         const int j = q / kPB, pp = q - j * kPB;
         const int n = tab.n[j];
-        int d[MM_ZOP_MAX_COPIES];
-#pragma unroll
-        for (int k = 0; k < MM_ZOP_MAX_COPIES; ++k) d[k] = tab.off[j][k];
         float2 *col = Ms + j * kPB + pp;
-        for (int i = 0; i < Z; ++i) {
-            float2 v = make_float2(0.f, 0.f);
+        for (int i0 = 0; i0 < Z; i0 += 10) {
+            float2 acc[10];
 #pragma unroll
-            for (int k = 0; k < MM_ZOP_MAX_COPIES; ++k) {
-                if (k < n) {
-                    const float2 t = ws[d[k] * kPB + pp];
-                    v.x += t.x;
-                    v.y += t.y;
+            for (int ii = 0; ii < 10; ++ii) acc[ii] = make_float2(0.f, 0.f);
+            for (int k = 0; k < n; ++k) {
+                int d0 = tab.off[j][k] + i0;
+                if (d0 >= Zp) d0 -= Zp;
+                if (d0 + 10 <= Zp) {
+                    const float2 *wp = ws + d0 * kPB + pp;
+#pragma unroll
+                    for (int ii = 0; ii < 10; ++ii) {
+                        const float2 t = wp[ii * kPB];
+                        acc[ii].x += t.x;
+                        acc[ii].y += t.y;
+                    }
+                } else {
+#pragma unroll
+                    for (int ii = 0; ii < 10; ++ii) {
+                        const int dd = (d0 + ii) % Zp;
+                        const float2 t = ws[dd * kPB + pp];
+                        acc[ii].x += t.x;
+                        acc[ii].y += t.y;
+                    }
                 }
-                d[k] = d[k] + 1 == Zp ? 0 : d[k] + 1;
             }
-            col[i * msw] = v;
+#pragma unroll
+            for (int ii = 0; ii < 10; ++ii)
+                if (i0 + ii < Z) col[(i0 + ii) * msw] = acc[ii];
         }
     }
 
