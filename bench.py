@@ -22,7 +22,8 @@ A step is one FOV of the workload, inputs resident in HBM:
 ``--form plain`` times the per-tile loop of ``Deconvolver.tile_wise`` +
 ``find_local_maxima`` instead.  ``e2e`` is the same metric through the same
 public calls with the channels copied from pinned host memory every step and
-the spot tables read back.  ``roofline`` reports the dominant kernel (largest
+the spot tables read back; in the batched form through ``pipeline.FovRunner``,
+which copies the next FOV on a side stream while the current one computes.  ``roofline`` reports the dominant kernel (largest
 share of device time in the timed region) from the library's per-stage CUDA
 events, against the measured HBM copy bandwidth.  ``--impl reference`` times
 the CPU restatement of the reference's functions (FP64 NumPy/SciPy FFT
@@ -321,24 +322,56 @@ def gpu_arm(args, rank, world, local):
 
     if not args.no_e2e:
         import torch
+
+        from mermake_gb300 import pipeline
         host_ch = [c.cpu().pin_memory() for c in s["chans"]]
         host_dapi = s["dapi"].cpu().pin_memory() if s["dapi"] is not None else None
-        dev_ch = [torch.empty_like(c) for c in s["chans"]]
-        dev_dapi = torch.empty_like(s["dapi"]) if s["dapi"] is not None else None
         io = {"h2d": 0, "d2h": 0}
+        if args.form == "batched":
+            # the public FovRunner: FOV k+1's channels are copied from pinned host
+            # memory on a side stream while FOV k computes; every step copies one
+            # FOV and computes one FOV, and the timed region ends after the last
+            # copy it issued
+            runner = pipeline.FovRunner(s["dec_h"], s["dec_d"], w["hyb"], w.get("dapi_args"))
+            state = {}
 
-        def e2e_step():
-            for h, d in zip(host_ch, dev_ch):
-                d.copy_(h, non_blocking=True)
-            if host_dapi is not None:
-                dev_dapi.copy_(host_dapi, non_blocking=True)
-            outs = run_fov(s, args.form, chans=dev_ch, dapi=dev_dapi)
-            hb = [o.to("cpu") for o in outs]
-            io["h2d"] = sum(h.numel() * h.element_size() for h in host_ch) + (
-                host_dapi.numel() * host_dapi.element_size() if host_dapi is not None else 0)
-            io["d2h"] = sum(h.numel() * h.element_size() for h in hb)
+            def e2e_step():
+                t = state.pop("ticket", None) or runner.submit(host_dapi, host_ch)
+                state["ticket"] = runner.submit(host_dapi, host_ch)
+                p, m, rows = runner.run(t, s["flats"])
+                io["h2d"] = runner.h2d_bytes
+                io["d2h"] = sum(a.nbytes for a in [p, m] + rows if a is not None)
 
-        e_ms, _ = timed(e2e_step, args.steps, 1, barrier)
+            for _ in range(max(args.warmup, 1)):
+                e2e_step()
+            torch.cuda.synchronize()
+            barrier()
+            st = torch.cuda.current_stream()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(args.steps):
+                e2e_step()
+            st.wait_stream(runner.copy_stream)
+            e1.record(st)
+            torch.cuda.synchronize()
+            barrier()
+            e_ms = e0.elapsed_time(e1)
+        else:
+            dev_ch = [torch.empty_like(c) for c in s["chans"]]
+            dev_dapi = torch.empty_like(s["dapi"]) if s["dapi"] is not None else None
+
+            def e2e_step():
+                for h, d in zip(host_ch, dev_ch):
+                    d.copy_(h, non_blocking=True)
+                if host_dapi is not None:
+                    dev_dapi.copy_(host_dapi, non_blocking=True)
+                outs = run_fov(s, args.form, chans=dev_ch, dapi=dev_dapi)
+                hb = [o.to("cpu") for o in outs]
+                io["h2d"] = sum(h.numel() * h.element_size() for h in host_ch) + (
+                    host_dapi.numel() * host_dapi.element_size() if host_dapi is not None else 0)
+                io["d2h"] = sum(h.numel() * h.element_size() for h in hb)
+
+            e_ms, _ = timed(e2e_step, args.steps, 1, barrier)
         t = torch.tensor([e_ms], device=dev)
         if pg:
             pg.all_reduce(t, op=pg.ReduceOp.MAX)

@@ -105,3 +105,75 @@ def dapi_spots(dec, image, flat_field=None, *, threshold=None, delta=1, delta_fi
         _lib.check(rc)
         return op[: n_p.value], om[: n_m.value], buffer, float(rms.value)
     raise _lib.MermakeError("spot rows did not fit after resizing")
+
+
+class FovRunner:
+    """Whole FOVs from pinned host memory, with the next FOV's channels copied
+    to the device on a side stream while the current FOV computes: the role of
+    the reference's prefetching ``ImageQueue`` (mermake/io.py:405-463) for the
+    host-to-device step of ``__main__.py:211-283``.
+
+    ``submit(dapi, colours)`` enqueues the copies of one FOV (uint16 host
+    arrays, pinned for overlap) into the next of two device slots and returns
+    a ticket; ``run(ticket, flats)`` waits for that FOV's copies channel by
+    channel and returns ``(Xh_plus, Xh_minus, [Xh per colour])`` as host
+    arrays.  Submit FOV k+1 before running FOV k to overlap them.
+    """
+
+    def __init__(self, dec_hyb, dec_dapi=None, hyb_args=None, dapi_args=None, batch=0):
+        self.dec_hyb, self.dec_dapi = dec_hyb, dec_dapi
+        self.hyb_args = dict(hyb_args or {})
+        self.dapi_args = dict(dapi_args or {})
+        self.batch = batch
+        self.copy_stream = torch.cuda.Stream()
+        self._slots = [dict(), dict()]
+        self._next = 0
+        self._buffer = None
+        self.h2d_bytes = 0
+
+    def _dev(self, slot, key, host):
+        buf = self._slots[slot].get(key)
+        if buf is None or buf.shape != host.shape or buf.dtype != host.dtype:
+            buf = torch.empty(host.shape, dtype=host.dtype, device="cuda")
+            self._slots[slot][key] = buf
+        return buf
+
+    def submit(self, dapi, colours):
+        slot = self._next
+        self._next ^= 1
+        ticket = {"slot": slot, "events": [], "dev": [], "free": self._slots[slot].get("free")}
+        cs = self.copy_stream
+        if ticket["free"] is not None:
+            cs.wait_event(ticket["free"])  # the slot's previous FOV is done with its buffers
+        nbytes = 0
+        with torch.cuda.stream(cs):
+            for k, h in enumerate(([dapi] if dapi is not None else []) + list(colours)):
+                d = self._dev(slot, k, h)
+                d.copy_(h, non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(cs)
+                ticket["events"].append(ev)
+                ticket["dev"].append(d)
+                nbytes += h.numel() * h.element_size()
+        ticket["has_dapi"] = dapi is not None
+        self.h2d_bytes = nbytes
+        return ticket
+
+    def run(self, ticket, flats=None, dapi_flat=None):
+        cur = torch.cuda.current_stream()
+        evs, devs = list(ticket["events"]), list(ticket["dev"])
+        out_plus = out_minus = None
+        if ticket["has_dapi"]:
+            cur.wait_event(evs.pop(0))
+            p, m, self._buffer, _ = dapi_spots(self.dec_dapi, devs.pop(0), dapi_flat, buffer=self._buffer,
+                                               batch=self.batch, **self.dapi_args)
+            out_plus, out_minus = p.cpu().numpy(), m.cpu().numpy()
+        flats = list(flats) if flats is not None else [None] * len(devs)
+        rows = []
+        for ev, d, f in zip(evs, devs, flats):
+            cur.wait_event(ev)
+            rows.append(hyb_spots(self.dec_hyb, d, f, batch=self.batch, **self.hyb_args).cpu().numpy())
+        done = torch.cuda.Event()
+        done.record(cur)
+        self._slots[ticket["slot"]]["free"] = done
+        return out_plus, out_minus, rows

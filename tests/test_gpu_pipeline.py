@@ -121,3 +121,32 @@ def test_dapi_batched_equals_stepwise(mm):
     np.testing.assert_array_equal(ck.sort_rows(plus.cpu().numpy()), ck.sort_rows(p2.cpu().numpy()))
     np.testing.assert_array_equal(ck.sort_rows(minus.cpu().numpy()), ck.sort_rows(m2.cpu().numpy()))
     assert len(plus) > 0 and len(minus) > 0
+
+
+def test_fov_runner_matches_direct_calls(mm):
+    """FovRunner (pinned host channels, copies of FOV k+1 overlapping FOV k)
+    gives the rows of the direct dapi_spots / hyb_spots calls, FOV after FOV,
+    with both device slots reused."""
+    Z, X, Y = 12, 170, 150
+    dapi = mm["synth"].dapi_stack(Z, X, Y, 5, n_nuclei=12, radii=(3.0, 12.0, 12.0))
+    cols, flats = [], []
+    for seed in (1, 2):
+        img, flat, psf = hyb_case(mm, seed=seed, Z=Z, X=X, Y=Y)
+        cols.append(img.cpu().pin_memory())
+        flats.append(torch.from_numpy(flat).cuda())
+    dh = mm["dc"].Deconvolver(psf, (Z, X, Y), zpad=Z - 1, **HYB)
+    dd = mm["dc"].Deconvolver(psf, (Z, X, Y), zpad=(Z - 1) // 2, **DAPI)
+    hd = dapi.cpu().pin_memory()
+    want_p, want_m, _, _ = mm["pl"].dapi_spots(dd, dapi.cuda(), None, **DAPI)
+    want_rows = [mm["pl"].hyb_spots(dh, c.cuda(), f, **HYB) for c, f in zip(cols, flats)]
+    runner = mm["pl"].FovRunner(dh, dd, HYB, DAPI)
+    ticket = runner.submit(hd, cols)
+    for _ in range(3):
+        nxt = runner.submit(hd, cols)
+        p, m, rows = runner.run(ticket, flats)
+        ticket = nxt
+        np.testing.assert_array_equal(ck.sort_rows(p), ck.sort_rows(want_p.cpu().numpy()))
+        np.testing.assert_array_equal(ck.sort_rows(m), ck.sort_rows(want_m.cpu().numpy()))
+        for got, want in zip(rows, want_rows):
+            np.testing.assert_array_equal(ck.sort_rows(got), ck.sort_rows(want.cpu().numpy()))
+    assert runner.h2d_bytes == 3 * Z * X * Y * 2
