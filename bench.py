@@ -16,6 +16,10 @@ A step is one FOV of the workload, inputs resident in HBM:
 * ``grid25``: one colour of 50 x 1000 x 1000 in 5 x 5 tiles of 200 (padded
   378): a 25-tile batch, like a colour of ``fov3c``, in a few GB.
 * ``tile``: one smFISH tile, uint16 40 x 500 x 500, 2,000 puncta, no flat field.
+* ``served``: a Poisson stream of ``--fovs`` FOV requests over four FOV shapes
+  (Z 30-60, XY 1024/2048, 1-3 colours + DAPI) through ``serve.FovServer``
+  (continuous batching under a 120 GB budget); reports stream voxels/s and
+  p50/p99 request latency.
 
 ``value`` is FOV input voxels per second (all channels) of the batched form
 (tiles of a colour in one batch, spots kept and offset on the device);
@@ -67,7 +71,10 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mermake_gb300", choices=["mermake_gb300", "reference"])
-    ap.add_argument("--workload", default="fov3c", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="fov3c", choices=sorted(WORKLOADS) + ["served"])
+    ap.add_argument("--fovs", type=int, default=16, help="served: number of FOV requests in the stream")
+    ap.add_argument("--interval", type=float, default=0.25, help="served: mean Poisson arrival interval (s)")
+    ap.add_argument("--workers", type=int, default=2, help="served: concurrent requests on the device")
     ap.add_argument("--form", default="batched", choices=["batched", "plain"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -477,11 +484,85 @@ def reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# served form: a Poisson stream of mixed-shape FOVs through serve.FovServer
+# ---------------------------------------------------------------------------
+SERVED_FOVS = [  # (Z, X, Y, colours) per FOV id, from the mixed-shape stream's ranges
+    (30, 1024, 1024, 1), (40, 2048, 2048, 3), (60, 1024, 1024, 2), (50, 2048, 2048, 3)]
+
+
+def served_arm(args, local):
+    import numpy as np
+    import torch
+
+    from mermake_gb300 import serve, synth
+    torch.cuda.set_device(local)
+    hyb = dict(WORKLOADS["fov3c"]["hyb"])
+    dap = dict(WORKLOADS["fov3c"]["dapi_args"])
+    psf = synth.gaussian_psf((40, 40, 40), 2.0, 1.3)
+    data = []
+    for f, (Z, X, Y, nc) in enumerate(SERVED_FOVS):
+        dapi = synth.dapi_stack(Z, X, Y, 500 + f, device="cuda", n_nuclei=max(20, 300 * X * Y // 2048 ** 2))
+        gain = synth.flat_gain(X, Y)
+        cols = [synth.hyb_stack(Z, X, Y, 40000 * X * Y // 2048 ** 2, 600 + 7 * f + c, device="cuda", gain=gain)
+                for c in range(nc)]
+        data.append(dict(dapi=dapi.cpu().pin_memory(), colours=[c.cpu().pin_memory() for c in cols],
+                         flats=[torch.from_numpy(gain).cuda() for _ in cols]))
+        del dapi, cols
+    rng = np.random.default_rng(7)
+    nf = len(SERVED_FOVS)
+    reqs = [dict(fov=i % nf, round=i // nf, **data[i % nf]) for i in range(args.fovs)]
+    vox = [sum(int(np.prod(a.shape)) for a in [r["dapi"]] + r["colours"]) for r in reqs]
+    gaps = rng.exponential(args.interval, size=len(reqs))
+    with ClockSampler(local) as clk:
+        with serve.FovServer(psf, hyb, dap, hbm_budget=120e9, workers=args.workers) as srv:
+            # warm-up: one request per shape builds the resident spectra (untimed)
+            for f in range(nf):
+                srv.submit(serve.FovRequest(fov=1000 + f, round=0, **data[f])).result()
+            srv.results.clear()
+            futs, t0 = [], time.perf_counter()
+            t = t0
+            for r, g in zip(reqs, gaps):
+                t += g
+                while time.perf_counter() < t:
+                    time.sleep(min(0.002, max(0.0, t - time.perf_counter())))
+                futs.append(srv.submit(serve.FovRequest(arrival=t, **r)))
+            res = [fu.result() for fu in futs]
+            t1 = max(x.done for x in res)
+            peak = srv.max_in_flight
+    lat = sorted(1e3 * x.latency for x in res)
+    line = {
+        "metric": "FOV voxels/s, served stream (Poisson arrivals, mixed Z/XY, continuous batching)",
+        "value": sum(vox) / (t1 - t0),
+        "unit": "voxels/s",
+        "n_gpus": 1,
+        "steps": len(reqs),
+        "warmup": nf,
+        "ms_per_step": 1e3 * (t1 - t0) / len(reqs),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded Poisson background + Gaussian puncta / nuclei), %d FOV shapes" % nf,
+        "config": {"workload": "served", "fovs": [list(f) for f in SERVED_FOVS], "requests": len(reqs),
+                   "mean_interval_s": args.interval, "workers": args.workers, "hbm_budget_gb": 120,
+                   "peak_in_flight": peak, "tile_size": hyb["tile_size"], "overlap": hyb["overlap"]},
+        "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": lat[-1]},
+        "drift_px": [float(np.abs(np.asarray(x.drift[0])).max()) for x in res if x.drift is not None][:8],
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
     if args.impl == "reference":
         reference_arm(args, rank, world)
+        return
+    if args.workload == "served":
+        if rank == 0:
+            served_arm(args, local)
         return
     gpu_arm(args, rank, world, local)
 

@@ -94,7 +94,8 @@ int mm_wiener_spectrum(mm_ctx *ctx, const float *psf, int pz, int px, int py, in
  * z, from which every entry of the Z x Z matrix of a frequency is a sum of at
  * most four samples.  Passing zop to mm_deconv_tiles / mm_hyb_spots /
  * mm_dapi_spots replaces the two padded-depth transforms of each tile by one
- * complex matrix product per frequency over the tiles of a batch.
+ * complex matrix product per frequency over the tiles of a batch (for batches
+ * of at least 10 tiles; smaller batches keep the transforms).
  * tile_height <= 64 and Zp <= 400, and no plane copied more than four times
  * by the z padding (MM_EINVAL otherwise). */
 int mm_wiener_zop(mm_ctx *ctx, const void *W, int tile_height, int zpad, int tile_size, int overlap, void *zop,

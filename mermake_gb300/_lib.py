@@ -18,7 +18,7 @@ MM_OK, MM_EINVAL, MM_ENOMEM, MM_EOVERFLOW, MM_ETIMEOUT, MM_EDEVICE = range(6)
 
 _lock = threading.Lock()
 _lib = None
-_ctx = {}
+_tls = threading.local()  # per-thread mm_ctx handles (ctx())
 
 
 class MermakeError(RuntimeError):
@@ -103,17 +103,31 @@ def lib():
 
 
 def ctx(device=None):
-    """The process-wide mm_ctx of a device (scratch owner)."""
+    """The calling thread's mm_ctx on a device (scratch owner).  The C ABI wants
+    one context per host thread, so threads that call in concurrently (the
+    serving workers) each get their own and run without waiting on a shared
+    one."""
     L = lib()
     dev = torch.cuda.current_device() if device is None else int(device)
-    with _lock:
-        c = _ctx.get(dev)
-        if c is None:
-            with torch.cuda.device(dev):
-                p = _vp()
-                check(L.mm_ctx_create(C.byref(p)))
-            c = _ctx[dev] = p
+    per = getattr(_tls, "ctx", None)
+    if per is None:
+        per = _tls.ctx = {}
+    c = per.get(dev)
+    if c is None:
+        with torch.cuda.device(dev):
+            p = _vp()
+            check(L.mm_ctx_create(C.byref(p)))
+        c = per[dev] = p
     return c
+
+
+def release_thread_ctx():
+    """Frees the calling thread's contexts (their scratch); a later call makes new ones."""
+    per = getattr(_tls, "ctx", None) or {}
+    for dev, c in list(per.items()):
+        with torch.cuda.device(dev):
+            check(lib().mm_ctx_destroy(c))
+    per.clear()
 
 
 def last_error():

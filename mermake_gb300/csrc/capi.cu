@@ -130,6 +130,7 @@ struct Small {
     double sumsq;
     float div;
     float pad_;
+    double parts[MM_SUM_PARTS];  // per-block partial sums (fixed-order reductions)
 };
 
 int small_get(mm_ctx *c, Small **out) {
@@ -202,7 +203,7 @@ int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *
         StageTimer t(c, ST_COLS_FWD, 2 * spec_b, st);
         if ((rc = mm_launch_cols(S, g.P, g.H, g.H, plane_c, g.nt * g.Z, false, st))) return rc;
     }
-    if (zop) {
+    if (zop && g.nt >= MM_ZOP_MIN_TILES) {
         // the z kernel (Zp per frequency, the size of W) is read once per batch
         StageTimer t(c, ST_ZPASS, 2 * spec_b + 8.0 * wstride, st);
         if ((rc = mm_launch_zop_apply(S, zop, g.Z, g.zpad, g.Zp, plane_c, g.nt, st))) return rc;
@@ -293,7 +294,7 @@ int mm_wiener_spectrum(mm_ctx *c, const float *psf, int pz, int px, int py, int 
     if ((rc = small_get(c, &sm))) return rc;
     StageTimer tm(c, ST_WIENER, 4.0 * nz * nx * nx + 8.0 * nz * nx * H, st);
     return mm_wiener_build_impl(psf, pz, px, py, tile_height, tile_size, zpad, overlap, beta, (float2 *)W,
-                                (float *)vol, (float2 *)spec, &sm->sumsq, st);
+                                (float *)vol, (float2 *)spec, &sm->sumsq, sm->parts, st);
 }
 
 int mm_wiener_zop(mm_ctx *c, const void *W, int tile_height, int zpad, int tile_size, int overlap, void *zop,
@@ -475,7 +476,7 @@ int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t
     }
     {
         StageTimer tm(c, ST_SUMSQ, 4.0 * N, st);
-        if ((rc = mm_launch_sumsq(buffer, N, &sm->sumsq, st))) return rc;
+        if ((rc = mm_launch_sumsq(buffer, N, sm->parts, &sm->sumsq, st))) return rc;
     }
     if ((rc = mm_launch_rms_div(&sm->sumsq, N, &sm->div, st))) return rc;
     for (int attempt = 0; attempt < 2; ++attempt) {

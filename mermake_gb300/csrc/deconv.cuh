@@ -118,6 +118,11 @@ int mm_launch_zpass(const TileGeom &g, float2 *S, const float2 *W, long long wst
 
 // z pass as a matrix per frequency (zop.cu), single spectrum only: the z
 // kernel w (Zp, P, P/2+1) is the inverse DFT of W along z.
+// The z operator's cost per launch is dominated by summing M (Z x Z per
+// frequency) and hardly depends on the batch; below this many tiles the
+// padded-depth transforms are cheaper (about 0.4 ms per 678 x 678 tile
+// against about 3.9 ms per launch at Z = 50).
+#define MM_ZOP_MIN_TILES 10
 #define MM_ZOP_MAX_Z 64
 #define MM_ZOP_MAX_ZP 400
 #define MM_ZOP_MAX_COPIES 4
@@ -156,8 +161,11 @@ int mm_maxima_ensure_init(cudaStream_t st);
 int mm_launch_maxima_fit(const MaximaArgs &a, uint2 *cand, unsigned cand_cap, unsigned *ncand, float *out,
                          unsigned out_cap, unsigned *out_count, int zero_out_count, cudaStream_t st);
 int mm_launch_note_overflow(const unsigned *ncand, unsigned cap, unsigned *overflow, cudaStream_t st);
-int mm_launch_sumsq(const float *x, long long n, double *out, cudaStream_t st);
+// largest number of per-block partial sums (grid cap of the elementwise kernels)
+#define MM_SUM_PARTS 4864
+int mm_launch_sumsq(const float *x, long long n, double *parts, double *out, cudaStream_t st);
+int mm_launch_sum_parts(const double *parts, int nparts, double *out, cudaStream_t st);
 int mm_launch_rms_div(const double *sumsq, long long n, float *div, cudaStream_t st);
 int mm_wiener_build_impl(const float *psf, int pz, int px, int py, int tile_height, int tile_size, int zpad,
-                         int overlap, float beta, float2 *W, float *vol, float2 *S, double *dsum,
+                         int overlap, float beta, float2 *W, float *vol, float2 *S, double *dsum, double *parts,
                          cudaStream_t st);

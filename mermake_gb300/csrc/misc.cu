@@ -78,21 +78,23 @@ __global__ void k_subtract_u16(const uint16_t *__restrict__ x, const uint16_t *_
     }
 }
 
-__global__ void k_sumsq(const float *__restrict__ x, long long n, double *__restrict__ out) {
+// Sums of squares in a fixed order (the result does not depend on block
+// timing): each block writes its partial sum, k_sum_parts adds the partials.
+__global__ void k_sumsq(const float *__restrict__ x, long long n, double *__restrict__ parts) {
     double acc = 0.0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         double v = x[i];
         acc += v * v;
     }
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    __shared__ double part[32];
-    if ((threadIdx.x & 31) == 0) part[threadIdx.x / 32] = acc;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-        acc = threadIdx.x < blockDim.x / 32 ? part[threadIdx.x] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-        if (threadIdx.x == 0) atomicAdd(out, acc);
-    }
+    acc = mm_block_sum(acc);
+    if (threadIdx.x == 0) parts[blockIdx.x] = acc;
+}
+
+__global__ void k_sum_parts(const double *__restrict__ parts, int nparts, double *__restrict__ out) {
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < nparts; i += blockDim.x) acc += parts[i];
+    acc = mm_block_sum(acc);
+    if (threadIdx.x == 0) out[0] = acc;
 }
 
 // DAPI divisor (__main__.py:221-222): norm = sqrt of the sum of squares rounded
@@ -172,12 +174,21 @@ extern "C" int mm_subtract_u16(const uint16_t *x, const int64_t *xs, const uint1
     return MM_OK;
 }
 
-int mm_launch_sumsq(const float *x, long long n, double *out, cudaStream_t st) {
-    MM_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double), st));
-    if (n == 0) return MM_OK;
-    k_sumsq<<<grid_for(n), 256, 0, st>>>(x, n, out);
+int mm_launch_sum_parts(const double *parts, int nparts, double *out, cudaStream_t st) {
+    k_sum_parts<<<1, 256, 0, st>>>(parts, nparts, out);
     MM_CHECK_LAUNCH();
     return MM_OK;
+}
+
+int mm_launch_sumsq(const float *x, long long n, double *parts, double *out, cudaStream_t st) {
+    if (n == 0) {
+        MM_CUDA_TRY(cudaMemsetAsync(out, 0, sizeof(double), st));
+        return MM_OK;
+    }
+    const int g = grid_for(n);
+    k_sumsq<<<g, 256, 0, st>>>(x, n, parts);
+    MM_CHECK_LAUNCH();
+    return mm_launch_sum_parts(parts, g, out, st);
 }
 
 int mm_launch_rms_div(const double *sumsq, long long n, float *div, cudaStream_t st) {

@@ -53,3 +53,21 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
 }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 __device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+
+// Block-wide sum of one double per thread in a fixed order (warp shuffles,
+// then the warps' sums by warp 0): thread 0 gets the total.  All threads of
+// the block must call it; blockDim.x is a multiple of 32, at most 1024.
+#ifdef __CUDACC__
+__device__ __forceinline__ double mm_block_sum(double v) {
+    __shared__ double part[32];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+    __syncthreads();
+    v = 0.0;
+    if (threadIdx.x < 32) {
+        v = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    }
+    return v;
+}
+#endif

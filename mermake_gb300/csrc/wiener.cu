@@ -39,7 +39,7 @@ __device__ inline int unroll_pad(int i, int n, int pad, int T, int S) {
 }
 
 __global__ void k_psf_place(PsfGeom g, const float *__restrict__ psf, float *__restrict__ vol,
-                            double *__restrict__ sum) {
+                            double *__restrict__ parts) {
     const long long total = (long long)g.nz * g.nx * g.ny;
     double acc = 0.0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total;
@@ -55,8 +55,9 @@ __global__ void k_psf_place(PsfGeom g, const float *__restrict__ psf, float *__r
         vol[i] = v;
         acc += (double)v;
     }
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(sum, acc);
+    // the PSF sum in a fixed order (k_sum_parts adds the block partials)
+    acc = mm_block_sum(acc);
+    if (threadIdx.x == 0) parts[blockIdx.x] = acc;
 }
 
 __global__ void k_wiener(const float2 *__restrict__ Hs, int nz, int nx, int hy, int ny, float beta,
@@ -83,7 +84,7 @@ __global__ void k_wiener(const float2 *__restrict__ Hs, int nz, int nx, int hy, 
 }  // namespace
 
 int mm_wiener_build_impl(const float *psf, int pz, int px, int py, int tile_height, int tile_size, int zpad,
-                         int overlap, float beta, float2 *W, float *vol, float2 *S, double *dsum,
+                         int overlap, float beta, float2 *W, float *vol, float2 *S, double *dsum, double *parts,
                          cudaStream_t st) {
     PsfGeom g;
     g.pz = pz; g.px = px; g.py = py;
@@ -93,10 +94,10 @@ int mm_wiener_build_impl(const float *psf, int pz, int px, int py, int tile_heig
     g.nx = tile_size + 2 * overlap;
     g.ny = g.nx;
     const int H = g.ny / 2 + 1;
-    MM_CUDA_TRY(cudaMemsetAsync(dsum, 0, sizeof(double), st));
-    k_psf_place<<<608, 256, 0, st>>>(g, psf, vol, dsum);
+    k_psf_place<<<608, 256, 0, st>>>(g, psf, vol, parts);
     MM_CHECK_LAUNCH();
     int rc;
+    if ((rc = mm_launch_sum_parts(parts, 608, dsum, st))) return rc;
     if ((rc = mm_launch_rows_fwd_f32(vol, g.nz * g.nx, g.ny, S, st))) return rc;
     if ((rc = mm_launch_cols(S, g.nx, H, H, (long long)g.nx * H, g.nz, false, st))) return rc;
     if ((rc = mm_launch_zfwd(S, g.nz, g.nx * H, st))) return rc;
