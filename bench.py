@@ -531,6 +531,8 @@ def served_arm(args, local):
             t1 = max(x.done for x in res)
             peak = srv.max_in_flight
     lat = sorted(1e3 * x.latency for x in res)
+    svc = sorted(1e3 * (x.done - x.admitted) for x in res)
+    que = sorted(1e3 * (x.admitted - x.request.arrival) for x in res)
     line = {
         "metric": "FOV voxels/s, served stream (Poisson arrivals, mixed Z/XY, continuous batching)",
         "value": sum(vox) / (t1 - t0),
@@ -548,6 +550,10 @@ def served_arm(args, local):
                    "mean_interval_s": args.interval, "workers": args.workers, "hbm_budget_gb": 120,
                    "peak_in_flight": peak, "tile_size": hyb["tile_size"], "overlap": hyb["overlap"]},
         "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": lat[-1]},
+        "service_ms": {"p50": pct(svc, 50), "p99": pct(svc, 99)},
+        "queue_ms": {"p50": pct(que, 50), "p99": pct(que, 99)},
+        "per_shape_service_ms": {str(list(SERVED_FOVS[f][:3])): round(statistics.median(
+            1e3 * (x.done - x.admitted) for x in res if x.request.fov == f), 1) for f in range(nf)},
         "drift_px": [float(np.abs(np.asarray(x.drift[0])).max()) for x in res if x.drift is not None][:8],
         "clocks": clk.summary(),
     }

@@ -20,6 +20,10 @@
 #include <math.h>
 #include <string.h>
 
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
 #include "deconv.cuh"
 
 // per-aligner scratch for the moving sets, grown on demand
@@ -34,6 +38,20 @@ struct MmDriftWork {
     int *h_small = nullptr;
 };
 
+// Uniform cell grid of the reference points for the nearest-neighbour
+// refinement: cells of edge cs >= the largest match radius, so every point
+// within the radius of a query lies in the query's cell or its neighbours.
+struct MmCellGrid {
+    int dims[3] = {0, 0, 0};
+    float lo[3] = {0, 0, 0};
+    float cs = 0;
+    int *start = nullptr;     // device, cells + 1: first sorted point of each cell
+    float *pts = nullptr;     // device, n x 3: points sorted by cell (index order within a cell)
+    int *idx = nullptr;       // device, n: original index of each sorted point
+    double *state = nullptr;  // device: shift (3), integer-shift flag, matched count
+    double *parts = nullptr;  // device: per-block partial sums of a refinement round
+};
+
 struct mm_aligner {
     int n;            // reference points kept by the threshold
     float *pts;       // device, n x 3
@@ -43,6 +61,7 @@ struct mm_aligner {
     int resc, trim;
     float th;         // NaN: no threshold
     MmDriftWork w;
+    MmCellGrid cg;
 };
 
 namespace {
@@ -174,89 +193,108 @@ __global__ void k_argmax(const int *__restrict__ hist, long long total, unsigned
 // five nearest-neighbour refinements in one CTA (align.py:61-77).  t0: the
 // coarse shift (integer, times resc).  out: tzxy (3 floats) and the count of
 // the last round.
-__global__ void k_refine(const float *__restrict__ X, const int *__restrict__ n_p, const float *__restrict__ R,
-                         int nr, const unsigned long long *__restrict__ best, int o1, int o2, int sb0, int sb1,
-                         int sb2, int resc, float target, float *__restrict__ out, int *__restrict__ npts) {
-    __shared__ double acc[4][32];
-    __shared__ double tz[3];
-    __shared__ int tint;  // 1 while the shift is still the integer coarse one
+// Nearest-neighbour refinement (align.py:55-76, five rounds with radii
+// np.linspace(resc, target, 5)), one round per launch over many CTAs.  Each
+// moving point X - shift looks for its nearest reference point among the
+// cells around it (distance in double, ties to the lower reference index:
+// the point a brute-force search over all references would pick); if it lies
+// within the round's radius, X - R (float32) is added in double.  Blocks
+// write partial sums that k_refine_update adds in a fixed order.
+constexpr int kRefineThreads = 256;
+constexpr int kRefineMaxBlocks = 304;
+
+__global__ void k_refine_init(const unsigned long long *__restrict__ best, int o1, int o2, int sb0, int sb1,
+                              int sb2, int resc, double *__restrict__ state) {
+    const unsigned long long b = *best;
+    const long long idx = (long long)(~(unsigned)(b & 0xffffffffu));
+    const long long z = idx / ((long long)o1 * o2), x = (idx / o2) % o1, y = idx % o2;
+    state[0] = (double)((z - sb0 + 1) * resc);
+    state[1] = (double)((x - sb1 + 1) * resc);
+    state[2] = (double)((y - sb2 + 1) * resc);
+    state[3] = 1.0;  // the shift is still the integer coarse one
+    state[4] = 0.0;
+}
+
+__global__ void __launch_bounds__(kRefineThreads)
+k_refine_round(const float *__restrict__ X, const int *__restrict__ n_p, const float *__restrict__ gp,
+               const int *__restrict__ gidx, const int *__restrict__ gstart, int gd0, int gd1, int gd2, float lo0,
+               float lo1, float lo2, float cs, int reach, double dist_th, const double *__restrict__ state,
+               double *__restrict__ parts) {
     const int n = *n_p;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (threadIdx.x == 0) {
-        const unsigned long long b = *best;
-        const long long idx = (long long)(~(unsigned)(b & 0xffffffffu));
-        const long long z = idx / ((long long)o1 * o2), x = (idx / o2) % o1, y = idx % o2;
-        tz[0] = (double)((z - sb0 + 1) * resc);
-        tz[1] = (double)((x - sb1 + 1) * resc);
-        tz[2] = (double)((y - sb2 + 1) * resc);
-        tint = 1;
-    }
-    __syncthreads();
-    int kept_last = 0;
-    for (int it = 0; it < 5; ++it) {
-        // np.linspace(resc, target, 5)
-        const double dist_th = (double)resc + (double)it * (((double)target - (double)resc) / 4.0);
-        double sz = 0, sx = 0, sy = 0, cnt = 0;
-        const float t0 = (float)tz[0], t1 = (float)tz[1], t2 = (float)tz[2];
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            // XT = X - tzxy: float64 against the integer coarse shift, float32 after
-            double q0, q1, q2;
-            if (tint) {
-                q0 = (double)X[i * 3] - tz[0];
-                q1 = (double)X[i * 3 + 1] - tz[1];
-                q2 = (double)X[i * 3 + 2] - tz[2];
-            } else {
-                q0 = (double)(X[i * 3] - t0);
-                q1 = (double)(X[i * 3 + 1] - t1);
-                q2 = (double)(X[i * 3 + 2] - t2);
-            }
-            double bd = 1e300;
-            int bj = 0;
-            for (int j = 0; j < nr; ++j) {
-                const double d0 = q0 - R[j * 3], d1 = q1 - R[j * 3 + 1], d2 = q2 - R[j * 3 + 2];
-                const double d = d0 * d0 + d1 * d1 + d2 * d2;
-                if (d < bd) {
-                    bd = d;
-                    bj = j;
+    const bool tint = state[3] != 0.0;
+    const double tz0 = state[0], tz1 = state[1], tz2 = state[2];
+    const float t0 = (float)tz0, t1 = (float)tz1, t2 = (float)tz2;
+    double sz = 0, sx = 0, sy = 0, cnt = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        // XT = X - tzxy: float64 against the integer coarse shift, float32 after
+        double q0, q1, q2;
+        if (tint) {
+            q0 = (double)X[i * 3] - tz0;
+            q1 = (double)X[i * 3 + 1] - tz1;
+            q2 = (double)X[i * 3 + 2] - tz2;
+        } else {
+            q0 = (double)(X[i * 3] - t0);
+            q1 = (double)(X[i * 3 + 1] - t1);
+            q2 = (double)(X[i * 3 + 2] - t2);
+        }
+        const int c0 = (int)floor((q0 - lo0) / cs), c1 = (int)floor((q1 - lo1) / cs), c2 = (int)floor((q2 - lo2) / cs);
+        double bd = 1e300;
+        int bj = 0x7fffffff, bk = -1;
+        for (int a = max(c0 - reach, 0); a <= min(c0 + reach, gd0 - 1); ++a)
+            for (int b = max(c1 - reach, 0); b <= min(c1 + reach, gd1 - 1); ++b) {
+                const int lc = max(c2 - reach, 0), hc = min(c2 + reach, gd2 - 1);
+                if (lc > hc) continue;
+                const long long row = ((long long)a * gd1 + b) * gd2;
+                const int e0 = gstart[row + lc], e1 = gstart[row + hc + 1];
+                for (int k = e0; k < e1; ++k) {
+                    const double d0 = q0 - gp[k * 3], d1 = q1 - gp[k * 3 + 1], d2 = q2 - gp[k * 3 + 2];
+                    const double d = d0 * d0 + d1 * d1 + d2 * d2;
+                    const int j = gidx[k];
+                    if (d < bd || (d == bd && j < bj)) {
+                        bd = d;
+                        bj = j;
+                        bk = k;
+                    }
                 }
             }
-            if (sqrt(bd) < dist_th) {
-                // X_ - X_ref_ in float32, summed in double
-                sz += (double)(X[i * 3] - R[bj * 3]);
-                sx += (double)(X[i * 3 + 1] - R[bj * 3 + 1]);
-                sy += (double)(X[i * 3 + 2] - R[bj * 3 + 2]);
-                cnt += 1;
-            }
+        if (bk >= 0 && sqrt(bd) < dist_th) {
+            // X_ - X_ref_ in float32, summed in double
+            sz += (double)(X[i * 3] - gp[bk * 3]);
+            sx += (double)(X[i * 3 + 1] - gp[bk * 3 + 1]);
+            sy += (double)(X[i * 3 + 2] - gp[bk * 3 + 2]);
+            cnt += 1;
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            sz += __shfl_xor_sync(0xffffffffu, sz, o);
-            sx += __shfl_xor_sync(0xffffffffu, sx, o);
-            sy += __shfl_xor_sync(0xffffffffu, sy, o);
-            cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
-        }
-        if (lane == 0) {
-            acc[0][warp] = sz;
-            acc[1][warp] = sx;
-            acc[2][warp] = sy;
-            acc[3][warp] = cnt;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double s[4] = {0, 0, 0, 0};
-            for (int w = 0; w < nw; ++w)
-                for (int k = 0; k < 4; ++k) s[k] += acc[k][w];
-            kept_last = (int)s[3];
-            if (s[3] > 0) {  // else: no point kept, the shift stays (align.py:72-74)
-                for (int k = 0; k < 3; ++k) tz[k] = (double)(float)(s[k] / s[3]);
-                tint = 0;
-            }
-        }
-        __syncthreads();
     }
+    sz = mm_block_sum(sz);
+    __syncthreads();
+    sx = mm_block_sum(sx);
+    __syncthreads();
+    sy = mm_block_sum(sy);
+    __syncthreads();
+    cnt = mm_block_sum(cnt);
     if (threadIdx.x == 0) {
-        for (int k = 0; k < 3; ++k) out[k] = (float)tz[k];
-        npts[0] = kept_last;
-        npts[1] = tint;
+        parts[blockIdx.x * 4 + 0] = sz;
+        parts[blockIdx.x * 4 + 1] = sx;
+        parts[blockIdx.x * 4 + 2] = sy;
+        parts[blockIdx.x * 4 + 3] = cnt;
+    }
+}
+
+__global__ void k_refine_update(const double *__restrict__ parts, int nblocks, double *__restrict__ state,
+                                int last, float *__restrict__ out, int *__restrict__ npts) {
+    if (threadIdx.x != 0) return;
+    double s[4] = {0, 0, 0, 0};
+    for (int b = 0; b < nblocks; ++b)
+        for (int k = 0; k < 4; ++k) s[k] += parts[b * 4 + k];
+    state[4] = s[3];
+    if (s[3] > 0) {  // else: no point kept, the shift stays (align.py:72-74)
+        for (int k = 0; k < 3; ++k) state[k] = (double)(float)(s[k] / s[3]);
+        state[3] = 0.0;
+    }
+    if (last) {
+        for (int k = 0; k < 3; ++k) out[k] = (float)state[k];
+        npts[0] = (int)state[4];
+        npts[1] = (int)state[3];
     }
 }
 
@@ -337,6 +375,66 @@ void work_free(MmDriftWork &w) {
 // small-buffer slots (ints) inside Work::small
 enum { SM_N = 0, SM_MM = 1, SM_KMAX = 8, SM_NVOX = 12, SM_NPTS = 14, SM_BEST = 16, SM_OUT = 20 };
 
+// The cell grid of the reference points (host-side counting sort, points in
+// index order within a cell), and the refinement's small device state.
+int cell_grid_build(MmCellGrid &g, const float *pts_dev, int n, float cs_min, cudaStream_t st) {
+    std::vector<float> p((size_t)n * 3);
+    MM_CUDA_TRY(cudaMemcpyAsync(p.data(), pts_dev, sizeof(float) * 3 * n, cudaMemcpyDeviceToHost, st));
+    MM_CUDA_TRY(cudaStreamSynchronize(st));
+    float lo[3], hi[3];
+    for (int c = 0; c < 3; ++c) lo[c] = hi[c] = p[c];
+    for (int i = 0; i < n; ++i)
+        for (int c = 0; c < 3; ++c) {
+            lo[c] = std::min(lo[c], p[i * 3 + c]);
+            hi[c] = std::max(hi[c], p[i * 3 + c]);
+        }
+    // cells of edge >= cs_min, coarser if the box would need more than 2^24 cells
+    double cs = cs_min;
+    for (;;) {
+        double cells = 1;
+        for (int c = 0; c < 3; ++c) cells *= std::floor((hi[c] - lo[c]) / cs) + 1;
+        if (cells <= (double)(1 << 24)) break;
+        cs *= 1.5;
+    }
+    g.cs = (float)cs;
+    for (int c = 0; c < 3; ++c) {
+        g.lo[c] = lo[c];
+        g.dims[c] = (int)std::floor((hi[c] - lo[c]) / g.cs) + 1;
+    }
+    const long long ncell = (long long)g.dims[0] * g.dims[1] * g.dims[2];
+    std::vector<int> cell(n), start(ncell + 1, 0), idx(n);
+    for (int i = 0; i < n; ++i) {
+        int k[3];
+        for (int c = 0; c < 3; ++c)
+            k[c] = std::min(g.dims[c] - 1, std::max(0, (int)std::floor(((double)p[i * 3 + c] - g.lo[c]) / g.cs)));
+        cell[i] = (int)(((long long)k[0] * g.dims[1] + k[1]) * g.dims[2] + k[2]);
+        start[cell[i] + 1]++;
+    }
+    for (long long c = 0; c < ncell; ++c) start[c + 1] += start[c];
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    std::vector<float> sp((size_t)n * 3);
+    for (int i = 0; i < n; ++i) {
+        const int at = fill[cell[i]]++;
+        idx[at] = i;
+        for (int c = 0; c < 3; ++c) sp[at * 3 + c] = p[i * 3 + c];
+    }
+    MM_CUDA_TRY(cudaMalloc(&g.start, sizeof(int) * (ncell + 1)));
+    MM_CUDA_TRY(cudaMalloc(&g.pts, sizeof(float) * 3 * n));
+    MM_CUDA_TRY(cudaMalloc(&g.idx, sizeof(int) * n));
+    MM_CUDA_TRY(cudaMalloc(&g.state, sizeof(double) * 8));
+    MM_CUDA_TRY(cudaMalloc(&g.parts, sizeof(double) * 4 * kRefineMaxBlocks));
+    MM_CUDA_TRY(cudaMemcpyAsync(g.start, start.data(), sizeof(int) * (ncell + 1), cudaMemcpyHostToDevice, st));
+    MM_CUDA_TRY(cudaMemcpyAsync(g.pts, sp.data(), sizeof(float) * 3 * n, cudaMemcpyHostToDevice, st));
+    MM_CUDA_TRY(cudaMemcpyAsync(g.idx, idx.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st));
+    MM_CUDA_TRY(cudaStreamSynchronize(st));
+    return MM_OK;
+}
+
+void cell_grid_free(MmCellGrid &g) {
+    cudaFree(g.start); cudaFree(g.pts); cudaFree(g.idx); cudaFree(g.state); cudaFree(g.parts);
+    g = MmCellGrid();
+}
+
 }  // namespace
 
 extern "C" int mm_aligner_create(const float *X_ref, int n, int cols, int64_t ld, float th, int resc, int trim,
@@ -392,6 +490,10 @@ extern "C" int mm_aligner_create(const float *X_ref, int n, int cols, int64_t ld
     cudaMemcpyAsync(S->pts, w.pts, sizeof(float) * 3 * nkeep, cudaMemcpyDeviceToDevice, st);
     if (sp.nvox) cudaMemcpyAsync(S->vox, w.vox, sizeof(int) * 3 * sp.nvox, cudaMemcpyDeviceToDevice, st);
     MM_CUDA_TRY(cudaStreamSynchronize(st));
+    if ((rc = cell_grid_build(S->cg, S->pts, nkeep, (float)resc, st))) {
+        cell_grid_free(S->cg); cudaFree(S->pts); cudaFree(S->vox); work_free(w); delete S;
+        return rc;
+    }
     *out = S;
     return MM_OK;
 }
@@ -402,6 +504,7 @@ extern "C" int mm_aligner_destroy(mm_aligner *S) {
     cudaFree(S->pts);
     cudaFree(S->vox);
     work_free(S->w);
+    cell_grid_free(S->cg);
     delete S;
     return MM_OK;
 }
@@ -466,9 +569,24 @@ extern "C" int mm_aligner_translation(mm_aligner *S, const float *X, int n, int 
     k_argmax<<<ga, 256, 0, st>>>(w.hist, (long long)total, best);
     MM_CHECK_LAUNCH();
     float *outp = reinterpret_cast<float *>(w.small + SM_OUT);
-    k_refine<<<1, 1024, 0, st>>>(w.pts, w.small + SM_N, A.pts, A.n, best, o1, o2, A.shape[0], A.shape[1],
-                                 A.shape[2], A.resc, target, outp, w.small + SM_NPTS);
+    const MmCellGrid &G = A.cg;
+    k_refine_init<<<1, 1, 0, st>>>(best, o1, o2, A.shape[0], A.shape[1], A.shape[2], A.resc, G.state);
     MM_CHECK_LAUNCH();
+    // radius in cells: the largest match radius over the rounds
+    const double rmax = std::max((double)A.resc, (double)target);
+    const int reach = (int)std::ceil(rmax / G.cs);
+    int nb = (nm + kRefineThreads - 1) / kRefineThreads;
+    nb = std::max(1, std::min(nb, kRefineMaxBlocks));
+    for (int it = 0; it < 5; ++it) {
+        // np.linspace(resc, target, 5)
+        const double dist_th = (double)A.resc + (double)it * (((double)target - (double)A.resc) / 4.0);
+        k_refine_round<<<nb, kRefineThreads, 0, st>>>(w.pts, w.small + SM_N, G.pts, G.idx, G.start, G.dims[0],
+                                                      G.dims[1], G.dims[2], G.lo[0], G.lo[1], G.lo[2], G.cs, reach,
+                                                      dist_th, G.state, G.parts);
+        MM_CHECK_LAUNCH();
+        k_refine_update<<<1, 32, 0, st>>>(G.parts, nb, G.state, it == 4, outp, w.small + SM_NPTS);
+        MM_CHECK_LAUNCH();
+    }
     MM_CUDA_TRY(cudaMemcpyAsync(w.h_small, outp, sizeof(float) * 3, cudaMemcpyDeviceToHost, st));
     MM_CUDA_TRY(cudaMemcpyAsync(w.h_small + 4, w.small + SM_NPTS, sizeof(int) * 2, cudaMemcpyDeviceToHost, st));
     MM_CUDA_TRY(cudaStreamSynchronize(st));

@@ -76,3 +76,21 @@ def test_dual_aligner_and_no_points(al, feats):
     assert got[3:] == want[3:]
     with pytest.raises(ValueError, match="No points left"):
         al.Aligner(torch.zeros((5, 3), device="cuda"), th=4)
+
+
+@pytest.mark.parametrize("npts,shift", [(6000, (2.0, -13.4, 7.7)), (20000, (-1.2, 4.9, -18.6))])
+def test_translation_many_points_matches_oracle(al, npts, shift):
+    """A field-sized point set (the DAPI maxima of a 50 x 2048 x 2048 FOV are
+    thousands): the cell-grid nearest-neighbour refinement spread over many
+    blocks gives the oracle's shift and match count."""
+    rng = np.random.default_rng(npts)
+    ref = np.stack([rng.uniform(0, 50, npts), rng.uniform(0, 2048, npts), rng.uniform(0, 2048, npts)],
+                   axis=1).astype(np.float32)
+    mov = shifted(np.concatenate([ref, np.full((npts, 1), 10, np.float32)], axis=1), shift, seed=3)[:, :3]
+    g = al.Aligner(torch.from_numpy(ref).cuda(), th=None)
+    o = oalign.Aligner(ref, th=None)
+    tg, ng = g.get_best_translation_points(torch.from_numpy(np.ascontiguousarray(mov)).cuda(), return_counts=True)
+    to, no = o.get_best_translation_points(np.ascontiguousarray(mov), return_counts=True)
+    assert ng == no
+    np.testing.assert_allclose(tg, to, atol=0.01)
+    np.testing.assert_allclose(tg, shift, atol=0.5)
