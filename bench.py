@@ -20,6 +20,10 @@ A step is one FOV of the workload, inputs resident in HBM:
   (Z 30-60, XY 1024/2048, 1-3 colours + DAPI) through ``serve.FovServer``
   (continuous batching under a 120 GB budget); reports stream voxels/s and
   p50/p99 request latency.
+* ``drift16``: 16 DAPI rounds of one 50 x 2048 x 2048 field drifted by known
+  shifts (+-3 z, +-20 x/y, sub-pixel), each deconvolved, spot-called and
+  aligned against round 0's resident maxima; reports rounds/s and the error
+  against the known shifts.
 
 ``value`` is FOV input voxels per second (all channels) of the batched form
 (tiles of a colour in one batch, spots kept and offset on the device);
@@ -71,7 +75,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mermake_gb300", choices=["mermake_gb300", "reference"])
-    ap.add_argument("--workload", default="fov3c", choices=sorted(WORKLOADS) + ["served"])
+    ap.add_argument("--workload", default="fov3c", choices=sorted(WORKLOADS) + ["served", "drift16"])
     ap.add_argument("--fovs", type=int, default=16, help="served: number of FOV requests in the stream")
     ap.add_argument("--interval", type=float, default=0.25, help="served: mean Poisson arrival interval (s)")
     ap.add_argument("--workers", type=int, default=2, help="served: concurrent requests on the device")
@@ -560,6 +564,62 @@ def served_arm(args, local):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# drift: 16 DAPI rounds of one FOV with known drifts against round 0
+# ---------------------------------------------------------------------------
+def drift_arm(args, local):
+    import types
+
+    import numpy as np
+    import torch
+
+    from mermake_gb300 import align, deconvolver, pipeline, synth
+    torch.cuda.set_device(local)
+    Z, X, Y = 50, 2048, 2048
+    dap = dict(WORKLOADS["fov3c"]["dapi_args"])
+    psf = synth.gaussian_psf((40, 40, 40), 2.0, 1.3)
+    dec = deconvolver.Deconvolver(psf, (Z, X, Y), zpad=(Z - 1) // 2, **dap)
+    rng = np.random.default_rng(11)
+    shifts = [(0.0, 0.0, 0.0)] + [(rng.uniform(-3, 3), rng.uniform(-20, 20), rng.uniform(-20, 20))
+                                  for _ in range(15)]
+    rounds = [synth.dapi_stack(Z, X, Y, 900, device="cuda", offset=s, noise_seed=900 + r).cpu().pin_memory()
+              for r, s in enumerate(shifts)]
+    buf = [None]
+
+    def maxima(h):
+        p, m, buf[0], _ = pipeline.dapi_spots(dec, h.to("cuda", non_blocking=True), None, buffer=buf[0], **dap)
+        return types.SimpleNamespace(Xh_plus=p, Xh_minus=m)
+
+    ref = maxima(rounds[0])
+    dual = align.DualAligner(ref, th=4)  # round 0's maxima stay on the device
+    for r in range(1, 4):  # warm-up
+        dual.get_best_translation_pointsV2(maxima(rounds[r]))
+    torch.cuda.synchronize()
+    errs, times = [], []
+    with ClockSampler(local) as clk:
+        for r in range(1, len(rounds)):
+            t0 = time.perf_counter()
+            tz = dual.get_best_translation_pointsV2(maxima(rounds[r]))[0]
+            times.append(1e3 * (time.perf_counter() - t0))
+            errs.append(np.asarray(tz, np.float64) + np.asarray(shifts[r]))
+    errs = np.abs(np.array(errs))
+    line = {
+        "metric": "drift rounds/s (DAPI deconvolution + maxima + drift against round 0)",
+        "value": 1e3 * len(times) / sum(times),
+        "unit": "rounds/s",
+        "n_gpus": 1, "steps": len(times), "warmup": 3,
+        "ms_per_step": sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic DAPI field of 300 nuclei, drifted by known shifts (+-3 z, +-20 x/y, sub-pixel)",
+        "config": {"workload": "drift16", "Z": Z, "X": X, "Y": Y, "rounds": len(rounds), "reference": "round 0"},
+        "drift_error_px": {"max_z": float(errs[:, 0].max()), "max_x": float(errs[:, 1].max()),
+                           "max_y": float(errs[:, 2].max()), "mean": float(errs.mean())},
+        "latency_ms": {"p50": pct(sorted(times), 50), "p99": pct(sorted(times), 99)},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -569,6 +629,10 @@ def main():
     if args.workload == "served":
         if rank == 0:
             served_arm(args, local)
+        return
+    if args.workload == "drift16":
+        if rank == 0:
+            drift_arm(args, local)
         return
     gpu_arm(args, rank, world, local)
 

@@ -21,7 +21,7 @@ struct TileDesc {
     int x0, y0;      // first input row / column (max(x - ov, 0))
     int xd, yd;      // input extent
     int xs, ys;      // placement offset inside the padded tile (ov on the first row/col)
-    int xend, yend;  // yielded extent (deconvolver.py:120-144)
+    int xend, yend;  // yielded extent (deconvolver.py:120-144), at most P
     int psf;         // spectrum index
 };
 
@@ -38,8 +38,12 @@ __device__ __host__ inline TileDesc mm_tile_desc(const TileGeom &g, int ti) {
     d.yd = y1 - d.y0;
     d.xs = d.x == 0 ? g.ov : 0;
     d.ys = d.y == 0 ? g.ov : 0;
+    // the yielded view tile_res[:, :xend, :yend] of a P x P tile: slicing
+    // clips xend = xd + ov at P when xd > P - ov (deconvolver.py:133-144, 170)
     d.xend = d.xd + ((d.x == 0 || d.xd < g.P) ? g.ov : 0);
     d.yend = d.yd + ((d.y == 0 || d.yd < g.P) ? g.ov : 0);
+    if (d.xend > g.P) d.xend = g.P;
+    if (d.yend > g.P) d.yend = g.P;
     d.psf = g.npsf == 1 ? 0 : ti;
     return d;
 }

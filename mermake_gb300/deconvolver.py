@@ -146,7 +146,8 @@ class Deconvolver:
         xd, yd = x1 - x0, y1 - y0
         xend = xd + (self.overlap if (x == 0 or xd < self.P) else 0)
         yend = yd + (self.overlap if (y == 0 or yd < self.P) else 0)
-        return xend, yend
+        # the reference's tile_res[:, :xend, :yend] clips at the padded size
+        return min(xend, self.P), min(yend, self.P)
 
     def n_tiles(self, shape):
         n = len(self.tile_boxes(shape))

@@ -70,13 +70,19 @@ def hyb_stack(Z, X, Y, n_puncta, seed, device="cpu", sigma_z=1.0, sigma_xy=1.5, 
     return torch.clamp(torch.round(vol), 0, 65535).to(torch.int32).to(torch.uint16)
 
 
-def dapi_stack(Z, X, Y, seed, device="cpu", n_nuclei=300, radii=(4.0, 25.0, 25.0), value=3000.0):
-    """uint16 (Z, X, Y) nuclei-like channel."""
+def dapi_stack(Z, X, Y, seed, device="cpu", n_nuclei=300, radii=(4.0, 25.0, 25.0), value=3000.0,
+               offset=(0.0, 0.0, 0.0), noise_seed=None):
+    """uint16 (Z, X, Y) nuclei-like channel.  ``offset`` moves every nucleus
+    centre by (dz, dx, dy) before it is rounded to the grid (a drifted round of
+    the same field); ``noise_seed`` draws the Poisson background independently
+    of the nuclei (default: ``seed``)."""
     dev = torch.device(device)
-    g = _gen(seed, dev)
+    g = _gen(seed if noise_seed is None else noise_seed, dev)
     vol = torch.poisson(torch.full((Z, X, Y), 600.0, device=dev), generator=g)
-    cen = torch.rand((n_nuclei, 3), generator=g, device=dev) * torch.tensor([Z, X, Y], device=dev,
-                                                                             dtype=torch.float32)
+    gc = _gen(seed + 7919, dev)
+    cen = torch.rand((n_nuclei, 3), generator=gc, device=dev) * torch.tensor([Z, X, Y], device=dev,
+                                                                              dtype=torch.float32)
+    cen = cen + torch.tensor(offset, device=dev, dtype=torch.float32)
     rz, rx, ry = radii
     oz = torch.arange(-int(rz), int(rz) + 1, device=dev)
     ox = torch.arange(-int(rx), int(rx) + 1, device=dev)

@@ -47,8 +47,11 @@ def plain_loop(mm, dec, img, flat, a):
     return torch.cat(out) if out else torch.zeros((0, 8), device="cuda")
 
 
-def test_hyb_batched_equals_plain_loop(mm):
-    img, flat, psf = hyb_case(mm)
+@pytest.mark.parametrize("X,Y", [(170, 150), (130, 130)])
+def test_hyb_batched_equals_plain_loop(mm, X, Y):
+    """Also at X = Y = 130, where the second tile has xd = 82 > P - overlap, so
+    xd + overlap is clipped to the padded size P = 84 in the yielded view."""
+    img, flat, psf = hyb_case(mm, X=X, Y=Y)
     Z = img.shape[0]
     dec = mm["dc"].Deconvolver(psf, img.shape, zpad=Z - 1, **HYB)
     dimg, dflat = img.cuda(), torch.from_numpy(flat).cuda()

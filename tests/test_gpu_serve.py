@@ -30,7 +30,9 @@ def requests(mm, n=6):
     for i in range(n):
         fov, rnd = i % 2, i // 2
         Z, X, Y = SHAPES[fov]
-        dapi = synth.dapi_stack(Z, X, Y, 100 + fov, n_nuclei=10, radii=(2.5, 10.0, 10.0))
+        # sparse nuclei: after the RMS normalisation their maxima exceed the
+        # drift threshold of 4 (a field filled to 7 % would top out near 3.9)
+        dapi = synth.dapi_stack(Z, X, Y, 100 + fov, n_nuclei=6, radii=(2.0, 6.0, 6.0))
         if rnd:  # a known integer drift of the whole stack
             dapi = torch.roll(dapi, shifts=(0, 2 * rnd, -rnd), dims=(0, 1, 2))
         cols = [synth.hyb_stack(Z, X, Y, 250, 10 * i + c, gain=synth.flat_gain(X, Y)) for c in range(1 + i % 2)]
@@ -84,6 +86,7 @@ def test_drift_against_round_zero(mm):
             assert r.drift is None
         else:
             tzxyf = np.asarray(r.drift[0])
+            assert r.drift[3] + r.drift[4] > 0  # matched points
             np.testing.assert_allclose(tzxyf, [0.0, -2.0 * r.request.round, 1.0 * r.request.round], atol=0.5)
 
 
