@@ -40,18 +40,14 @@ int set_smem(K *kernel, size_t bytes) {
 // float32 tiles gather straight from global memory.
 // ---------------------------------------------------------------------------
 template <typename T, int LMAX>
-__global__ void __launch_bounds__(kThreads)
-k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ flat,
-               float2 *__restrict__ S, FftPlan P, int nl) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void rows_fwd_group(const TileGeom &g, const T *__restrict__ img,
+                                               const float *__restrict__ flat, float2 *__restrict__ S,
+                                               const FftPlan &P, int nl, const FftSmem &L, int bx, int by) {
     const int n = P.n;
-    const FftSmem L = fft_smem_layout(smem_raw, P, nl);
-    fft_load_tables(P, L.tw, L.tab);
-
-    const int ti = g.t0 + blockIdx.y;
+    const int ti = g.t0 + by;
     const TileDesc d = mm_tile_desc(g, ti);
     const long long nrows = (long long)g.Z * g.P;
-    const long long row0 = (long long)blockIdx.x * 2 * nl;  // in (x, z) order
+    const long long row0 = (long long)bx * 2 * nl;  // in (x, z) order
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     float *Af = reinterpret_cast<float *>(L.A);
     // the y map of the tile (same for every row), after the scratch
@@ -165,7 +161,7 @@ k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ 
     // unpack the two real rows of each line into their spectrum rows z P + x
     const int H = g.H;
     const float invH = 1.0f / (float)H;
-    float2 *Sb = S + (long long)blockIdx.y * nrows * H;
+    float2 *Sb = S + (long long)by * nrows * H;
     for (int it = threadIdx.x; it < nl * H; it += blockDim.x) {
         const int l = fdiv_i(it, H, invH), k = it - l * H;
         const long long r0 = row0 + 2 * l, r1 = r0 + 1;
@@ -179,6 +175,21 @@ k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ 
             const long long xp = r1 / g.Z;
             Sb[((r1 - xp * g.Z) * g.P + xp) * H + k] = make_float2(0.5f * (ck.y + cn.y), -0.5f * (ck.x - cn.x));
         }
+    }
+}
+
+// persistent: a CTA per SM walks the groups (tables loaded once)
+template <typename T, int LMAX>
+__global__ void __launch_bounds__(kThreads)
+k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ flat,
+               float2 *__restrict__ S, FftPlan P, int nl, int gx, int ngroups) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const FftSmem L = fft_smem_layout(smem_raw, P, nl);
+    fft_load_tables(P, L.tw, L.tab);
+    for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+        const int by = grp / gx;
+        rows_fwd_group<T, LMAX>(g, img, flat, S, P, nl, L, grp - by * gx, by);
+        __syncthreads();
     }
 }
 
@@ -218,14 +229,11 @@ k_rows_fwd_f32(const float *__restrict__ vol, long long nrows, float2 *__restric
 // over a contiguous segment of the row held in shared memory.
 // ---------------------------------------------------------------------------
 template <int LMAX>
-__global__ void __launch_bounds__(kThreads)
-k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restrict__ out,
-           float *__restrict__ blur, int delta, FftPlan P, int nl) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void rows_inv_group(const float2 *__restrict__ S, long long nrows, int H,
+                                               float *__restrict__ out, float *__restrict__ blur, int delta,
+                                               const FftPlan &P, int nl, const FftSmem &L, int bx) {
     const int n = P.n;
-    const FftSmem L = fft_smem_layout(smem_raw, P, nl);
-    fft_load_tables(P, L.tw, L.tab);
-    const long long row0 = (long long)blockIdx.x * 2 * nl;
+    const long long row0 = (long long)bx * 2 * nl;
     const bool even = (n % 2) == 0;
     const float invH = 1.0f / (float)H, invn = 1.0f / (float)n;
     constexpr int U = 4;
@@ -298,6 +306,20 @@ k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restri
             if (row < nrows)
                 for (int e = lane; e < n; e += 32) blur[row * n + e] = Bf[(2 * l + c) * n + e];
         }
+    }
+}
+
+// persistent: a CTA per SM walks the row groups (tables loaded once)
+template <int LMAX>
+__global__ void __launch_bounds__(kThreads)
+k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restrict__ out,
+           float *__restrict__ blur, int delta, FftPlan P, int nl, int ngroups) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const FftSmem L = fft_smem_layout(smem_raw, P, nl);
+    fft_load_tables(P, L.tw, L.tab);
+    for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+        rows_inv_group<LMAX>(S, nrows, H, out, blur, delta, P, nl, L, grp);
+        __syncthreads();
     }
 }
 
@@ -419,11 +441,13 @@ int mm_launch_rows_fwd_img(const TileGeom &g, const void *img, int dtype, const 
     int nl = 16;
     while (nl > 1 && fft_smem(P, nl) + sizeof(int) * P.n > (size_t)kSmemLimit) nl >>= 1;
     size_t sm = fft_smem(P, nl) + sizeof(int) * P.n;
-    dim3 grid(mm_cdiv((long)g.Z * g.P, 2 * nl), g.nt);
+    int gx = mm_cdiv((long)g.Z * g.P, 2 * nl);
+    int ngroups = gx * g.nt;
+    dim3 grid(ngroups < mm_sm_count() ? ngroups : mm_sm_count());
     TileGeom ga = g;
     const void *imga = img;
     const float *fa = flat;
-    void *args[] = {&ga, &imga, &fa, &S, &P, &nl};
+    void *args[] = {&ga, &imga, &fa, &S, &P, &nl, &gx, &ngroups};
     const void *fn = dtype == MM_DTYPE_U16 ? MM_BY_CLASS(P, k_rows_fwd_img, uint16_t,)
                                           : MM_BY_CLASS(P, k_rows_fwd_img, float,);
     return launch_fft_kernel(fn, grid, sm, st, args);
@@ -448,8 +472,10 @@ int mm_launch_rows_inv(const float2 *S, int nrows, int Pn, int H, float *out, fl
     int nl = pick_nl(P, 16);
     size_t sm = fft_smem(P, nl);
     long long nr = nrows;
-    void *args[] = {&S, &nr, &H, &out, &blur, &delta, &P, &nl};
-    return launch_fft_kernel(MM_BY_CLASS(P, k_rows_inv, ), dim3(mm_cdiv(nrows, 2 * nl)), sm, st, args);
+    int ngroups = mm_cdiv(nrows, 2 * nl);
+    void *args[] = {&S, &nr, &H, &out, &blur, &delta, &P, &nl, &ngroups};
+    return launch_fft_kernel(MM_BY_CLASS(P, k_rows_inv, ), dim3(ngroups < mm_sm_count() ? ngroups : mm_sm_count()),
+                             sm, st, args);
 }
 
 int mm_launch_blur_x_sub(const TileGeom &g, const float *res, const float *tmp, int delta, float *res_out,

@@ -740,6 +740,20 @@ static inline int pick_nl(const FftPlan &P, int maxnl) {
     ((P).lclass == 0 ? (const void *)KERNEL_TMPL<__VA_ARGS__ 0>             \
      : (P).lclass == 63 ? (const void *)KERNEL_TMPL<__VA_ARGS__ 63>         \
                         : (const void *)KERNEL_TMPL<__VA_ARGS__ 127>)
+// SMs of the current device (cached per device)
+static inline int mm_sm_count() {
+    static int cache[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) dev = 0;
+    if (!cache[dev]) {
+        int v = 0;
+        cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+        cache[dev] = v > 0 ? v : 1;
+    }
+    return cache[dev];
+}
+
 static inline int launch_fft_kernel(const void *fn, dim3 grid, size_t sm, cudaStream_t st, void **args) {
     MM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     MM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(kFftThreads), args, sm, st));

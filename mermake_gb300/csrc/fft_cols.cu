@@ -13,26 +13,32 @@ constexpr int kSmemLimit = kFftSmemLimit;
 // ---------------------------------------------------------------------------
 template <bool INV, int LMAX>
 __global__ void __launch_bounds__(kThreads)
-k_cols(float2 *__restrict__ S, long long se, int nlines, long long plane_stride, FftPlan P, int nl) {
+k_cols(float2 *__restrict__ S, long long se, int nlines, long long plane_stride, FftPlan P, int nl, int gx,
+       int ngroups) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = P.n, lnl = log2_pow2(nl);
     const FftSmem L = fft_smem_layout(smem_raw, P, nl);
     fft_load_tables(P, L.tw, L.tab);
-    float2 *base = S + (long long)blockIdx.y * plane_stride;
-    const int l0 = blockIdx.x * nl;
-    for (int it = threadIdx.x; it < nl * n; it += blockDim.x) {
-        const int l = it & (nl - 1), e = it >> lnl;
-        if (l0 + l < nlines)
-            cp_async8(&L.A[sidx(e, l, nl)], &base[e * se + l0 + l]);
-        else
-            L.A[sidx(e, l, nl)] = make_float2(0.f, 0.f);
-    }
-    cp_async_wait_all();
-    __syncthreads();
-    float2 *R = fft_lines<INV, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
-    for (int it = threadIdx.x; it < nl * n; it += blockDim.x) {
-        const int l = it & (nl - 1), e = it >> lnl;
-        if (l0 + l < nlines) base[e * se + l0 + l] = R[sidx(e, l, nl)];
+    // persistent: a CTA per SM walks the groups of nl lines (tables loaded once)
+    for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+        const int by = grp / gx, bx = grp - by * gx;
+        float2 *base = S + (long long)by * plane_stride;
+        const int l0 = bx * nl;
+        for (int it = threadIdx.x; it < nl * n; it += blockDim.x) {
+            const int l = it & (nl - 1), e = it >> lnl;
+            if (l0 + l < nlines)
+                cp_async8(&L.A[sidx(e, l, nl)], &base[e * se + l0 + l]);
+            else
+                L.A[sidx(e, l, nl)] = make_float2(0.f, 0.f);
+        }
+        cp_async_wait_all();
+        __syncthreads();
+        float2 *R = fft_lines<INV, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
+        for (int it = threadIdx.x; it < nl * n; it += blockDim.x) {
+            const int l = it & (nl - 1), e = it >> lnl;
+            if (l0 + l < nlines) base[e * se + l0 + l] = R[sidx(e, l, nl)];
+        }
+        __syncthreads();  // the next group's loads overwrite the line buffers
     }
 }
 
@@ -45,8 +51,11 @@ int mm_launch_cols(float2 *S, int n, long long se, int nlines, long long plane_s
     if (rc) return rc;
     int nl = pick_nl(P, 16);
     size_t sm = fft_smem(P, nl);
-    dim3 grid(mm_cdiv(nlines, nl), nplanes);
-    void *args[] = {&S, &se, &nlines, &plane_stride, &P, &nl};
+    int gx = mm_cdiv(nlines, nl);
+    int ngroups = gx * nplanes;
+    // one CTA per SM (the line buffers fill its shared memory), persistent
+    dim3 grid(ngroups < mm_sm_count() ? ngroups : mm_sm_count());
+    void *args[] = {&S, &se, &nlines, &plane_stride, &P, &nl, &gx, &ngroups};
     const void *fn = inv ? MM_BY_CLASS(P, k_cols, true,) : MM_BY_CLASS(P, k_cols, false,);
     return launch_fft_kernel(fn, grid, sm, st, args);
 }
