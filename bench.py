@@ -2,7 +2,8 @@
 """Benchmark of the per-FOV image path (deconv + blur + maxima + fit).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mermake_gb300|reference]
-                    [--workload fov3c|quad|grid25|tile] [--form batched|plain]
+                    [--workload fov3c|quad|grid25|psfgrid|tile|served|drift16]
+                    [--form batched|plain] [--batch B]
 
 A step is one FOV of the workload, inputs resident in HBM:
 
@@ -15,6 +16,9 @@ A step is one FOV of the workload, inputs resident in HBM:
   field: the small case for profiler captures (spectra larger than L2).
 * ``grid25``: one colour of 50 x 1000 x 1000 in 5 x 5 tiles of 200 (padded
   378): a 25-tile batch, like a colour of ``fov3c``, in a few GB.
+* ``psfgrid``: one colour of 40 x 3000 x 3000 in tiles of 300 (padded 478),
+  each of the 100 tiles with its own PSF from a 10 x 10 grid (sigma growing
+  across the field), 60,000 puncta.
 * ``tile``: one smFISH tile, uint16 40 x 500 x 500, 2,000 puncta, no flat field.
 * ``served``: a Poisson stream of ``--fovs`` FOV requests over four FOV shapes
   (Z 30-60, XY 1024/2048, 1-3 colours + DAPI) through ``serve.FovServer``
@@ -63,6 +67,9 @@ WORKLOADS = {
     "grid25": dict(Z=50, X=1000, Y=1000, colours=1, puncta=10000, flat=True, dapi=False, nuclei=0,
                    hyb=dict(tile_size=200, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
                             delta_fit=3, sigmaZ=1, sigmaXY=1.5)),
+    "psfgrid": dict(Z=40, X=3000, Y=3000, colours=1, puncta=60000, flat=False, dapi=False, nuclei=0, psf_grid=10,
+                    hyb=dict(tile_size=300, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
+                             delta_fit=3, sigmaZ=1, sigmaXY=1.5)),
     "tile": dict(Z=40, X=500, Y=500, colours=1, puncta=2000, flat=False, dapi=False, nuclei=0,
                  hyb=dict(tile_size=500, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
                           delta_fit=3, sigmaZ=1, sigmaXY=1.5)),
@@ -80,6 +87,8 @@ def parse():
     ap.add_argument("--interval", type=float, default=0.25, help="served: mean Poisson arrival interval (s)")
     ap.add_argument("--workers", type=int, default=2, help="served: concurrent requests on the device")
     ap.add_argument("--form", default="batched", choices=["batched", "plain"])
+    ap.add_argument("--batch", type=int, default=0,
+                    help="batched form: tiles per batch (0: the tuned / L2-rule size, -1: all tiles)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     return ap.parse_args()
@@ -162,6 +171,11 @@ def setup(w, device, seed=1000):
     from mermake_gb300 import deconvolver, synth
     Z, X, Y = w["Z"], w["X"], w["Y"]
     psf = synth.gaussian_psf((40, 40, 40), 2.0, 1.3)
+    if w.get("psf_grid"):
+        # a PSF per tile in tile (x-major) order; sigma grows linearly across the field
+        n = w["psf_grid"]
+        psf = {(i, j): synth.gaussian_psf((40, 40, 40), 1.8 + 0.6 * (i + j) / (2 * n - 2),
+                                          1.1 + 0.5 * (i + j) / (2 * n - 2)) for i in range(n) for j in range(n)}
     gain = synth.flat_gain(X, Y) if w["flat"] else None
     chans, flats = [], []
     for c in range(w["colours"]):
@@ -186,12 +200,13 @@ def run_fov(s, form, chans=None, dapi=None):
     dapi = s["dapi"] if dapi is None else dapi
     out = []
     if w["dapi"]:
-        p, m, buf, _ = pipeline.dapi_spots(s["dec_d"], dapi, None, buffer=s.get("buffer"), **w["dapi_args"])
+        p, m, buf, _ = pipeline.dapi_spots(s["dec_d"], dapi, None, buffer=s.get("buffer"), batch=s["batch"],
+                                           **w["dapi_args"])
         s["buffer"] = buf
         out += [p, m]
     for c, ch in enumerate(chans):
         if form == "batched":
-            out.append(pipeline.hyb_spots(s["dec_h"], ch, s["flats"][c], **w["hyb"]))
+            out.append(pipeline.hyb_spots(s["dec_h"], ch, s["flats"][c], batch=s["batch"], **w["hyb"]))
         else:
             ov = w["hyb"]["overlap"]
             rows = []
@@ -252,6 +267,7 @@ def gpu_arm(args, rank, world, local):
             pg.barrier()
 
     s = setup(w, dev, seed=1000 + rank)
+    s["batch"] = args.batch
     vox = fov_voxels(w)
 
     # device-resident timed region, with per-stage events live
@@ -317,7 +333,7 @@ def gpu_arm(args, rank, world, local):
         "data": "synthetic (seeded Poisson background + Gaussian puncta / nuclei, shapes of the named workload)",
         "config": {"workload": args.workload, "form": args.form, "Z": w["Z"], "X": w["X"], "Y": w["Y"],
                    "channels": w["colours"] + (1 if w["dapi"] else 0), "tile_size": w["hyb"]["tile_size"],
-                   "overlap": w["hyb"]["overlap"], "fov_voxels": vox,
+                   "overlap": w["hyb"]["overlap"], "fov_voxels": vox, "batch": args.batch,
                    "l2": "inputs larger than L2 (%.2f GB per FOV vs 129 MB)" % (vox * 2 / 1e9),
                    "parallelism": "replicas" if world > 1 else "single"},
         "latency_ms": {"p50": pct(per, 50), "p99": pct(per, 99)},
@@ -343,7 +359,7 @@ def gpu_arm(args, rank, world, local):
             # memory on a side stream while FOV k computes; every step copies one
             # FOV and computes one FOV, and the timed region ends after the last
             # copy it issued
-            runner = pipeline.FovRunner(s["dec_h"], s["dec_d"], w["hyb"], w.get("dapi_args"))
+            runner = pipeline.FovRunner(s["dec_h"], s["dec_d"], w["hyb"], w.get("dapi_args"), batch=args.batch)
             state = {}
 
             def e2e_step():

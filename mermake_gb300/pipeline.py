@@ -15,7 +15,7 @@ import ctypes as C
 
 import torch
 
-from . import _lib
+from . import _lib, tune
 from ._arrays import as_device
 
 
@@ -46,26 +46,47 @@ def _check_delta(delta):
         raise TypeError("Delta must be an less than or equal to 5 due to MAX_KERNEL_POINTS")
 
 
+def _capacity(dec, key, default):
+    """Output rows to allocate: the largest count seen for ``key`` on this
+    Deconvolver plus a quarter, at least ``default``."""
+    seen = getattr(dec, "_rows_seen", {}).get(key, 0)
+    return max(default, seen + seen // 4)
+
+
+def _seen(dec, key, n):
+    d = dec.__dict__.setdefault("_rows_seen", {})
+    if n > d.get(key, 0):
+        d[key] = n
+
+
 def hyb_spots(dec, image, flat_field=None, *, threshold=None, delta=1, delta_fit=0, sigmaZ=1, sigmaXY=1.5,
-              blur_radius=None, batch=0, capacity=1 << 18, stream=None, **kwargs):
+              blur_radius=None, batch=0, capacity=None, stream=None, **kwargs):
     """Rows ``[zc, xc, yc, bg, a, habs, hn, h]`` of one colour, in FOV coordinates
-    (mermake/__main__.py:253-265).  ``dec`` is a ``Deconvolver``."""
+    (mermake/__main__.py:253-265).  ``dec`` is a ``Deconvolver``.  ``batch``:
+    tiles per batch; 0 picks it (``tune.batch_for``), negative means all.
+    ``capacity``: rows allocated for the output; None sizes it from the
+    largest count this Deconvolver has returned for the shape (a call that
+    overflows is run again with the exact count)."""
     _check_delta(delta)
     img = _u16_channel(image)
+    if batch == 0:
+        batch = tune.batch_for(dec, img.shape)
     fl = _flat(flat_field, img.shape)
     Z, X, Y = img.shape
     L = _lib.lib()
     th = float("nan") if threshold is None else float(threshold)
     br = -1 if blur_radius is None else int(blur_radius)
-    cap = int(capacity)
+    key = ("hyb", Z, X, Y)
+    cap = _capacity(dec, key, 1 << 18) if capacity is None else int(capacity)
     for _ in range(2):
         out = torch.empty((cap, 8), dtype=torch.float32, device=img.device)
         n = C.c_uint32(0)
         rc = L.mm_hyb_spots(_lib.ctx(img.device.index), _lib.ptr(img), Z, X, Y, img.stride(0), img.stride(1),
                             _lib.ptr(fl), fl.stride(0) if fl is not None else 0, _lib.ptr(dec.psf_fft),
                             dec.psf_fft.shape[0], _lib.ptr(dec.z_operator), dec.tile_size, dec.zpad, dec.overlap,
-                            br, th, int(delta), int(delta_fit), float(sigmaZ), float(sigmaXY), int(batch),
+                            br, th, int(delta), int(delta_fit), float(sigmaZ), float(sigmaXY), max(int(batch), 0),
                             _lib.ptr(out), cap, C.byref(n), _lib.stream_ptr(stream))
+        _seen(dec, key, int(n.value))
         if rc == _lib.MM_EOVERFLOW:
             cap = int(n.value)
             continue
@@ -75,12 +96,14 @@ def hyb_spots(dec, image, flat_field=None, *, threshold=None, delta=1, delta_fit
 
 
 def dapi_spots(dec, image, flat_field=None, *, threshold=None, delta=1, delta_fit=0, sigmaZ=1, sigmaXY=1.5,
-               blur_radius=None, batch=0, buffer=None, capacity=1 << 16, stream=None, **kwargs):
+               blur_radius=None, batch=0, buffer=None, capacity=None, stream=None, **kwargs):
     """``(Xh_plus, Xh_minus, buffer, rms)`` of the DAPI block
     (mermake/__main__.py:215-225); ``buffer`` holds the stitched deconvolution
-    before normalisation."""
+    before normalisation.  ``batch`` as in ``hyb_spots``."""
     _check_delta(delta)
     img = _u16_channel(image)
+    if batch == 0:
+        batch = tune.batch_for(dec, img.shape, dapi=True)
     fl = _flat(flat_field, img.shape)
     Z, X, Y = img.shape
     if buffer is None:
@@ -88,7 +111,11 @@ def dapi_spots(dec, image, flat_field=None, *, threshold=None, delta=1, delta_fi
     L = _lib.lib()
     th = float("nan") if threshold is None else float(threshold)
     br = -1 if blur_radius is None else int(blur_radius)
-    cp, cm = int(capacity), int(capacity)
+    kp, km = ("dapi+", Z, X, Y), ("dapi-", Z, X, Y)
+    if capacity is None:
+        cp, cm = _capacity(dec, kp, 1 << 16), _capacity(dec, km, 1 << 16)
+    else:
+        cp, cm = int(capacity), int(capacity)
     for _ in range(2):
         op = torch.empty((cp, 8), dtype=torch.float32, device=img.device)
         om = torch.empty((cm, 8), dtype=torch.float32, device=img.device)
@@ -97,8 +124,10 @@ def dapi_spots(dec, image, flat_field=None, *, threshold=None, delta=1, delta_fi
                              _lib.ptr(fl), fl.stride(0) if fl is not None else 0, _lib.ptr(dec.psf_fft),
                              dec.psf_fft.shape[0], _lib.ptr(dec.z_operator), dec.tile_size, dec.zpad,
                              dec.overlap, br, th, int(delta), int(delta_fit), float(sigmaZ), float(sigmaXY),
-                             int(batch), _lib.ptr(buffer), _lib.ptr(op), cp, C.byref(n_p), _lib.ptr(om), cm, C.byref(n_m), C.byref(rms),
+                             max(int(batch), 0), _lib.ptr(buffer), _lib.ptr(op), cp, C.byref(n_p), _lib.ptr(om), cm, C.byref(n_m), C.byref(rms),
                              _lib.stream_ptr(stream))
+        _seen(dec, kp, int(n_p.value))
+        _seen(dec, km, int(n_m.value))
         if rc == _lib.MM_EOVERFLOW:
             cp, cm = max(cp, int(n_p.value)), max(cm, int(n_m.value))
             continue

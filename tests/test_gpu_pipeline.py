@@ -153,3 +153,20 @@ def test_fov_runner_matches_direct_calls(mm):
         for got, want in zip(rows, want_rows):
             np.testing.assert_array_equal(ck.sort_rows(got), ck.sort_rows(want.cpu().numpy()))
     assert runner.h2d_bytes == 3 * Z * X * Y * 2
+
+
+def test_autotune_picks_a_batch_and_keeps_rows(mm):
+    """tune.autotune times candidate batch sizes on the channel, keeps the
+    fastest for the geometry, and hyb_spots(batch=0) then uses it with the
+    same rows (9 tiles: every candidate runs the padded-depth transforms)."""
+    from mermake_gb300 import tune
+    img, flat, psf = hyb_case(mm)
+    Z = img.shape[0]
+    dec = mm["dc"].Deconvolver(psf, img.shape, zpad=Z - 1, **HYB)
+    dimg, dflat = img.cuda(), torch.from_numpy(flat).cuda()
+    times = tune.autotune(dec, dimg, dflat, HYB, candidates=(1, 4, -1), reps=1)
+    assert set(times) == {1, 4, -1} and all(t > 0 for t in times.values())
+    assert tune.batch_for(dec, img.shape) == min(times, key=times.get)
+    want = ck.sort_rows(mm["pl"].hyb_spots(dec, dimg, dflat, batch=-1, **HYB).cpu().numpy())
+    got = ck.sort_rows(mm["pl"].hyb_spots(dec, dimg, dflat, **HYB).cpu().numpy())
+    np.testing.assert_array_equal(got, want)

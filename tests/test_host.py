@@ -103,3 +103,40 @@ def test_find_local_maxima_rejects_large_delta_before_any_device_work():
     from mermake_gb300.maxima import find_local_maxima
     with pytest.raises(TypeError, match="Delta must be an less than or equal to 5"):
         find_local_maxima(np.ones((3, 3, 3), np.float32), threshold=0.5, delta=6, delta_fit=1)
+
+
+def test_default_batch_takes_all_tiles_within_the_scratch_budget(monkeypatch):
+    """tune.default_batch: one batch of all tiles (-1) while their scratch
+    fits SCRATCH_BYTES, else as many tiles as fit; a tuned size wins."""
+    import types
+    from mermake_gb300 import tune
+
+    def dec(Z, ts, ov, nt):
+        P = ts + 2 * ov
+        return types.SimpleNamespace(tile_height=Z, P=P, H=P // 2 + 1, n_tiles=lambda shape: nt)
+
+    assert tune.default_batch(dec(40, 300, 89, 100), (40, 3000, 3000)) == -1    # 11 GB
+    assert tune.default_batch(dec(50, 500, 89, 25), (50, 2048, 2048)) == -1    # 6.9 GB
+    monkeypatch.setattr(tune, "SCRATCH_BYTES", 1 << 30)
+    assert tune.default_batch(dec(40, 300, 89, 100), (40, 3000, 3000)) == 9     # 110 MB per tile
+    assert tune.default_batch(dec(50, 500, 89, 25), (50, 2048, 2048)) == 3
+    d = dec(40, 300, 89, 100)
+    d._tuned_batch = {((40, 3000, 3000), False): 4}
+    assert tune.batch_for(d, (40, 3000, 3000)) == 4
+    assert tune.batch_for(d, (40, 3000, 3000), dapi=True) == 9
+
+
+def test_spot_capacity_grows_from_counts_seen():
+    """The drivers size the output rows from the largest count a Deconvolver
+    has returned for the shape (plus a quarter), so a FOV with more spots than
+    the default overflows (and reruns) once, not on every call."""
+    import types
+    from mermake_gb300 import pipeline
+    dec = types.SimpleNamespace()
+    key = ("hyb", 40, 3000, 3000)
+    assert pipeline._capacity(dec, key, 1 << 18) == 1 << 18
+    pipeline._seen(dec, key, 322214)
+    assert pipeline._capacity(dec, key, 1 << 18) == 322214 + 322214 // 4
+    pipeline._seen(dec, key, 1000)                       # a smaller count keeps the largest
+    assert pipeline._capacity(dec, key, 1 << 18) == 322214 + 322214 // 4
+    assert pipeline._capacity(dec, ("dapi+", 40, 3000, 3000), 1 << 16) == 1 << 16
