@@ -23,6 +23,7 @@ namespace {
 
 constexpr int kThreads = kFftThreads;
 constexpr int kSmemLimit = kFftSmemLimit;
+constexpr int kBlurThreads = 512;  // k_blur_x_sub, k_make_raw
 
 template <typename K>
 int set_smem(K *kernel, size_t bytes) {
@@ -51,7 +52,7 @@ __device__ __forceinline__ void rows_fwd_group(const TileGeom &g, const T *__res
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
     float *Af = reinterpret_cast<float *>(L.A);
     // the y map of the tile (same for every row), after the scratch
-    int *ymap = reinterpret_cast<int *>(L.scr + MM_FFT_SCR_PER_WARP * nw);
+    int *ymap = reinterpret_cast<int *>(L.scr + fft_scr_f4(P, nl, nw));
     for (int e = threadIdx.x; e < n; e += blockDim.x) ymap[e] = mm_map_xy(e, d.y == 0, d.yd, g.P, g.ov);
 
     if constexpr (sizeof(T) == 2) {
@@ -178,9 +179,9 @@ __device__ __forceinline__ void rows_fwd_group(const TileGeom &g, const T *__res
     }
 }
 
-// persistent: a CTA per SM walks the groups (tables loaded once)
+// persistent: the CTAs walk the groups (tables loaded once)
 template <typename T, int LMAX>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kFftCtasPerSm)
 k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ flat,
                float2 *__restrict__ S, FftPlan P, int nl, int gx, int ngroups) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -195,7 +196,7 @@ k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ 
 
 // y pass, forward, dense f32 source (the padded PSF volume)
 template <int LMAX>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kFftCtasPerSm)
 k_rows_fwd_f32(const float *__restrict__ vol, long long nrows, float2 *__restrict__ S, FftPlan P, int nl) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = P.n, H = n / 2 + 1;
@@ -309,9 +310,9 @@ __device__ __forceinline__ void rows_inv_group(const float2 *__restrict__ S, lon
     }
 }
 
-// persistent: a CTA per SM walks the row groups (tables loaded once)
+// persistent: the CTAs walk the row groups (tables loaded once)
 template <int LMAX>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kFftCtasPerSm)
 k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restrict__ out,
            float *__restrict__ blur, int delta, FftPlan P, int nl, int ngroups) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -331,7 +332,7 @@ k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restri
 // down a segment of rows.  delta < 0: no blur (res copied).
 // ---------------------------------------------------------------------------
 template <bool STITCH>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kBlurThreads)
 k_blur_x_sub(TileGeom g, const float *__restrict__ res, const float *__restrict__ tmp, int delta,
              float *res_out, float *__restrict__ stitch, long long osz, long long osx) {
     extern __shared__ __align__(16) float colbuf[];  // P x 32, then the reciprocal table
@@ -443,7 +444,7 @@ int mm_launch_rows_fwd_img(const TileGeom &g, const void *img, int dtype, const 
     size_t sm = fft_smem(P, nl) + sizeof(int) * P.n;
     int gx = mm_cdiv((long)g.Z * g.P, 2 * nl);
     int ngroups = gx * g.nt;
-    dim3 grid(ngroups < mm_sm_count() ? ngroups : mm_sm_count());
+    dim3 grid(fft_grid(ngroups));
     TileGeom ga = g;
     const void *imga = img;
     const float *fa = flat;
@@ -469,13 +470,20 @@ int mm_launch_rows_inv(const float2 *S, int nrows, int Pn, int H, float *out, fl
     FftPlan P;
     int rc = mm_fft_plan_get(Pn, &P);
     if (rc) return rc;
-    int nl = pick_nl(P, 16);
-    size_t sm = fft_smem(P, nl);
+    // the y blur's reciprocal table goes in the scratch: room for 2 delta + 2 floats
+    auto bytes = [&](int l) {
+        const size_t scr = sizeof(float4) * fft_scr_f4(P, l, kThreads / 32);
+        const size_t rt = delta >= 0 ? sizeof(float) * (2 * (size_t)delta + 2) : 0;
+        return fft_smem(P, l) + (rt > scr ? ((rt - scr + 15) & ~(size_t)15) : 0);
+    };
+    int nl = 16;
+    while (nl > 1 && bytes(nl) > (size_t)kSmemLimit) nl >>= 1;
+    MM_REQUIRE(bytes(nl) <= (size_t)kSmemLimit, "blur radius %d too large for the tile", delta);
+    size_t sm = bytes(nl);
     long long nr = nrows;
     int ngroups = mm_cdiv(nrows, 2 * nl);
     void *args[] = {&S, &nr, &H, &out, &blur, &delta, &P, &nl, &ngroups};
-    return launch_fft_kernel(MM_BY_CLASS(P, k_rows_inv, ), dim3(ngroups < mm_sm_count() ? ngroups : mm_sm_count()),
-                             sm, st, args);
+    return launch_fft_kernel(MM_BY_CLASS(P, k_rows_inv, ), dim3(fft_grid(ngroups)), sm, st, args);
 }
 
 int mm_launch_blur_x_sub(const TileGeom &g, const float *res, const float *tmp, int delta, float *res_out,
@@ -486,10 +494,10 @@ int mm_launch_blur_x_sub(const TileGeom &g, const float *res, const float *tmp, 
     dim3 grid(mm_cdiv(g.P, 32), g.Z, g.nt);
     if (stitch) {
         if ((rc = set_smem(k_blur_x_sub<true>, sm > 0 ? sm : 1))) return rc;
-        k_blur_x_sub<true><<<grid, kThreads, sm, st>>>(g, res, tmp, delta, res_out, stitch, osz, osx);
+        k_blur_x_sub<true><<<grid, kBlurThreads, sm, st>>>(g, res, tmp, delta, res_out, stitch, osz, osx);
     } else {
         if ((rc = set_smem(k_blur_x_sub<false>, sm > 0 ? sm : 1))) return rc;
-        k_blur_x_sub<false><<<grid, kThreads, sm, st>>>(g, res, tmp, delta, res_out, stitch, osz, osx);
+        k_blur_x_sub<false><<<grid, kBlurThreads, sm, st>>>(g, res, tmp, delta, res_out, stitch, osz, osx);
     }
     MM_CHECK_LAUNCH();
     return MM_OK;
@@ -499,9 +507,9 @@ int mm_launch_make_raw(const TileGeom &g, const void *img, int dtype, const floa
                        cudaStream_t st) {
     dim3 grid(304, 1, g.nt);
     if (dtype == MM_DTYPE_U16)
-        k_make_raw<uint16_t><<<grid, kThreads, 0, st>>>(g, (const uint16_t *)img, flat, raw);
+        k_make_raw<uint16_t><<<grid, kBlurThreads, 0, st>>>(g, (const uint16_t *)img, flat, raw);
     else
-        k_make_raw<float><<<grid, kThreads, 0, st>>>(g, (const float *)img, flat, raw);
+        k_make_raw<float><<<grid, kBlurThreads, 0, st>>>(g, (const float *)img, flat, raw);
     MM_CHECK_LAUNCH();
     return MM_OK;
 }

@@ -6,9 +6,9 @@
 // factored into stages of four kinds:
 //   * radix 2/3/4/5/6/7 and the odd primes 11..37: one thread per butterfly,
 //     values in registers;
-//   * 113 (678 = 6*113): Rader's algorithm, the 113-point DFT as a cyclic
-//     convolution of length 112 = 16*7 done with small register DFTs
-//     (stage_rader113);
+//   * 113 (678 = 6*113) and 239 (478 = 2*239): Rader's algorithm, the prime
+//     DFT as a cyclic convolution of length 112 = 16*7 or 238 = 14*17 done
+//     with small register DFTs (stage_rader);
 //   * primes 41..61, 79 and 89 ("lane" stage; 59, 79 and 89 are the primes of
 //     the reference's padded depths such as 118 = 2*59): one warp per
 //     butterfly and one lane per output pair (k, R-k); each lane keeps its
@@ -450,43 +450,137 @@ __device__ __forceinline__ void dft16(float2 *v) {
     }
 }
 
-// The 113-point stage by Rader's algorithm.  With g = 3 a primitive root,
-// X[g^m] = x_0 + sum_q u[q] h[(m - q) mod 112], u[q] = x[g^-q],
-// h[s] = w113^(g^s), and X[0] = x_0 + sum u: a cyclic convolution of length
-// 112 = 16 x 7, done as FFT-112, a product with the precomputed FFT of h
-// (already divided by 112), and an inverse FFT-112, in three passes over the
-// CTA's m * nl butterflies held in dst as T[q1 * 7 + k2][b]:
-//   1. gather u[q1 + 16 q2] (twiddled), 7-point DFT over q2, times w112^(q1 k2);
-//   2. per (k2, b): 16-point DFT over q1, product with H[k2 + 7 k1], inverse
-//      16-point DFT over k1, times w112^-(q1 k2), all in registers;
-//   3. inverse 7-point DFT over k2, then X[g^(q1 + 16 q2)] = x_0 + c into src.
-// About three times fewer arithmetic instructions than the direct DFT.  The
-// stage's output is left in src; x_0 and sum u go through scr_all.
-// tb: the stage's table (cos/sin, then the Rader tables of fft_plan.cu).
+// radix 14 = 2 x 7: X[k] = E[k] + w14^k O[k], X[k+7] = E[k] - w14^k O[k]
+// (k < 7), E/O the 7-point DFTs of the even/odd samples
 template <bool INV>
-__device__ __noinline__ void stage_rader113(float2 *__restrict__ src, float2 *__restrict__ dst, int n, int nl,
-                                            int Ns, const float2 *__restrict__ tw, const float2 *__restrict__ tb,
-                                            float4 *__restrict__ scr_all) {
-    constexpr int R = 113;
+__device__ __forceinline__ void dft14(float2 *v) {
+    float2 e[7], o[7];
+#pragma unroll
+    for (int r = 0; r < 7; ++r) {
+        e[r] = v[2 * r];
+        o[r] = v[2 * r + 1];
+    }
+    dft_odd<7, INV>(e);
+    dft_odd<7, INV>(o);
+    // cos / sin of pi k / 7, k = 1..6
+    const float c[6] = {0.90096886790241912624f, 0.62348980185873353053f, 0.22252093395631440429f,
+                        -0.22252093395631440429f, -0.62348980185873353053f, -0.90096886790241912624f};
+    const float sn[6] = {0.43388373911755812048f, 0.78183148246802980871f, 0.97492791218182360702f,
+                         0.97492791218182360702f, 0.78183148246802980871f, 0.43388373911755812048f};
+    v[0] = cadd(e[0], o[0]);
+    v[7] = csub(e[0], o[0]);
+#pragma unroll
+    for (int k = 1; k < 7; ++k) {
+        const float2 w = make_float2(c[k - 1], INV ? sn[k - 1] : -sn[k - 1]);
+        const float2 t = cmul(o[k], w);
+        v[k] = cadd(e[k], t);
+        v[k + 7] = csub(e[k], t);
+    }
+}
+
+// Odd radix R in registers with its cos/sin values passed in registers:
+// c[m-1] = cos(2 pi m / R), sn[m-1] = sin(2 pi m / R), m = 1..(R-1)/2.
+template <int R, bool INV>
+__device__ __forceinline__ void dft_odd_t(float2 *v, const float *c, const float *sn) {
+    constexpr int H = (R - 1) / 2;
+    float2 a[H], b[H];
+#pragma unroll
+    for (int r = 1; r <= H; ++r) {
+        a[r - 1] = cadd(v[r], v[R - r]);
+        b[r - 1] = csub(v[r], v[R - r]);
+    }
+    const float2 x0 = v[0];
+    float2 s0 = x0;
+#pragma unroll
+    for (int r = 0; r < H; ++r) s0 = cadd(s0, a[r]);
+#pragma unroll
+    for (int k = 1; k <= H; ++k) {
+        float ax = x0.x, ay = x0.y, bx = 0.f, by = 0.f;
+#pragma unroll
+        for (int r = 1; r <= H; ++r) {
+            const int m = (r * k) % R;
+            const float cc = m <= H ? c[m - 1] : c[R - m - 1];
+            const float ss = m <= H ? sn[m - 1] : -sn[R - m - 1];
+            ax += a[r - 1].x * cc;
+            ay += a[r - 1].y * cc;
+            bx += b[r - 1].x * ss;
+            by += b[r - 1].y * ss;
+        }
+        if (!INV) {
+            v[k] = make_float2(ax + by, ay - bx);
+            v[R - k] = make_float2(ax - by, ay + bx);
+        } else {
+            v[k] = make_float2(ax - by, ay + bx);
+            v[R - k] = make_float2(ax + by, ay - bx);
+        }
+    }
+    v[0] = s0;
+}
+
+// The register DFTs of the Rader stages: 7, 14 and 16 with constants, 17
+// with the cos/sin values the stage loaded into c / sn.
+template <int N, bool INV>
+__device__ __forceinline__ void rader_dft(float2 *v, const float *c, const float *sn) {
+    if constexpr (N == 7)
+        dft_odd<7, INV>(v);
+    else if constexpr (N == 14)
+        dft14<INV>(v);
+    else if constexpr (N == 16)
+        dft16<INV>(v);
+    else {
+        static_assert(N == 17, "Rader sub-transform lengths are 7, 14, 16 and 17");
+        dft_odd_t<17, INV>(v, c, sn);
+    }
+}
+
+// A prime stage R by Rader's algorithm (113 = 1 + 16 x 7, 239 = 1 + 14 x 17).
+// With g a primitive root mod R, X[g^m] = x_0 + sum_q u[q] h[(m - q) mod M],
+// M = R - 1, u[q] = x[g^-q], h[s] = wR^(g^s), and X[0] = x_0 + sum u: a cyclic
+// convolution of length M = N1 x N2, done as FFT-M, a product with the
+// precomputed FFT of h (already divided by M), and an inverse FFT-M, in three
+// passes over the CTA's m * nl butterflies held in dst as T[q1 * N2 + k2][b]:
+//   1. gather u[q1 + N1 q2] (twiddled), N2-point DFT over q2, times wM^(q1 k2);
+//   2. per (k2, b): N1-point DFT over q1, product with H[k2 + N2 k1], inverse
+//      N1-point DFT over k1, times wM^-(q1 k2), all in registers;
+//   3. inverse N2-point DFT over k2, then X[g^(q1 + N1 q2)] = x_0 + c into src.
+// The stage's output is left in src; x_0 and sum u go through scr_all.
+// tb: the stage's table (cos/sin of R, then the Rader tables of fft_plan.cu:
+// FFT of h forward and inverse, wM, the (g^-q, g^q) index pairs, and for
+// N2 = 17 the cos/sin of 17).
+template <int R, int N1, int N2, bool INV>
+__device__ __noinline__ void stage_rader(float2 *__restrict__ src, float2 *__restrict__ dst, int n, int nl,
+                                         int Ns, const float2 *__restrict__ tw, const float2 *__restrict__ tb,
+                                         float4 *__restrict__ scr_all) {
+    constexpr int M = R - 1;
+    static_assert(N1 * N2 == M, "Rader split must cover R - 1");
     const int m = n / R, nb = m * nl;
     const int tstep = n / (Ns * R);
     const int lnl = log2_pow2(nl);
     const float invNs = 1.0f / (float)Ns, invnb = 1.0f / (float)nb;
-    const float2 *Hh = tb + R + (INV ? 112 : 0);
-    const float2 *w112 = tb + R + 224;
-    const int2 *gq = reinterpret_cast<const int2 *>(tb + R + 336);  // (g^-q, g^q)
+    const float2 *Hh = tb + R + (INV ? M : 0);
+    const float2 *wM = tb + R + 2 * M;
+    const int2 *gq = reinterpret_cast<const int2 *>(tb + R + 3 * M);  // (g^-q, g^q)
+    float c2[N2 == 17 ? 8 : 1], s2[N2 == 17 ? 8 : 1];
+    if constexpr (N2 == 17) {
+        const float2 *cs = tb + R + 4 * M;
+#pragma unroll
+        for (int k = 1; k <= 8; ++k) {
+            c2[k - 1] = cs[k].x;
+            s2[k - 1] = -cs[k].y;  // table holds (cos, -sin)
+        }
+    }
     float2 *x0s = reinterpret_cast<float2 *>(scr_all);
     float2 *s0s = x0s + nb;
     float2 *T = dst;
 
-    for (int e = threadIdx.x; e < 16 * nb; e += blockDim.x) {
+    for (int e = threadIdx.x; e < N1 * nb; e += blockDim.x) {
         const int q1 = fdiv_i(e, nb, invnb), b = e - q1 * nb;
         const int l = b & (nl - 1), j = b >> lnl;
         const int kk = Ns > 1 ? j - fdiv_i(j, Ns, invNs) * Ns : 0;
-        float2 v[7];
+        float2 v[N2];
 #pragma unroll
-        for (int q2 = 0; q2 < 7; ++q2) {
-            const int r = gq[q1 + 16 * q2].x;
+        for (int q2 = 0; q2 < N2; ++q2) {
+            const int r = gq[q1 + N1 * q2].x;
             float2 x = src[sidx(j + r * m, l, nl)];
             if (Ns > 1) {
                 const float2 w = tw[kk * r * tstep];
@@ -495,39 +589,39 @@ __device__ __noinline__ void stage_rader113(float2 *__restrict__ src, float2 *__
             v[q2] = x;
         }
         if (q1 == 0) x0s[b] = src[sidx(j, l, nl)];
-        dft_small<7, false>(v);
-        T[(q1 * 7) * nb + b] = v[0];
+        rader_dft<N2, false>(v, c2, s2);
+        T[(q1 * N2) * nb + b] = v[0];
 #pragma unroll
-        for (int k2 = 1; k2 < 7; ++k2) T[(q1 * 7 + k2) * nb + b] = cmul(v[k2], w112[q1 * k2]);
+        for (int k2 = 1; k2 < N2; ++k2) T[(q1 * N2 + k2) * nb + b] = cmul(v[k2], wM[q1 * k2]);
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < 7 * nb; e += blockDim.x) {
+    for (int e = threadIdx.x; e < N2 * nb; e += blockDim.x) {
         const int k2 = fdiv_i(e, nb, invnb), b = e - k2 * nb;
-        float2 v[16];
+        float2 v[N1];
 #pragma unroll
-        for (int q1 = 0; q1 < 16; ++q1) v[q1] = T[(q1 * 7 + k2) * nb + b];
-        dft16<false>(v);
+        for (int q1 = 0; q1 < N1; ++q1) v[q1] = T[(q1 * N2 + k2) * nb + b];
+        rader_dft<N1, false>(v, c2, s2);
         if (k2 == 0) s0s[b] = v[0];
 #pragma unroll
-        for (int k1 = 0; k1 < 16; ++k1) v[k1] = cmul(v[k1], Hh[k2 + 7 * k1]);
-        dft16<true>(v);
+        for (int k1 = 0; k1 < N1; ++k1) v[k1] = cmul(v[k1], Hh[k2 + N2 * k1]);
+        rader_dft<N1, true>(v, c2, s2);
         T[k2 * nb + b] = v[0];
 #pragma unroll
-        for (int q1 = 1; q1 < 16; ++q1) T[(q1 * 7 + k2) * nb + b] = cmulc(v[q1], w112[q1 * k2]);
+        for (int q1 = 1; q1 < N1; ++q1) T[(q1 * N2 + k2) * nb + b] = cmulc(v[q1], wM[q1 * k2]);
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < 16 * nb; e += blockDim.x) {
+    for (int e = threadIdx.x; e < N1 * nb; e += blockDim.x) {
         const int q1 = fdiv_i(e, nb, invnb), b = e - q1 * nb;
         const int l = b & (nl - 1), j = b >> lnl;
         const int kk = Ns > 1 ? j - fdiv_i(j, Ns, invNs) * Ns : 0;
         const int d = (j - kk) * R + kk;
-        float2 v[7];
+        float2 v[N2];
 #pragma unroll
-        for (int k2 = 0; k2 < 7; ++k2) v[k2] = T[(q1 * 7 + k2) * nb + b];
-        dft_small<7, true>(v);
+        for (int k2 = 0; k2 < N2; ++k2) v[k2] = T[(q1 * N2 + k2) * nb + b];
+        rader_dft<N2, true>(v, c2, s2);
         const float2 x0 = x0s[b];
 #pragma unroll
-        for (int q2 = 0; q2 < 7; ++q2) src[sidx(d + gq[q1 + 16 * q2].y * Ns, l, nl)] = cadd(x0, v[q2]);
+        for (int q2 = 0; q2 < N2; ++q2) src[sidx(d + gq[q1 + N1 * q2].y * Ns, l, nl)] = cadd(x0, v[q2]);
         if (q1 == 0) src[sidx(d, l, nl)] = cadd(x0, s0s[b]);
     }
 }
@@ -648,9 +742,12 @@ __device__ float2 *fft_lines(float2 *A, float2 *B, int nl, const FftPlan &P,
     for (int st = 0; st < P.nst; ++st) {
         const int R = P.rad[st], Ns = P.ns[st];
         if constexpr (LMAX >= 113) {
-            // 113 by Rader's algorithm (output left in src)
-            if (R == 113) {
-                stage_rader113<INV>(src, dst, P.n, nl, Ns, tw_s, tab_s + P.ptab[st], scr);
+            // 113 and 239 by Rader's algorithm (output left in src)
+            if (R == 113 || R == 239) {
+                if (R == 113)
+                    stage_rader<113, 16, 7, INV>(src, dst, P.n, nl, Ns, tw_s, tab_s + P.ptab[st], scr);
+                else
+                    stage_rader<239, 14, 17, INV>(src, dst, P.n, nl, Ns, tw_s, tab_s + P.ptab[st], scr);
                 __syncthreads();
                 continue;
             }
@@ -684,10 +781,26 @@ struct FftSmem {
     float2 *A, *B, *tw, *tab;
     float4 *scr;
 };
-__device__ __host__ inline size_t fft_smem_bytes(int n, int ntab, int nl, int nwarps) {
-    size_t b = sizeof(float2) * ((size_t)2 * n * nl + n + ntab);
+// Scratch (float4 entries) the plan's stages use: MM_FFT_SCR_PER_WARP per warp
+// for a lane stage, x_0 and sum u of every butterfly (one float4) for the
+// 113- and 239-point stages, none for the others.
+__device__ __host__ inline int fft_scr_f4(const FftPlan &P, int nl, int nwarps) {
+    int f4 = 0;
+    for (int s = 0; s < P.nst; ++s) {
+        const int R = P.rad[s];
+        int need = 0;
+        if (R == 113 || R == 239)
+            need = (P.n / R) * nl;
+        else if (R == 41 || R == 43 || R == 47 || R == 53 || R == 59 || R == 61 || R == 79 || R == 89)
+            need = MM_FFT_SCR_PER_WARP * nwarps;
+        f4 = need > f4 ? need : f4;
+    }
+    return f4;
+}
+__device__ __host__ inline size_t fft_smem_bytes(const FftPlan &P, int nl, int nwarps) {
+    size_t b = sizeof(float2) * ((size_t)2 * P.n * nl + P.n + P.ntab);
     b = (b + 15) & ~(size_t)15;
-    return b + sizeof(float4) * MM_FFT_SCR_PER_WARP * nwarps;
+    return b + sizeof(float4) * fft_scr_f4(P, nl, nwarps);
 }
 __device__ inline FftSmem fft_smem_layout(void *base, const FftPlan &P, int nl) {
     FftSmem L;
@@ -723,12 +836,14 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 int mm_fft_plan_get(int n, FftPlan *out);
 
 // ---- launch helpers shared by the FFT kernel translation units -------------
+// kFftCtasPerSm CTAs of kFftThreads threads share an SM (228 KB of shared
+// memory, 1 KB of it reserved per CTA); the persistent passes launch that many
+// CTAs per SM.
 constexpr int kFftThreads = 512;
-constexpr int kFftSmemLimit = 224 * 1024;
+constexpr int kFftCtasPerSm = 1;
+constexpr int kFftSmemLimit = (224 / kFftCtasPerSm) * 1024;
 
-static inline size_t fft_smem(const FftPlan &P, int nl) {
-    return fft_smem_bytes(P.n, P.ntab, nl, kFftThreads / 32);
-}
+static inline size_t fft_smem(const FftPlan &P, int nl) { return fft_smem_bytes(P, nl, kFftThreads / 32); }
 // Lines per CTA: the largest power of two <= maxnl whose buffers fit the budget.
 static inline int pick_nl(const FftPlan &P, int maxnl) {
     int nl = maxnl;
@@ -752,6 +867,12 @@ static inline int mm_sm_count() {
         cache[dev] = v > 0 ? v : 1;
     }
     return cache[dev];
+}
+
+// CTAs of a persistent pass over ngroups line groups
+static inline unsigned fft_grid(long long ngroups) {
+    const long long cap = (long long)mm_sm_count() * kFftCtasPerSm;
+    return (unsigned)(ngroups < cap ? ngroups : cap);
 }
 
 static inline int launch_fft_kernel(const void *fn, dim3 grid, size_t sm, cudaStream_t st, void **args) {

@@ -12,14 +12,14 @@ constexpr int kSmemLimit = kFftSmemLimit;
 // staged into shared memory with cp.async.
 // ---------------------------------------------------------------------------
 template <bool INV, int LMAX>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kFftCtasPerSm)
 k_cols(float2 *__restrict__ S, long long se, int nlines, long long plane_stride, FftPlan P, int nl, int gx,
        int ngroups) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = P.n, lnl = log2_pow2(nl);
     const FftSmem L = fft_smem_layout(smem_raw, P, nl);
     fft_load_tables(P, L.tw, L.tab);
-    // persistent: a CTA per SM walks the groups of nl lines (tables loaded once)
+    // persistent: the CTAs walk the groups of nl lines (tables loaded once)
     for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
         const int by = grp / gx, bx = grp - by * gx;
         float2 *base = S + (long long)by * plane_stride;
@@ -53,8 +53,8 @@ int mm_launch_cols(float2 *S, int n, long long se, int nlines, long long plane_s
     size_t sm = fft_smem(P, nl);
     int gx = mm_cdiv(nlines, nl);
     int ngroups = gx * nplanes;
-    // one CTA per SM (the line buffers fill its shared memory), persistent
-    dim3 grid(ngroups < mm_sm_count() ? ngroups : mm_sm_count());
+    // persistent: kFftCtasPerSm CTAs per SM (their line buffers fill its shared memory)
+    dim3 grid(fft_grid(ngroups));
     void *args[] = {&S, &se, &nlines, &plane_stride, &P, &nl, &gx, &ngroups};
     const void *fn = inv ? MM_BY_CLASS(P, k_cols, true,) : MM_BY_CLASS(P, k_cols, false,);
     return launch_fft_kernel(fn, grid, sm, st, args);

@@ -40,14 +40,15 @@ void factor(int n, std::vector<int> &first, std::vector<int> &small) {
     // the table-driven odd stages go after the large ones, before the constant radices
     small.insert(small.begin(), mid.begin(), mid.end());
 }
-// Rader tables of the 113-point stage (stage_rader113 in fft.cuh), appended
-// after its cos/sin table: the FFT-112 of the Rader sequence
-// h[s] = exp(-+2 pi i g^s / 113) / 112 for the forward and the inverse
-// transform, the twiddles exp(-2 pi i m / 112), and the index pairs
-// (g^-q mod 113, g^q mod 113) stored as the bits of a float2; g = 3.
-void rader113_tables(std::vector<float2> &tab) {
-    constexpr int R = 113, M = 112, g = 3;
-    int gp[M], gi[M];
+// Rader tables of a prime stage R (stage_rader in fft.cuh; g a primitive
+// root mod R, 3 for 113 and 7 for 239), appended after its cos/sin table: the
+// FFT-M (M = R - 1) of the Rader sequence h[s] = exp(-+2 pi i g^s / R) / M for
+// the forward and the inverse transform, the twiddles exp(-2 pi i m / M), the
+// index pairs (g^-q mod R, g^q mod R) stored as the bits of a float2, and for
+// R = 239 the cos/sin table of its 17-point sub-transforms.
+void rader_tables(int R, int g, std::vector<float2> &tab) {
+    const int M = R - 1;
+    std::vector<int> gp(M), gi(M);
     int ginv = 1;
     for (int e = 0; e < R - 2; ++e) ginv = ginv * g % R;  // g^(R-2) = g^-1
     gp[0] = gi[0] = 1;
@@ -78,6 +79,11 @@ void rader113_tables(std::vector<float2> &tab) {
         memcpy(&e.y, &gp[q], sizeof(int));
         tab.push_back(e);
     }
+    if (R == 239)
+        for (int m = 0; m < 17; ++m) {
+            const double a = -2.0 * M_PI * (double)m / 17.0;
+            tab.push_back(make_float2((float)cos(a), (float)sin(a)));
+        }
 }
 }  // namespace
 
@@ -109,7 +115,8 @@ int mm_fft_plan_get(int n, FftPlan *out) {
             double a = -2.0 * M_PI * (double)m / (double)R;
             tab.push_back(make_float2((float)cos(a), (float)sin(a)));
         }
-        if (R == 113) rader113_tables(tab);
+        if (R == 113) rader_tables(113, 3, tab);
+        if (R == 239) rader_tables(239, 7, tab);
         Ns *= R;
         P.nst++;
     }
@@ -128,12 +135,12 @@ int mm_fft_plan_get(int n, FftPlan *out) {
         P.nst++;
     }
     // stage class (fft.cuh): 0 none, 63 lane primes 41..61, 127 also the lane
-    // primes 79, 89 and the Rader stage 113
+    // primes 79, 89 and the Rader stages 113 and 239
     P.lclass = 0;
     for (int i = 0; i < P.nst; ++i) {
         const int R = P.rad[i];
         if (R >= 41 && R <= 61 && P.lclass < 63) P.lclass = 63;
-        if (R == 79 || R == 89 || R == 113) P.lclass = 127;
+        if (R == 79 || R == 89 || R == 113 || R == 239) P.lclass = 127;
     }
     if (P.nst > MM_FFT_MAXST) {
         mm_set_error("FFT length %d needs too many stages", n);

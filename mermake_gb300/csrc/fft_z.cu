@@ -29,8 +29,7 @@ k_zpass(TileGeom g, float2 *__restrict__ S, const float2 *__restrict__ W, long l
     const int lnq = log2_pow2(kZq);
     const FftSmem L = fft_smem_layout(smem_raw, P, nl);
     // the Wiener chunk of the CTA's kZq positions (Zp x kZq), then the z map
-    float2 *Ws = reinterpret_cast<float2 *>(reinterpret_cast<unsigned char *>(L.scr) +
-                                            sizeof(float4) * MM_FFT_SCR_PER_WARP * (kZThreads / 32));
+    float2 *Ws = reinterpret_cast<float2 *>(L.scr + fft_scr_f4(P, nl, kZThreads / 32));
     int *zmap = reinterpret_cast<int *>(Ws + (size_t)n * kZq);
     fft_load_tables(P, L.tw, L.tab);
     for (int e = threadIdx.x; e < n; e += blockDim.x) zmap[e] = mm_map_z(e, g.Z, g.zpad, g.Zp);
@@ -115,7 +114,7 @@ int mm_launch_zpass(const TileGeom &g, float2 *S, const float2 *W, long long wst
     // lines per CTA: kZq positions of tg tiles (tg up to 4, one tile when each
     // tile has its own spectrum), fewer positions' worth of tiles if too large
     auto bytes = [&](int l) {
-        return fft_smem_bytes(P.n, P.ntab, l, kZThreads / 32) + sizeof(float2) * (size_t)P.n * kZq +
+        return fft_smem_bytes(P, l, kZThreads / 32) + sizeof(float2) * (size_t)P.n * kZq +
                sizeof(int) * (size_t)P.n;
     };
     int tg = 1;

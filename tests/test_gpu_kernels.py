@@ -25,7 +25,7 @@ def mm():
 # plus primes and composites around them
 FFT_LENGTHS = [1, 2, 3, 4, 5, 7, 8, 11, 13, 16, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 58, 59, 61, 67, 71, 73, 78,
                79, 83, 88, 89, 97, 98, 101, 103, 105, 107, 109, 113, 118, 121, 127, 131, 143, 148, 158, 178, 226,
-               238, 239, 256, 437, 478, 678, 1000, 1024, 1073, 2048, 2053]
+               238, 239, 256, 437, 478, 678, 717, 956, 1000, 1024, 1073, 2048, 2053]
 
 
 @pytest.mark.parametrize("n", FFT_LENGTHS)
