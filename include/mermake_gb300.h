@@ -86,27 +86,32 @@ int mm_median_f32(mm_ctx *ctx, const float *x, int64_t n, float *median, float *
 int mm_wiener_spectrum(mm_ctx *ctx, const float *psf, int pz, int px, int py, int tile_height, int tile_size,
                        int zpad, int overlap, float beta, void *W, void *stream);
 
-/* The z step of tile_wise for one spectrum as a matrix per frequency
- * (mermake/deconvolver.py:139-157: z padding by reflection, FFT over Zp, times
- * W, inverse FFT, keep planes [zpad, zpad + Z)).  No counterpart in the
- * reference, which transforms every tile over the padded depth.  Writes the
- * z kernel zop, (Zp, P, P/2+1) complex64 like W: the inverse DFT of W along
- * z, from which every entry of the Z x Z matrix of a frequency is a sum of at
- * most four samples.  Passing zop to mm_deconv_tiles / mm_hyb_spots /
- * mm_dapi_spots replaces the two padded-depth transforms of each tile by one
- * complex matrix product per frequency over the tiles of a batch (for batches
- * of at least 10 tiles; smaller batches keep the transforms).
- * tile_height <= 64 and Zp <= 400, and no plane copied more than four times
- * by the z padding (MM_EINVAL otherwise). */
+/* The z kernel of one spectrum, for the z step of tile_wise without the
+ * padded-depth transforms (mermake/deconvolver.py:139-157: z padding by
+ * reflection, FFT over Zp, times W, inverse FFT, keep planes
+ * [zpad, zpad + Z)).  No counterpart in the reference, which transforms every
+ * tile over the padded depth.  Writes zop, (Zp, P, P/2+1) complex64 like W:
+ * the inverse DFT of W along z, so that output plane i of a tile is
+ * sum_z zop[(zpad + i - z) mod Zp] x[map(z)] per frequency.  Passing zop
+ * (one kernel per spectrum, laid out like W) to mm_deconv_tiles /
+ * mm_hyb_spots / mm_dapi_spots replaces the two padded-depth transforms of
+ * each tile: with one spectrum and batches of at least 10 tiles by one Z x Z
+ * complex matrix per frequency over the batch (each entry a sum of at most
+ * four kernel samples; tile_height <= 64 and no plane copied more than four
+ * times by the padding), otherwise by that sum taken directly per tile
+ * (tile_height <= 128).  Zp <= 400 (MM_EINVAL otherwise). */
 int mm_wiener_zop(mm_ctx *ctx, const void *W, int tile_height, int zpad, int tile_size, int overlap, void *zop,
                   void *stream);
+
+/* 1 when mm_wiener_zop accepts (tile_height, zpad), else 0. */
+int mm_zkernel_supported(int tile_height, int zpad);
 
 /* Deconvolver.tile_wise / apply (mermake/deconvolver.py:98-184) for tiles
  * [tile_begin, tile_begin + tile_count) of the x-major tile grid of a
  * (Z, X, Y) channel, uint16 or float32 (image_dtype; strides isz, isx, 1).  flat: float32 (X, Y) with row stride fsx, or NULL.
  * W: npsf spectra as made by mm_wiener_spectrum (tile i uses spectrum i when
- * npsf > 1).  zop: NULL, or the z operator of W made by mm_wiener_zop
- * (npsf == 1 only).  blur_radius < 0: no background subtraction.
+ * npsf > 1).  zop: NULL, or the z kernels of the npsf spectra made by
+ * mm_wiener_zop, laid out like W.  blur_radius < 0: no background subtraction.
  * Outputs (any may be NULL):
  *   res_out    (tile_count, Z, P, P) float32: tile_res after blur subtraction;
  *              the yielded view is [:, :xend, :yend]

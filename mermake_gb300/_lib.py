@@ -50,6 +50,7 @@ _SIGS = {
     "mm_subtract_u16": ([_vp, _pi64, _vp, _pi64, _vp, _pi64, _i32, _pi64, _i32, _vp], _i32),
     "mm_wiener_spectrum": ([_vp, _vp, _i32, _i32, _i32, _i32, _i32, _i32, _i32, _f32, _vp, _vp], _i32),
     "mm_wiener_zop": ([_vp, _vp, _i32, _i32, _i32, _i32, _vp, _vp], _i32),
+    "mm_zkernel_supported": ([_i32, _i32], _i32),
     "mm_deconv_tiles": ([_vp, _vp, _i32, _i32, _i32, _i32, _i64, _i64, _vp, _i64, _vp, _i32, _vp] + [_i32] * 6
                         + [_vp, _vp, _vp, _i64, _i64, _vp], _i32),
     "mm_find_local_maxima": ([_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i32, _i64, _i64, _f32, _i32, _i32,

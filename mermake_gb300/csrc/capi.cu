@@ -203,10 +203,14 @@ int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *
         StageTimer t(c, ST_COLS_FWD, 2 * spec_b, st);
         if ((rc = mm_launch_cols(S, g.P, g.H, g.H, plane_c, g.nt * g.Z, false, st))) return rc;
     }
-    if (zop && g.nt >= MM_ZOP_MIN_TILES) {
+    if (zop && g.npsf == 1 && g.nt >= MM_ZOP_MIN_TILES && mm_zop_supported(g.Z, g.zpad)) {
         // the z kernel (Zp per frequency, the size of W) is read once per batch
         StageTimer t(c, ST_ZPASS, 2 * spec_b + 8.0 * wstride, st);
         if ((rc = mm_launch_zop_apply(S, zop, g.Z, g.zpad, g.Zp, plane_c, g.nt, st))) return rc;
+    } else if (zop && mm_zconv_supported(g.Z, g.zpad)) {
+        // each tile's z kernel read once (once per batch when shared)
+        StageTimer t(c, ST_ZPASS, 2 * spec_b + (g.npsf == 1 ? 8.0 * wstride : w_b), st);
+        if ((rc = mm_launch_zconv(S, zop, wstride, g.Z, g.zpad, g.Zp, plane_c, g.t0, g.nt, g.npsf, st))) return rc;
     } else {
         StageTimer t(c, ST_ZPASS, 2 * spec_b + w_b, st);
         if ((rc = mm_launch_zpass(g, S, W, wstride, st))) return rc;
@@ -301,7 +305,8 @@ int mm_wiener_zop(mm_ctx *c, const void *W, int tile_height, int zpad, int tile_
                   void *stream) {
     MM_REQUIRE(c && W && zop, "null argument");
     MM_REQUIRE(tile_height > 0 && tile_size > 0 && zpad >= 0 && overlap >= 0, "bad tile geometry");
-    MM_REQUIRE(tile_height <= MM_ZOP_MAX_Z, "z operator needs tile height <= %d", MM_ZOP_MAX_Z);
+    MM_REQUIRE(mm_zconv_supported(tile_height, zpad), "z kernel needs 1 <= zpad, tile height <= 128 and Zp <= %d",
+               MM_ZOP_MAX_ZP);
     std::lock_guard<std::mutex> lock(c->mu);
     cudaStream_t st = (cudaStream_t)stream;
     const int Zp = tile_height + 2 * zpad, P = tile_size + 2 * overlap;
@@ -309,6 +314,8 @@ int mm_wiener_zop(mm_ctx *c, const void *W, int tile_height, int zpad, int tile_
     StageTimer tm(c, ST_WIENER, 16.0 * Zp * plane, st);
     return mm_zker_build_impl((const float2 *)W, Zp, plane, (float2 *)zop, st);
 }
+
+int mm_zkernel_supported(int tile_height, int zpad) { return mm_zconv_supported(tile_height, zpad); }
 
 int mm_deconv_tiles(mm_ctx *c, const void *image, int image_dtype, int Z, int X, int Y, int64_t isz, int64_t isx,
                     const float *flat, int64_t fsx, const void *W, int npsf, const void *zop, int tile_size, int zpad,
@@ -318,7 +325,6 @@ int mm_deconv_tiles(mm_ctx *c, const void *image, int image_dtype, int Z, int X,
     TileGeom g;
     int rc = fill_geom(g, Z, X, Y, isz, isx, fsx, tile_size, zpad, overlap, npsf);
     if (rc) return rc;
-    MM_REQUIRE(!zop || npsf == 1, "a z operator needs a single spectrum (npsf == 1)");
     const int nt = ntiles_of(g);
     MM_REQUIRE(tile_begin >= 0 && tile_count >= 0 && tile_begin + tile_count <= nt,
                "tiles [%d, %d) outside the %d tiles of the channel", tile_begin, tile_begin + tile_count, nt);
@@ -387,7 +393,6 @@ int mm_hyb_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t 
     TileGeom g;
     int rc = fill_geom(g, Z, X, Y, isz, isx, fsx, tile_size, zpad, overlap, npsf);
     if (rc) return rc;
-    MM_REQUIRE(!zop || npsf == 1, "a z operator needs a single spectrum (npsf == 1)");
     const int nt = ntiles_of(g);
     if (batch <= 0) batch = nt;
     std::lock_guard<std::mutex> lock(c->mu);
@@ -457,7 +462,6 @@ int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t
     TileGeom g;
     int rc = fill_geom(g, Z, X, Y, isz, isx, fsx, tile_size, zpad, overlap, npsf);
     if (rc) return rc;
-    MM_REQUIRE(!zop || npsf == 1, "a z operator needs a single spectrum (npsf == 1)");
     const int nt = ntiles_of(g);
     if (batch <= 0) batch = nt;
     std::lock_guard<std::mutex> lock(c->mu);

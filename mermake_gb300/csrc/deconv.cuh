@@ -120,8 +120,10 @@ int mm_launch_cols(float2 *S, int n, long long se, int nlines, long long plane_s
                    bool inv, cudaStream_t st);
 int mm_launch_zpass(const TileGeom &g, float2 *S, const float2 *W, long long wstride, cudaStream_t st);
 
-// z pass as a matrix per frequency (zop.cu), single spectrum only: the z
-// kernel w (Zp, P, P/2+1) is the inverse DFT of W along z.
+// z pass from the z kernel w (Zp, P, P/2+1) per spectrum, the inverse DFT of
+// W along z (zop.cu): as a matrix per frequency over a batch that shares one
+// spectrum (mm_launch_zop_apply), or as the direct sum per tile
+// (mm_launch_zconv).
 // The z operator's cost per launch is dominated by summing M (Z x Z per
 // frequency) and hardly depends on the batch; below this many tiles the
 // padded-depth transforms are cheaper (about 0.4 ms per 678 x 678 tile
@@ -134,6 +136,9 @@ int mm_zop_supported(int Z, int zpad);
 int mm_zker_build_impl(const float2 *W, int Zp, long long plane, float2 *w, cudaStream_t st);
 int mm_launch_zop_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, long long plane, int nt,
                         cudaStream_t st);
+int mm_zconv_supported(int Z, int zpad);
+int mm_launch_zconv(float2 *S, const float2 *w, long long wstride, int Z, int zpad, int Zp, long long plane, int t0,
+                    int nt, int npsf, cudaStream_t st);
 int mm_launch_zfwd(float2 *S, int Zp, int plane, cudaStream_t st);
 int mm_launch_rows_inv(const float2 *S, int nrows, int P, int H, float *out, float *blur, int delta,
                        cudaStream_t st);

@@ -266,7 +266,121 @@ k_zop_apply(float2 *__restrict__ S, const float2 *__restrict__ w, int Z, int Zp,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Direct z convolution, for batches whose tiles each have their own spectrum
+// (a PSF grid) or are too few for the matrix form:
+//   Y[t][i][p] = sum_{z < Zp} w_t[(zpad + i - z) mod Zp][p] X[t][map_z(z)][p]
+// (map_z(z) < 0: a zero plane), with w_t the z kernel of tile t's spectrum.
+// A CTA owns kCq consecutive p (a lane each) of one tile; warp g computes the
+// outputs i in [g kCI, g kCI + kCI).  The CTA stages, for its p, the run of
+// the periodic z kernel its windows read (wx[u] = w[(u + zpad + 1 - Tpad)
+// mod Zp], so no index wraps) and the tile's Z planes plus a zero row, every
+// copy in flight at once (cp.async).  The z loop runs in
+// blocks of kCI planes: for a block the 2 kCI - 1 kernel values every output
+// of the thread needs are one contiguous run of wx, held in registers, so a
+// block costs kCI^2 complex FMAs for 3 kCI - 1 shared-memory loads.  Every
+// read of the tile's planes precedes the barrier and the CTAs own disjoint
+// (tile, p), so the update is in place.
+// ---------------------------------------------------------------------------
+constexpr int kCq = 32;
+constexpr int kCI = 8;
+constexpr int kConvMaxThreads = 512;  // 16 i-groups: Z <= 128
+
+// kernel rows a CTA reads: the windows of all its warps and z blocks form one
+// run of ceil(Z / kCI) kCI + Tpad - 1 consecutive rows of the periodic kernel
+__device__ __host__ __forceinline__ int zconv_tpad(int Zp) { return (Zp + kCI - 1) / kCI * kCI; }
+__device__ __host__ __forceinline__ int zconv_wx_rows(int Z, int Zp) {
+    return (Z + kCI - 1) / kCI * kCI + zconv_tpad(Zp) - 1;
+}
+
+__global__ void __launch_bounds__(kConvMaxThreads)
+k_zconv(float2 *__restrict__ S, const float2 *__restrict__ w, long long wstride, int Z, int zpad, int Zp,
+        long long plane, int t0, int npsf) {
+    extern __shared__ __align__(16) float2 sm[];
+    const int Lw = zconv_wx_rows(Z, Zp);
+    const int Tpad = zconv_tpad(Zp);
+    float2 *wx = sm;                                          // Lw x kCq
+    float2 *xs = wx + (size_t)Lw * kCq;                       // (Z + 1) x kCq, row Z zero
+    int *zm = reinterpret_cast<int *>(xs + (size_t)(Z + 1) * kCq);  // Tpad rows of xs
+    const int lane = threadIdx.x & 31, g = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const int t = blockIdx.y;
+    const long long p = (long long)blockIdx.x * kCq + lane;
+    const bool pv = p < plane;
+    const float2 *wp = w + (npsf == 1 ? 0 : (long long)(t0 + t)) * wstride;
+    float2 *Sp = S + (long long)t * Z * plane;
+    // all staging copies in flight at once (cp.async), then one wait
+    for (int u = g; u < Lw; u += nw) {
+        int d = (u + zpad + 1 - Tpad) % Zp;
+        if (d < 0) d += Zp;
+        if (pv)
+            cp_async8(&wx[u * kCq + lane], &wp[(long long)d * plane + p]);
+        else
+            wx[u * kCq + lane] = make_float2(0.f, 0.f);
+    }
+    for (int j = g; j <= Z; j += nw) {
+        if (j < Z && pv)
+            cp_async8(&xs[j * kCq + lane], &Sp[(long long)j * plane + p]);
+        else
+            xs[j * kCq + lane] = make_float2(0.f, 0.f);
+    }
+    for (int z = threadIdx.x; z < Tpad; z += blockDim.x) {
+        const int m = z < Zp ? mm_map_z(z, Z, zpad, Zp) : -1;
+        zm[z] = m < 0 ? Z : m;
+    }
+    cp_async_commit();
+    cp_async_wait_group<0>();
+    __syncthreads();
+    const int i0 = g * kCI;
+    if (i0 >= Z) return;
+    float2 acc[kCI];
+#pragma unroll
+    for (int a = 0; a < kCI; ++a) acc[a] = make_float2(0.f, 0.f);
+    for (int zb = 0; zb < Tpad; zb += kCI) {
+        // term (z = zb + s, i = i0 + a) uses w[(zpad + i - z) mod Zp] = wx[i0 - zb + Tpad - kCI + (kCI - 1 - s + a)]
+        float2 x[kCI], wr[2 * kCI - 1];
+#pragma unroll
+        for (int s = 0; s < kCI; ++s) x[s] = xs[zm[zb + s] * kCq + lane];
+        const float2 *wb = wx + (i0 - zb + Tpad - kCI) * kCq + lane;
+#pragma unroll
+        for (int r = 0; r < 2 * kCI - 1; ++r) wr[r] = wb[r * kCq];
+#pragma unroll
+        for (int s = 0; s < kCI; ++s)
+#pragma unroll
+            for (int a = 0; a < kCI; ++a) acc[a] = cfma(wr[kCI - 1 - s + a], x[s], acc[a]);
+    }
+    if (pv) {
+#pragma unroll
+        for (int a = 0; a < kCI; ++a)
+            if (i0 + a < Z) Sp[(long long)(i0 + a) * plane + p] = acc[a];
+    }
+}
+
 }  // namespace
+
+static size_t mm_zconv_smem(int Z, int Zp) {
+    return sizeof(float2) * ((size_t)zconv_wx_rows(Z, Zp) + Z + 1) * kCq + sizeof(int) * (size_t)zconv_tpad(Zp);
+}
+
+int mm_zconv_supported(int Z, int zpad) {
+    const int Zp = Z + 2 * zpad;
+    return Z >= 1 && zpad >= 1 && (Z + kCI - 1) / kCI * 32 <= kConvMaxThreads && Zp <= MM_ZOP_MAX_ZP &&
+           mm_zconv_smem(Z, Zp) <= 227 * 1024;
+}
+
+int mm_launch_zconv(float2 *S, const float2 *w, long long wstride, int Z, int zpad, int Zp, long long plane, int t0,
+                    int nt, int npsf, cudaStream_t st) {
+    MM_REQUIRE(Zp == Z + 2 * zpad && mm_zconv_supported(Z, zpad),
+               "z convolution needs Z <= %d and Zp <= %d (Z %d, zpad %d)", kConvMaxThreads / 32 * kCI, MM_ZOP_MAX_ZP,
+               Z, zpad);
+    if (nt <= 0) return MM_OK;
+    const size_t sm = mm_zconv_smem(Z, Zp);
+    MM_CUDA_TRY(cudaFuncSetAttribute(k_zconv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const int threads = (Z + kCI - 1) / kCI * 32;
+    dim3 grid((unsigned)((plane + kCq - 1) / kCq), (unsigned)nt);
+    k_zconv<<<grid, threads, sm, st>>>(S, w, wstride, Z, zpad, Zp, plane, t0, npsf);
+    MM_CHECK_LAUNCH();
+    return MM_OK;
+}
 
 int mm_zker_build_impl(const float2 *W, int Zp, long long plane, float2 *w, cudaStream_t st) {
     MM_REQUIRE(Zp >= 1 && Zp <= MM_ZOP_MAX_ZP, "z kernel needs 1 <= Zp <= %d (got %d)", MM_ZOP_MAX_ZP, Zp);

@@ -98,32 +98,27 @@ class Deconvolver:
         self.psf_fft = torch.view_as_complex(self.psf_fft)
         self.z_operator = None
         if self._want_z_operator(kwargs.get("z_operator")):
-            self.z_operator = torch.empty((self.Zp, self.P, self.H), dtype=torch.complex64, device="cuda")
-            _lib.check(L.mm_wiener_zop(ctx, _lib.ptr(self.psf_fft), self.tile_height, self.zpad, self.tile_size,
-                                       self.overlap, _lib.ptr(self.z_operator), st))
+            self.z_operator = torch.empty_like(self.psf_fft)
+            for i in range(self.psf_fft.shape[0]):
+                _lib.check(L.mm_wiener_zop(ctx, _lib.ptr(self.psf_fft[i]), self.tile_height, self.zpad,
+                                           self.tile_size, self.overlap, _lib.ptr(self.z_operator[i]), st))
         if self.tile_size:
             shape = (self.tile_height, self.P, self.P)
             self.tile_res = torch.empty(shape, dtype=torch.float32, device="cuda")
             self.tile_raw = torch.empty(shape, dtype=torch.float32, device="cuda")
 
-    # z operator: with one PSF, the z step of every tile is the same Z x Z
-    # complex matrix per (x, y) frequency, summed from the inverse DFT of the
-    # spectrum along z (csrc/zop.cu).  That kernel has the size of psf_fft and
-    # is kept beside it.
+    # z kernels: the z step of a tile (padding by reflection, transforms over
+    # Zp, times the spectrum, crop) is, per (x, y) frequency, a sum over the
+    # padded planes weighted by the inverse DFT of the spectrum along z
+    # (csrc/zop.cu).  One kernel per spectrum, the size of psf_fft, kept
+    # beside it.  With one PSF and batches of >= 10 tiles the sum runs as a
+    # Z x Z matrix per frequency over the batch; otherwise directly per tile.
     def _want_z_operator(self, request):
-        if request is False or self.psf_fft.shape[0] != 1 or not self.tile_size or self.zpad < 1:
-            return False
-        ok = self.tile_height <= 64 and self.Zp <= 400
-        if ok:
-            # every real plane is copied by at most four padded planes
-            mz = np.zeros(self.Zp, dtype=np.int32)
-            _lib.check(_lib.lib().mm_tile_geometry(self.tile_height, self.tile_size, self.tile_size, self.tile_size,
-                                                   self.zpad, self.overlap, 1, 0, None, mz.ctypes.data, None, None))
-            ok = np.bincount(mz[mz >= 0], minlength=1).max() <= 4
+        ok = bool(self.tile_size) and bool(_lib.lib().mm_zkernel_supported(self.tile_height, self.zpad))
         if request is True and not ok:
-            raise ValueError("z_operator needs tile height <= 64, padded depth <= 400 and at most four copies "
-                             "of a plane in the z padding")
-        return ok
+            raise ValueError("z_operator needs zpad >= 1, tile height <= 128 and padded depth <= 400 "
+                             "(with the z kernel's staging in shared memory)")
+        return ok and request is not False
 
     # -- geometry ------------------------------------------------------------
     def tile_boxes(self, shape):

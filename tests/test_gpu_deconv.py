@@ -186,3 +186,35 @@ def test_z_operator_matches_padded_transforms(dc, Z, zpad, ts, ov):
     b._call(u16(img), dc.MM_DTYPE_U16, None, 0, nt, 6, res_out=rb)
     err = float((ra - rb).abs().max() / rb.abs().max())
     assert err < 2e-5, err
+
+
+@pytest.mark.parametrize("Z,zpad,ts,ov,npsf,nx", [(13, 12, 10, 3, 1, 2), (40, 39, 12, 4, 4, 2), (7, 2, 15, 3, 9, 3),
+                                                  (5, 9, 10, 3, 6, 3), (80, 79, 8, 3, 1, 3), (128, 1, 8, 2, 4, 2),
+                                                  (50, 24, 30, 9, 25, 5)])
+def test_z_convolution_matches_padded_transforms(dc, Z, zpad, ts, ov, npsf, nx):
+    """The direct z convolution (each tile's own z kernel, summed over the
+    padded planes) against the FFT z pass over the padded depth: one PSF in
+    batches below the matrix form's 10 tiles, a PSF per tile, Z = 80 and 128
+    (past the matrix form's 64), zpad > Z, and 25 tiles of 25 PSFs."""
+    rng = np.random.default_rng(Z + npsf)
+    X = Y = nx * ts
+    img = rng.integers(100, 5000, (Z, X, Y)).astype(np.uint16)
+    psfs = {}
+    for k in range(npsf):
+        p = np.zeros((5, 5, 5), np.float32)
+        p[2, 2, 2] = 1.0
+        p[1:4, 1:4, 1:4] += 0.1 * rng.random((3, 3, 3)).astype(np.float32)
+        psfs[k] = p
+    psf = psfs if npsf > 1 else psfs[0]
+    args = dict(tile_size=ts, zpad=zpad, overlap=ov, beta=0.01)
+    a = dc.Deconvolver(psf, img.shape, z_operator=True, **args)
+    b = dc.Deconvolver(psf, img.shape, z_operator=False, **args)
+    assert a.z_operator.shape == a.psf_fft.shape
+    nt = a.n_tiles(img.shape)
+    assert npsf > 1 or nt < 10
+    ra = torch.empty((nt, Z, a.P, a.P), device="cuda")
+    rb = torch.empty_like(ra)
+    a._call(u16(img), dc.MM_DTYPE_U16, None, 0, nt, 6, res_out=ra)
+    b._call(u16(img), dc.MM_DTYPE_U16, None, 0, nt, 6, res_out=rb)
+    err = float((ra - rb).abs().max() / rb.abs().max())
+    assert err < 2e-5, err
