@@ -2,7 +2,7 @@
 """Benchmark of the per-FOV image path (deconv + blur + maxima + fit).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mermake_gb300|reference]
-                    [--workload fov3c|quad|grid25|psfgrid|tile|served|drift16]
+                    [--workload fov3c|quad|grid25|psfgrid|psfgrid9|tile|served|drift16]
                     [--form batched|plain] [--batch B]
 
 A step is one FOV of the workload, inputs resident in HBM:
@@ -19,6 +19,8 @@ A step is one FOV of the workload, inputs resident in HBM:
 * ``psfgrid``: one colour of 40 x 3000 x 3000 in tiles of 300 (padded 478),
   each of the 100 tiles with its own PSF from a 10 x 10 grid (sigma growing
   across the field), 60,000 puncta.
+* ``psfgrid9``: the same per-tile PSFs on 40 x 900 x 900 (3 x 3 tiles, 3 x 3
+  PSF grid): the small case for profiler captures of the PSF-grid kernels.
 * ``tile``: one smFISH tile, uint16 40 x 500 x 500, 2,000 puncta, no flat field.
 * ``served``: a Poisson stream of ``--fovs`` FOV requests over four FOV shapes
   (Z 30-60, XY 1024/2048, 1-3 colours + DAPI) through ``serve.FovServer``
@@ -70,6 +72,9 @@ WORKLOADS = {
     "psfgrid": dict(Z=40, X=3000, Y=3000, colours=1, puncta=60000, flat=False, dapi=False, nuclei=0, psf_grid=10,
                     hyb=dict(tile_size=300, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
                              delta_fit=3, sigmaZ=1, sigmaXY=1.5)),
+    "psfgrid9": dict(Z=40, X=900, Y=900, colours=1, puncta=5400, flat=False, dapi=False, nuclei=0, psf_grid=3,
+                     hyb=dict(tile_size=300, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
+                              delta_fit=3, sigmaZ=1, sigmaXY=1.5)),
     "tile": dict(Z=40, X=500, Y=500, colours=1, puncta=2000, flat=False, dapi=False, nuclei=0,
                  hyb=dict(tile_size=500, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
                           delta_fit=3, sigmaZ=1, sigmaXY=1.5)),

@@ -21,8 +21,10 @@
 
 namespace {
 
-constexpr int kThreads = kFftThreads;
+constexpr int kThreads = kFftThreads;  // k_rows_fwd_f32
 constexpr int kSmemLimit = kFftSmemLimit;
+constexpr FftCfg kRowsFwdCfg = kFftWide;  // its raw-row staging wants 2 nl rows per CTA
+constexpr FftCfg kRowsInvCfg = kFftPair;
 constexpr int kBlurThreads = 512;  // k_blur_x_sub, k_make_raw
 
 template <typename K>
@@ -181,7 +183,7 @@ __device__ __forceinline__ void rows_fwd_group(const TileGeom &g, const T *__res
 
 // persistent: the CTAs walk the groups (tables loaded once)
 template <typename T, int LMAX>
-__global__ void __launch_bounds__(kThreads, kFftCtasPerSm)
+__global__ void __launch_bounds__(kRowsFwdCfg.threads, kRowsFwdCfg.ctas)
 k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ flat,
                float2 *__restrict__ S, FftPlan P, int nl, int gx, int ngroups) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -196,7 +198,7 @@ k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ 
 
 // y pass, forward, dense f32 source (the padded PSF volume)
 template <int LMAX>
-__global__ void __launch_bounds__(kThreads, kFftCtasPerSm)
+__global__ void __launch_bounds__(kThreads)
 k_rows_fwd_f32(const float *__restrict__ vol, long long nrows, float2 *__restrict__ S, FftPlan P, int nl) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int n = P.n, H = n / 2 + 1;
@@ -312,7 +314,7 @@ __device__ __forceinline__ void rows_inv_group(const float2 *__restrict__ S, lon
 
 // persistent: the CTAs walk the row groups (tables loaded once)
 template <int LMAX>
-__global__ void __launch_bounds__(kThreads, kFftCtasPerSm)
+__global__ void __launch_bounds__(kRowsInvCfg.threads, kRowsInvCfg.ctas)
 k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restrict__ out,
            float *__restrict__ blur, int delta, FftPlan P, int nl, int ngroups) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -440,18 +442,18 @@ int mm_launch_rows_fwd_img(const TileGeom &g, const void *img, int dtype, const 
     if (rc) return rc;
     // lines per CTA, with room for the y map (P ints) after the scratch
     int nl = 16;
-    while (nl > 1 && fft_smem(P, nl) + sizeof(int) * P.n > (size_t)kSmemLimit) nl >>= 1;
-    size_t sm = fft_smem(P, nl) + sizeof(int) * P.n;
+    while (nl > 1 && fft_smem(P, nl, kRowsFwdCfg) + sizeof(int) * P.n > (size_t)fft_smem_limit(kRowsFwdCfg)) nl >>= 1;
+    size_t sm = fft_smem(P, nl, kRowsFwdCfg) + sizeof(int) * P.n;
     int gx = mm_cdiv((long)g.Z * g.P, 2 * nl);
     int ngroups = gx * g.nt;
-    dim3 grid(fft_grid(ngroups));
+    dim3 grid(fft_grid(ngroups, kRowsFwdCfg));
     TileGeom ga = g;
     const void *imga = img;
     const float *fa = flat;
     void *args[] = {&ga, &imga, &fa, &S, &P, &nl, &gx, &ngroups};
     const void *fn = dtype == MM_DTYPE_U16 ? MM_BY_CLASS(P, k_rows_fwd_img, uint16_t,)
                                           : MM_BY_CLASS(P, k_rows_fwd_img, float,);
-    return launch_fft_kernel(fn, grid, sm, st, args);
+    return launch_fft_kernel(fn, grid, sm, st, args, kRowsFwdCfg.threads);
 }
 
 int mm_launch_rows_fwd_f32(const float *vol, int nrows, int Pn, float2 *S, cudaStream_t st) {
@@ -472,18 +474,20 @@ int mm_launch_rows_inv(const float2 *S, int nrows, int Pn, int H, float *out, fl
     if (rc) return rc;
     // the y blur's reciprocal table goes in the scratch: room for 2 delta + 2 floats
     auto bytes = [&](int l) {
-        const size_t scr = sizeof(float4) * fft_scr_f4(P, l, kThreads / 32);
+        const size_t scr = sizeof(float4) * fft_scr_f4(P, l, kRowsInvCfg.threads / 32);
         const size_t rt = delta >= 0 ? sizeof(float) * (2 * (size_t)delta + 2) : 0;
-        return fft_smem(P, l) + (rt > scr ? ((rt - scr + 15) & ~(size_t)15) : 0);
+        return fft_smem(P, l, kRowsInvCfg) + (rt > scr ? ((rt - scr + 15) & ~(size_t)15) : 0);
     };
+    const size_t lim = (size_t)fft_smem_limit(kRowsInvCfg);
     int nl = 16;
-    while (nl > 1 && bytes(nl) > (size_t)kSmemLimit) nl >>= 1;
-    MM_REQUIRE(bytes(nl) <= (size_t)kSmemLimit, "blur radius %d too large for the tile", delta);
+    while (nl > 1 && bytes(nl) > lim) nl >>= 1;
+    MM_REQUIRE(bytes(nl) <= lim, "blur radius %d too large for the tile", delta);
     size_t sm = bytes(nl);
     long long nr = nrows;
     int ngroups = mm_cdiv(nrows, 2 * nl);
     void *args[] = {&S, &nr, &H, &out, &blur, &delta, &P, &nl, &ngroups};
-    return launch_fft_kernel(MM_BY_CLASS(P, k_rows_inv, ), dim3(fft_grid(ngroups)), sm, st, args);
+    return launch_fft_kernel(MM_BY_CLASS(P, k_rows_inv, ), dim3(fft_grid(ngroups, kRowsInvCfg)), sm, st, args,
+                             kRowsInvCfg.threads);
 }
 
 int mm_launch_blur_x_sub(const TileGeom &g, const float *res, const float *tmp, int delta, float *res_out,

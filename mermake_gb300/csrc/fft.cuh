@@ -836,18 +836,27 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 int mm_fft_plan_get(int n, FftPlan *out);
 
 // ---- launch helpers shared by the FFT kernel translation units -------------
-// kFftCtasPerSm CTAs of kFftThreads threads share an SM (228 KB of shared
-// memory, 1 KB of it reserved per CTA); the persistent passes launch that many
-// CTAs per SM.
-constexpr int kFftThreads = 512;
-constexpr int kFftCtasPerSm = 1;
-constexpr int kFftSmemLimit = (224 / kFftCtasPerSm) * 1024;
+// An FFT kernel runs `ctas` CTAs of `threads` threads per SM (228 KB of shared
+// memory, 1 KB of it reserved per CTA): one CTA of 512 ("wide") or two of 256
+// ("pair", so one CTA's barrier waits overlap the other's work).  The
+// persistent passes launch that many CTAs per SM; each kernel's
+// __launch_bounds__ names its layout.
+struct FftCfg {
+    int threads, ctas;
+};
+constexpr FftCfg kFftWide = {512, 1};
+constexpr FftCfg kFftPair = {256, 2};
+constexpr int kFftThreads = kFftWide.threads;  // the non-persistent FFT kernels
+constexpr int kFftSmemLimit = 224 * 1024;
+constexpr int fft_smem_limit(FftCfg c) { return (224 / c.ctas) * 1024; }
 
-static inline size_t fft_smem(const FftPlan &P, int nl) { return fft_smem_bytes(P, nl, kFftThreads / 32); }
+static inline size_t fft_smem(const FftPlan &P, int nl, FftCfg c = kFftWide) {
+    return fft_smem_bytes(P, nl, c.threads / 32);
+}
 // Lines per CTA: the largest power of two <= maxnl whose buffers fit the budget.
-static inline int pick_nl(const FftPlan &P, int maxnl) {
+static inline int pick_nl(const FftPlan &P, int maxnl, FftCfg c = kFftWide) {
     int nl = maxnl;
-    while (nl > 1 && fft_smem(P, nl) > (size_t)kFftSmemLimit) nl >>= 1;
+    while (nl > 1 && fft_smem(P, nl, c) > (size_t)fft_smem_limit(c)) nl >>= 1;
     return nl;
 }
 // Pointer to the kernel template instantiation of the plan's lane class.
@@ -870,14 +879,15 @@ static inline int mm_sm_count() {
 }
 
 // CTAs of a persistent pass over ngroups line groups
-static inline unsigned fft_grid(long long ngroups) {
-    const long long cap = (long long)mm_sm_count() * kFftCtasPerSm;
+static inline unsigned fft_grid(long long ngroups, FftCfg c) {
+    const long long cap = (long long)mm_sm_count() * c.ctas;
     return (unsigned)(ngroups < cap ? ngroups : cap);
 }
 
-static inline int launch_fft_kernel(const void *fn, dim3 grid, size_t sm, cudaStream_t st, void **args) {
+static inline int launch_fft_kernel(const void *fn, dim3 grid, size_t sm, cudaStream_t st, void **args,
+                                    int threads = kFftThreads) {
     MM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    MM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(kFftThreads), args, sm, st));
+    MM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(threads), args, sm, st));
     mm_launch_counter_add();
     return MM_OK;
 }

@@ -3,8 +3,7 @@
 #include "deconv.cuh"
 
 namespace {
-constexpr int kThreads = kFftThreads;
-constexpr int kSmemLimit = kFftSmemLimit;
+constexpr FftCfg kColsCfg = kFftPair;
 
 // ---------------------------------------------------------------------------
 // strided complex FFT, in place: line l of plane p starts at S + p*plane_stride + l,
@@ -12,7 +11,7 @@ constexpr int kSmemLimit = kFftSmemLimit;
 // staged into shared memory with cp.async.
 // ---------------------------------------------------------------------------
 template <bool INV, int LMAX>
-__global__ void __launch_bounds__(kThreads, kFftCtasPerSm)
+__global__ void __launch_bounds__(kColsCfg.threads, kColsCfg.ctas)
 k_cols(float2 *__restrict__ S, long long se, int nlines, long long plane_stride, FftPlan P, int nl, int gx,
        int ngroups) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -49,14 +48,14 @@ int mm_launch_cols(float2 *S, int n, long long se, int nlines, long long plane_s
     FftPlan P;
     int rc = mm_fft_plan_get(n, &P);
     if (rc) return rc;
-    int nl = pick_nl(P, 16);
-    size_t sm = fft_smem(P, nl);
+    int nl = pick_nl(P, 16, kColsCfg);
+    size_t sm = fft_smem(P, nl, kColsCfg);
     int gx = mm_cdiv(nlines, nl);
     int ngroups = gx * nplanes;
-    // persistent: kFftCtasPerSm CTAs per SM (their line buffers fill its shared memory)
-    dim3 grid(fft_grid(ngroups));
+    // persistent: kColsCfg.ctas CTAs per SM (their line buffers fill its shared memory)
+    dim3 grid(fft_grid(ngroups, kColsCfg));
     void *args[] = {&S, &se, &nlines, &plane_stride, &P, &nl, &gx, &ngroups};
     const void *fn = inv ? MM_BY_CLASS(P, k_cols, true,) : MM_BY_CLASS(P, k_cols, false,);
-    return launch_fft_kernel(fn, grid, sm, st, args);
+    return launch_fft_kernel(fn, grid, sm, st, args, kColsCfg.threads);
 }
 
