@@ -161,23 +161,25 @@ __device__ __forceinline__ void rows_fwd_group(const TileGeom &g, const T *__res
     __syncthreads();
     float2 *R = fft_lines<false, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
 
-    // unpack the two real rows of each line into their spectrum rows z P + x
+    // unpack the two real rows of each line into their spectrum rows z P + x;
+    // the spectrum row of each of the 2 nl rows goes in the (now idle) y map
     const int H = g.H;
     const float invH = 1.0f / (float)H;
     float2 *Sb = S + (long long)by * nrows * H;
+    int *drow = ymap;
+    if (threadIdx.x < 2 * nl) {
+        const long long r = row0 + threadIdx.x;
+        const int xp = (int)(r / g.Z);
+        drow[threadIdx.x] = r < nrows ? (int)(r - (long long)xp * g.Z) * g.P + xp : -1;
+    }
+    __syncthreads();
     for (int it = threadIdx.x; it < nl * H; it += blockDim.x) {
         const int l = fdiv_i(it, H, invH), k = it - l * H;
-        const long long r0 = row0 + 2 * l, r1 = r0 + 1;
         const float2 ck = R[sidx(k, l, nl)];
-        const float2 cn = R[sidx((n - k) % n, l, nl)];
-        if (r0 < nrows) {
-            const long long xp = r0 / g.Z;
-            Sb[((r0 - xp * g.Z) * g.P + xp) * H + k] = make_float2(0.5f * (ck.x + cn.x), 0.5f * (ck.y - cn.y));
-        }
-        if (r1 < nrows) {
-            const long long xp = r1 / g.Z;
-            Sb[((r1 - xp * g.Z) * g.P + xp) * H + k] = make_float2(0.5f * (ck.y + cn.y), -0.5f * (ck.x - cn.x));
-        }
+        const float2 cn = R[sidx(k == 0 ? 0 : n - k, l, nl)];
+        const int d0 = drow[2 * l], d1 = drow[2 * l + 1];
+        if (d0 >= 0) Sb[(long long)d0 * H + k] = make_float2(0.5f * (ck.x + cn.x), 0.5f * (ck.y - cn.y));
+        if (d1 >= 0) Sb[(long long)d1 * H + k] = make_float2(0.5f * (ck.y + cn.y), -0.5f * (ck.x - cn.x));
     }
 }
 
@@ -218,7 +220,7 @@ k_rows_fwd_f32(const float *__restrict__ vol, long long nrows, float2 *__restric
         const int l = fdiv_i(it, H, invH), k = it - l * H;
         const long long r0 = row0 + 2 * l;
         const float2 ck = R[sidx(k, l, nl)];
-        const float2 cn = R[sidx((n - k) % n, l, nl)];
+        const float2 cn = R[sidx(k == 0 ? 0 : n - k, l, nl)];
         if (r0 < nrows) S[r0 * H + k] = make_float2(0.5f * (ck.x + cn.x), 0.5f * (ck.y - cn.y));
         if (r0 + 1 < nrows) S[(r0 + 1) * H + k] = make_float2(0.5f * (ck.y + cn.y), -0.5f * (ck.x - cn.x));
     }
@@ -440,10 +442,12 @@ int mm_launch_rows_fwd_img(const TileGeom &g, const void *img, int dtype, const 
     FftPlan P;
     int rc = mm_fft_plan_get(g.P, &P);
     if (rc) return rc;
-    // lines per CTA, with room for the y map (P ints) after the scratch
+    // lines per CTA, with room after the scratch for the y map (P ints), which
+    // later holds the spectrum rows of the CTA's 2 nl <= 32 rows
+    const size_t mapb = sizeof(int) * (size_t)(P.n > 32 ? P.n : 32);
     int nl = 16;
-    while (nl > 1 && fft_smem(P, nl, kRowsFwdCfg) + sizeof(int) * P.n > (size_t)fft_smem_limit(kRowsFwdCfg)) nl >>= 1;
-    size_t sm = fft_smem(P, nl, kRowsFwdCfg) + sizeof(int) * P.n;
+    while (nl > 1 && fft_smem(P, nl, kRowsFwdCfg) + mapb > (size_t)fft_smem_limit(kRowsFwdCfg)) nl >>= 1;
+    size_t sm = fft_smem(P, nl, kRowsFwdCfg) + mapb;
     int gx = mm_cdiv((long)g.Z * g.P, 2 * nl);
     int ngroups = gx * g.nt;
     dim3 grid(fft_grid(ngroups, kRowsFwdCfg));

@@ -283,7 +283,7 @@ k_zop_apply(float2 *__restrict__ S, const float2 *__restrict__ w, int Z, int Zp,
 // (tile, p), so the update is in place.
 // ---------------------------------------------------------------------------
 constexpr int kCq = 32;
-constexpr int kCI = 8;
+constexpr int kCI = 8;  // the plane map is read as int4 pairs below
 constexpr int kConvMaxThreads = 512;  // 16 i-groups: Z <= 128
 
 // kernel rows a CTA reads: the windows of all its warps and z blocks form one
@@ -338,8 +338,12 @@ k_zconv(float2 *__restrict__ S, const float2 *__restrict__ w, long long wstride,
     for (int zb = 0; zb < Tpad; zb += kCI) {
         // term (z = zb + s, i = i0 + a) uses w[(zpad + i - z) mod Zp] = wx[i0 - zb + Tpad - kCI + (kCI - 1 - s + a)]
         float2 x[kCI], wr[2 * kCI - 1];
+        // the block's plane map as two 16-byte broadcasts (zb is a multiple of
+        // kCI = 8 and zm starts on a 256-byte boundary)
+        const int4 m0 = *reinterpret_cast<const int4 *>(zm + zb), m1 = *reinterpret_cast<const int4 *>(zm + zb + 4);
+        const int mz[kCI] = {m0.x, m0.y, m0.z, m0.w, m1.x, m1.y, m1.z, m1.w};
 #pragma unroll
-        for (int s = 0; s < kCI; ++s) x[s] = xs[zm[zb + s] * kCq + lane];
+        for (int s = 0; s < kCI; ++s) x[s] = xs[mz[s] * kCq + lane];
         const float2 *wb = wx + (i0 - zb + Tpad - kCI) * kCq + lane;
 #pragma unroll
         for (int r = 0; r < 2 * kCI - 1; ++r) wr[r] = wb[r * kCq];
