@@ -2,7 +2,7 @@
 """Benchmark of the per-FOV image path (deconv + blur + maxima + fit).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mermake_gb300|reference]
-                    [--workload fov3c|quad|grid25|psfgrid|psfgrid9|tile|served|drift16]
+                    [--workload fov3c|quad|ten|grid25|psfgrid|psfgrid9|tile|served|drift16]
                     [--form batched|plain] [--batch B]
 
 A step is one FOV of the workload, inputs resident in HBM:
@@ -14,6 +14,9 @@ A step is one FOV of the workload, inputs resident in HBM:
   threshold 3.0, delta 5, fit 5, zpad 24.
 * ``quad``: one colour of 50 x 1000 x 1000 (2 x 2 tiles), 10,000 puncta, flat
   field: the small case for profiler captures (spectra larger than L2).
+* ``ten``: one colour of 50 x 1000 x 2500 (2 x 5 tiles of 500), flat field:
+  the smallest batch that runs the z operator, for DRAM-traffic captures of
+  every stage of the ``fov3c`` kernels (about 3 GB on the device).
 * ``grid25``: one colour of 50 x 1000 x 1000 in 5 x 5 tiles of 200 (padded
   378): a 25-tile batch, like a colour of ``fov3c``, in a few GB.
 * ``psfgrid``: one colour of 40 x 3000 x 3000 in tiles of 300 (padded 478),
@@ -22,10 +25,12 @@ A step is one FOV of the workload, inputs resident in HBM:
 * ``psfgrid9``: the same per-tile PSFs on 40 x 900 x 900 (3 x 3 tiles, 3 x 3
   PSF grid): the small case for profiler captures of the PSF-grid kernels.
 * ``tile``: one smFISH tile, uint16 40 x 500 x 500, 2,000 puncta, no flat field.
-* ``served``: a Poisson stream of ``--fovs`` FOV requests over four FOV shapes
-  (Z 30-60, XY 1024/2048, 1-3 colours + DAPI) through ``serve.FovServer``
-  (continuous batching under a 120 GB budget); reports stream voxels/s and
-  p50/p99 request latency.
+* ``served``: a Poisson stream (mean ``--interval``, 1.5 s) of ``--fovs``
+  requests over 20 FOV ids whose shapes are drawn once per id (Z in
+  {30, 40, 60, 80}, XY in {1024, 2048, 3000}, 1-4 colours + DAPI; FOV id =
+  i mod 20, round = i div 20, later rounds drift-aligned against round 0)
+  through ``serve.FovServer`` (continuous batching under a 120 GB budget);
+  reports stream voxels/s and p50/p99 request latency.
 * ``drift16``: 16 DAPI rounds of one 50 x 2048 x 2048 field drifted by known
   shifts (+-3 z, +-20 x/y, sub-pixel), each deconvolved, spot-called and
   aligned against round 0's resident maxima; reports rounds/s and the error
@@ -66,6 +71,9 @@ WORKLOADS = {
     "quad": dict(Z=50, X=1000, Y=1000, colours=1, puncta=10000, flat=True, dapi=False, nuclei=0,
                  hyb=dict(tile_size=500, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
                           delta_fit=3, sigmaZ=1, sigmaXY=1.5)),
+    "ten": dict(Z=50, X=1000, Y=2500, colours=1, puncta=25000, flat=True, dapi=False, nuclei=0,
+                hyb=dict(tile_size=500, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
+                         delta_fit=3, sigmaZ=1, sigmaXY=1.5)),
     "grid25": dict(Z=50, X=1000, Y=1000, colours=1, puncta=10000, flat=True, dapi=False, nuclei=0,
                    hyb=dict(tile_size=200, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
                             delta_fit=3, sigmaZ=1, sigmaXY=1.5)),
@@ -88,8 +96,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mermake_gb300", choices=["mermake_gb300", "reference"])
     ap.add_argument("--workload", default="fov3c", choices=sorted(WORKLOADS) + ["served", "drift16"])
-    ap.add_argument("--fovs", type=int, default=16, help="served: number of FOV requests in the stream")
-    ap.add_argument("--interval", type=float, default=0.25, help="served: mean Poisson arrival interval (s)")
+    ap.add_argument("--fovs", type=int, default=40,
+                    help="served: requests in the stream (FOV id = i mod 20, round = i div 20)")
+    ap.add_argument("--interval", type=float, default=1.5, help="served: mean Poisson arrival interval (s)")
     ap.add_argument("--workers", type=int, default=2, help="served: concurrent requests on the device")
     ap.add_argument("--form", default="batched", choices=["batched", "plain"])
     ap.add_argument("--batch", type=int, default=0,
@@ -312,7 +321,7 @@ def gpu_arm(args, rank, world, local):
     # DRAM traffic of the dominant kernel per launch: ncu's bytes per tile on
     # the quad workload, scaled by the tiles one launch of this run processes
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "dram_traffic_quad.json")
+    tp = os.path.join(ROOT, "profiles", "dram_traffic_ten.json")
     if os.path.exists(tp):
         e = json.load(open(tp))["stages"].get(dom)
         if e:
@@ -346,7 +355,7 @@ def gpu_arm(args, rank, world, local):
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
-                     "traffic_source": "profiles/dram_traffic_quad.json scaled by tiles per launch" if traffic else None,
+                     "traffic_source": "profiles/dram_traffic_ten.json scaled by tiles per launch" if traffic else None,
                      "bytes_per_launch": dbytes / dl, "ms_per_launch": dms / dl,
                      "stage_share": stage_share},
         "clocks": clk.summary(),
@@ -512,8 +521,16 @@ def reference_arm(args, rank, world):
 # ---------------------------------------------------------------------------
 # served form: a Poisson stream of mixed-shape FOVs through serve.FovServer
 # ---------------------------------------------------------------------------
-SERVED_FOVS = [  # (Z, X, Y, colours) per FOV id, from the mixed-shape stream's ranges
-    (30, 1024, 1024, 1), (40, 2048, 2048, 3), (60, 1024, 1024, 2), (50, 2048, 2048, 3)]
+def served_fovs(n=20, seed=4):
+    """(Z, X, Y, colours) of the stream's FOV ids, drawn once per id: Z in
+    {30, 40, 60, 80}, XY in {1024, 2048, 3000}, 1-4 colours (plus DAPI)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        xy = int(rng.choice((1024, 2048, 3000)))
+        out.append((int(rng.choice((30, 40, 60, 80))), xy, xy, int(rng.integers(1, 5))))
+    return out
 
 
 def served_arm(args, local):
@@ -525,8 +542,9 @@ def served_arm(args, local):
     hyb = dict(WORKLOADS["fov3c"]["hyb"])
     dap = dict(WORKLOADS["fov3c"]["dapi_args"])
     psf = synth.gaussian_psf((40, 40, 40), 2.0, 1.3)
+    fovs = served_fovs()
     data = []
-    for f, (Z, X, Y, nc) in enumerate(SERVED_FOVS):
+    for f, (Z, X, Y, nc) in enumerate(fovs):
         dapi = synth.dapi_stack(Z, X, Y, 500 + f, device="cuda", n_nuclei=max(20, 300 * X * Y // 2048 ** 2))
         gain = synth.flat_gain(X, Y)
         cols = [synth.hyb_stack(Z, X, Y, 40000 * X * Y // 2048 ** 2, 600 + 7 * f + c, device="cuda", gain=gain)
@@ -535,7 +553,7 @@ def served_arm(args, local):
                          flats=[torch.from_numpy(gain).cuda() for _ in cols]))
         del dapi, cols
     rng = np.random.default_rng(7)
-    nf = len(SERVED_FOVS)
+    nf = len(fovs)
     reqs = [dict(fov=i % nf, round=i // nf, **data[i % nf]) for i in range(args.fovs)]
     vox = [sum(int(np.prod(a.shape)) for a in [r["dapi"]] + r["colours"]) for r in reqs]
     gaps = rng.exponential(args.interval, size=len(reqs))
@@ -571,14 +589,15 @@ def served_arm(args, local):
         "vs_baseline": None,
         "dtype": "f32",
         "data": "synthetic (seeded Poisson background + Gaussian puncta / nuclei), %d FOV shapes" % nf,
-        "config": {"workload": "served", "fovs": [list(f) for f in SERVED_FOVS], "requests": len(reqs),
+        "config": {"workload": "served", "fovs": [list(f) for f in fovs], "requests": len(reqs),
                    "mean_interval_s": args.interval, "workers": args.workers, "hbm_budget_gb": 120,
                    "peak_in_flight": peak, "tile_size": hyb["tile_size"], "overlap": hyb["overlap"]},
         "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": lat[-1]},
         "service_ms": {"p50": pct(svc, 50), "p99": pct(svc, 99)},
         "queue_ms": {"p50": pct(que, 50), "p99": pct(que, 99)},
-        "per_shape_service_ms": {str(list(SERVED_FOVS[f][:3])): round(statistics.median(
-            1e3 * (x.done - x.admitted) for x in res if x.request.fov == f), 1) for f in range(nf)},
+        "per_fov_service_ms": {"%d: %s" % (f, list(fovs[f])): round(statistics.median(
+            1e3 * (x.done - x.admitted) for x in res if x.request.fov == f), 1)
+            for f in range(nf) if any(x.request.fov == f for x in res)},
         "drift_px": [float(np.abs(np.asarray(x.drift[0])).max()) for x in res if x.drift is not None][:8],
         "clocks": clk.summary(),
     }
