@@ -42,11 +42,12 @@ int set_smem(K *kernel, size_t bytes) {
 // the flat), so the gathers do not stall on global latency row by row.
 // float32 tiles gather straight from global memory.
 // ---------------------------------------------------------------------------
-template <typename T, int LMAX>
+template <typename T, int LMAX, int NF, int NLF>
 __device__ __forceinline__ void rows_fwd_group(const TileGeom &g, const T *__restrict__ img,
                                                const float *__restrict__ flat, float2 *__restrict__ S,
                                                const FftPlan &P, int nl, const FftSmem &L, int bx, int by) {
-    const int n = P.n;
+    if constexpr (NF > 0) nl = NLF;
+    const int n = NF > 0 ? NF : P.n;
     const int ti = g.t0 + by;
     const TileDesc d = mm_tile_desc(g, ti);
     const long long nrows = (long long)g.Z * g.P;
@@ -159,11 +160,11 @@ __device__ __forceinline__ void rows_fwd_group(const TileGeom &g, const T *__res
         }
     }
     __syncthreads();
-    float2 *R = fft_lines<false, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
+    float2 *R = fft_run<false, LMAX, NF, NLF>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
 
     // unpack the two real rows of each line into their spectrum rows z P + x;
     // the spectrum row of each of the 2 nl rows goes in the (now idle) y map
-    const int H = g.H;
+    const int H = NF > 0 ? NF / 2 + 1 : g.H;
     const float invH = 1.0f / (float)H;
     float2 *Sb = S + (long long)by * nrows * H;
     int *drow = ymap;
@@ -183,8 +184,9 @@ __device__ __forceinline__ void rows_fwd_group(const TileGeom &g, const T *__res
     }
 }
 
-// persistent: the CTAs walk the groups (tables loaded once)
-template <typename T, int LMAX>
+// persistent: the CTAs walk the groups (tables loaded once); NF > 0: the
+// engine specialised for length NF at NLF lines per CTA
+template <typename T, int LMAX, int NF = 0, int NLF = 0>
 __global__ void __launch_bounds__(kRowsFwdCfg.threads, kRowsFwdCfg.ctas)
 k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ flat,
                float2 *__restrict__ S, FftPlan P, int nl, int gx, int ngroups) {
@@ -193,7 +195,7 @@ k_rows_fwd_img(TileGeom g, const T *__restrict__ img, const float *__restrict__ 
     fft_load_tables(P, L.tw, L.tab);
     for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
         const int by = grp / gx;
-        rows_fwd_group<T, LMAX>(g, img, flat, S, P, nl, L, grp - by * gx, by);
+        rows_fwd_group<T, LMAX, NF, NLF>(g, img, flat, S, P, nl, L, grp - by * gx, by);
         __syncthreads();
     }
 }
@@ -233,11 +235,15 @@ k_rows_fwd_f32(const float *__restrict__ vol, long long nrows, float2 *__restric
 // in-range count) is written to `blur` as well: each lane slides a window
 // over a contiguous segment of the row held in shared memory.
 // ---------------------------------------------------------------------------
-template <int LMAX>
+template <int LMAX, int NF, int NLF>
 __device__ __forceinline__ void rows_inv_group(const float2 *__restrict__ S, long long nrows, int H,
                                                float *__restrict__ out, float *__restrict__ blur, int delta,
                                                const FftPlan &P, int nl, const FftSmem &L, int bx) {
-    const int n = P.n;
+    if constexpr (NF > 0) {
+        nl = NLF;
+        H = NF / 2 + 1;
+    }
+    const int n = NF > 0 ? NF : P.n;
     const long long row0 = (long long)bx * 2 * nl;
     const bool even = (n % 2) == 0;
     const float invH = 1.0f / (float)H, invn = 1.0f / (float)n;
@@ -269,7 +275,7 @@ __device__ __forceinline__ void rows_inv_group(const float2 *__restrict__ S, lon
         }
     }
     __syncthreads();
-    float2 *R = fft_lines<true, LMAX>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
+    float2 *R = fft_run<true, LMAX, NF, NLF>(L.A, L.B, nl, P, L.tw, L.tab, L.scr);
     const float *Rf = reinterpret_cast<const float *>(R);
     for (int it = threadIdx.x; it < 2 * nl * n; it += blockDim.x) {
         const int q = fdiv_i(it, n, invn), e = it - q * n;
@@ -314,8 +320,9 @@ __device__ __forceinline__ void rows_inv_group(const float2 *__restrict__ S, lon
     }
 }
 
-// persistent: the CTAs walk the row groups (tables loaded once)
-template <int LMAX>
+// persistent: the CTAs walk the row groups (tables loaded once); NF > 0 as
+// for k_rows_fwd_img
+template <int LMAX, int NF = 0, int NLF = 0>
 __global__ void __launch_bounds__(kRowsInvCfg.threads, kRowsInvCfg.ctas)
 k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restrict__ out,
            float *__restrict__ blur, int delta, FftPlan P, int nl, int ngroups) {
@@ -323,7 +330,7 @@ k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restri
     const FftSmem L = fft_smem_layout(smem_raw, P, nl);
     fft_load_tables(P, L.tw, L.tab);
     for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
-        rows_inv_group<LMAX>(S, nrows, H, out, blur, delta, P, nl, L, grp);
+        rows_inv_group<LMAX, NF, NLF>(S, nrows, H, out, blur, delta, P, nl, L, grp);
         __syncthreads();
     }
 }
@@ -455,8 +462,8 @@ int mm_launch_rows_fwd_img(const TileGeom &g, const void *img, int dtype, const 
     const void *imga = img;
     const float *fa = flat;
     void *args[] = {&ga, &imga, &fa, &S, &P, &nl, &gx, &ngroups};
-    const void *fn = dtype == MM_DTYPE_U16 ? MM_BY_CLASS(P, k_rows_fwd_img, uint16_t,)
-                                          : MM_BY_CLASS(P, k_rows_fwd_img, float,);
+    const void *fn = dtype == MM_DTYPE_U16 ? MM_FFT_KERNEL(P, nl, 16, k_rows_fwd_img, uint16_t,)
+                                          : MM_FFT_KERNEL(P, nl, 16, k_rows_fwd_img, float,);
     return launch_fft_kernel(fn, grid, sm, st, args, kRowsFwdCfg.threads);
 }
 
@@ -490,7 +497,7 @@ int mm_launch_rows_inv(const float2 *S, int nrows, int Pn, int H, float *out, fl
     long long nr = nrows;
     int ngroups = mm_cdiv(nrows, 2 * nl);
     void *args[] = {&S, &nr, &H, &out, &blur, &delta, &P, &nl, &ngroups};
-    return launch_fft_kernel(MM_BY_CLASS(P, k_rows_inv, ), dim3(fft_grid(ngroups, kRowsInvCfg)), sm, st, args,
+    return launch_fft_kernel(MM_FFT_KERNEL(P, nl, 8, k_rows_inv, ), dim3(fft_grid(ngroups, kRowsInvCfg)), sm, st, args,
                              kRowsInvCfg.threads);
 }
 

@@ -59,6 +59,17 @@ __device__ __forceinline__ int fdiv_i(int a, int d, float inv) {
     return q;
 }
 __device__ __forceinline__ int log2_pow2(int nl) { return __ffs(nl) - 1; }
+constexpr int ilog2c(int v) { return v <= 1 ? 0 : 1 + ilog2c(v / 2); }
+
+// a / d for 0 <= a: by the constant C when the caller knows d at compile time
+// (C > 0: a multiply and a shift), else through the reciprocal (fdiv_i)
+template <int C>
+__device__ __forceinline__ int divc(int a, int d, float inv) {
+    if constexpr (C > 0)
+        return (int)((unsigned)a / (unsigned)C);
+    else
+        return fdiv_i(a, d, inv);
+}
 
 // ---- small radices, all values in registers ------------------------------
 template <bool INV>
@@ -547,15 +558,21 @@ __device__ __forceinline__ void rader_dft(float2 *v, const float *c, const float
 // tb: the stage's table (cos/sin of R, then the Rader tables of fft_plan.cu:
 // FFT of h forward and inverse, wM, the (g^-q, g^q) index pairs, and for
 // N2 = 17 the cos/sin of 17).
-template <int R, int N1, int N2, bool INV>
+// NC, NLC, NSC > 0: the line length, lines per CTA and Ns known at compile
+// time (the specialised engine, fft_lines_fixed), so the index arithmetic folds.
+template <int R, int N1, int N2, bool INV, int NC = 0, int NLC = 0, int NSC = 0>
 __device__ __noinline__ void stage_rader(float2 *__restrict__ src, float2 *__restrict__ dst, int n, int nl,
                                          int Ns, const float2 *__restrict__ tw, const float2 *__restrict__ tb,
                                          float4 *__restrict__ scr_all) {
     constexpr int M = R - 1;
     static_assert(N1 * N2 == M, "Rader split must cover R - 1");
+    if constexpr (NC > 0) n = NC;
+    if constexpr (NLC > 0) nl = NLC;
+    if constexpr (NSC > 0) Ns = NSC;
+    constexpr int NBC = (NC > 0 && NLC > 0) ? NC / R * NLC : 0;
     const int m = n / R, nb = m * nl;
     const int tstep = n / (Ns * R);
-    const int lnl = log2_pow2(nl);
+    const int lnl = NLC > 0 ? ilog2c(NLC) : log2_pow2(nl);
     const float invNs = 1.0f / (float)Ns, invnb = 1.0f / (float)nb;
     const float2 *Hh = tb + R + (INV ? M : 0);
     const float2 *wM = tb + R + 2 * M;
@@ -574,9 +591,9 @@ __device__ __noinline__ void stage_rader(float2 *__restrict__ src, float2 *__res
     float2 *T = dst;
 
     for (int e = threadIdx.x; e < N1 * nb; e += blockDim.x) {
-        const int q1 = fdiv_i(e, nb, invnb), b = e - q1 * nb;
+        const int q1 = divc<NBC>(e, nb, invnb), b = e - q1 * nb;
         const int l = b & (nl - 1), j = b >> lnl;
-        const int kk = Ns > 1 ? j - fdiv_i(j, Ns, invNs) * Ns : 0;
+        const int kk = Ns > 1 ? j - divc<NSC>(j, Ns, invNs) * Ns : 0;
         float2 v[N2];
 #pragma unroll
         for (int q2 = 0; q2 < N2; ++q2) {
@@ -596,7 +613,7 @@ __device__ __noinline__ void stage_rader(float2 *__restrict__ src, float2 *__res
     }
     __syncthreads();
     for (int e = threadIdx.x; e < N2 * nb; e += blockDim.x) {
-        const int k2 = fdiv_i(e, nb, invnb), b = e - k2 * nb;
+        const int k2 = divc<NBC>(e, nb, invnb), b = e - k2 * nb;
         float2 v[N1];
 #pragma unroll
         for (int q1 = 0; q1 < N1; ++q1) v[q1] = T[(q1 * N2 + k2) * nb + b];
@@ -611,9 +628,9 @@ __device__ __noinline__ void stage_rader(float2 *__restrict__ src, float2 *__res
     }
     __syncthreads();
     for (int e = threadIdx.x; e < N1 * nb; e += blockDim.x) {
-        const int q1 = fdiv_i(e, nb, invnb), b = e - q1 * nb;
+        const int q1 = divc<NBC>(e, nb, invnb), b = e - q1 * nb;
         const int l = b & (nl - 1), j = b >> lnl;
-        const int kk = Ns > 1 ? j - fdiv_i(j, Ns, invNs) * Ns : 0;
+        const int kk = Ns > 1 ? j - divc<NSC>(j, Ns, invNs) * Ns : 0;
         const int d = (j - kk) * R + kk;
         float2 v[N2];
 #pragma unroll
@@ -626,18 +643,21 @@ __device__ __noinline__ void stage_rader(float2 *__restrict__ src, float2 *__res
     }
 }
 
-template <int R, bool INV>
+template <int R, bool INV, int NC = 0, int NLC = 0, int NSC = 0>
 __device__ __forceinline__ void stage_small(const float2 *__restrict__ src, float2 *__restrict__ dst,
                                             int n, int nl, int Ns, const float2 *tw) {
+    if constexpr (NC > 0) n = NC;
+    if constexpr (NLC > 0) nl = NLC;
+    if constexpr (NSC > 0) Ns = NSC;
     const int m = n / R;
     const int tstep = n / (Ns * R);
     const int items = m * nl;
-    const int lnl = log2_pow2(nl);
+    const int lnl = NLC > 0 ? ilog2c(NLC) : log2_pow2(nl);
     const float invNs = 1.0f / (float)Ns;
     for (int it = threadIdx.x; it < items; it += blockDim.x) {
         const int l = it & (nl - 1);
         const int j = it >> lnl;
-        const int k = j - fdiv_i(j, Ns, invNs) * Ns;
+        const int k = j - divc<NSC>(j, Ns, invNs) * Ns;
         float2 v[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) v[r] = src[sidx(j + r * m, l, nl)];
@@ -773,6 +793,38 @@ __device__ float2 *fft_lines(float2 *A, float2 *B, int nl, const FftPlan &P,
     return src;
 }
 
+// The engine specialised at compile time for the padded lengths of the
+// benchmark tiles (678 = 113 x 6: tile 500, overlap 89; 478 = 239 x 2: tile
+// 300), NL lines per CTA: the same stages as their plans (fft_plan.cu: the
+// Rader stage first, at Ns = 1), with every size a constant.  Returns the
+// buffer holding the result.
+template <bool INV, int N, int NL>
+__device__ float2 *fft_lines_fixed(float2 *A, float2 *B, const FftPlan &P, const float2 *tw_s,
+                                   const float2 *tab_s, float4 *scr) {
+    static_assert(N == 678 || N == 478, "specialised lengths: 678, 478");
+    if constexpr (N == 678) {
+        stage_rader<113, 16, 7, INV, 678, NL, 1>(A, B, N, NL, 1, tw_s, tab_s + P.ptab[0], scr);
+        __syncthreads();
+        stage_small<6, INV, 678, NL, 113>(A, B, N, NL, 113, tw_s);
+    } else {
+        stage_rader<239, 14, 17, INV, 478, NL, 1>(A, B, N, NL, 1, tw_s, tab_s + P.ptab[0], scr);
+        __syncthreads();
+        stage_small<2, INV, 478, NL, 239>(A, B, N, NL, 239, tw_s);
+    }
+    __syncthreads();
+    return B;
+}
+
+// fft_lines, or the specialised engine when NF > 0 (NF = P.n, NLF = nl)
+template <bool INV, int LMAX, int NF, int NLF>
+__device__ __forceinline__ float2 *fft_run(float2 *A, float2 *B, int nl, const FftPlan &P, const float2 *tw_s,
+                                           const float2 *tab_s, float4 *scr) {
+    if constexpr (NF > 0)
+        return fft_lines_fixed<INV, NF, NLF>(A, B, P, tw_s, tab_s, scr);
+    else
+        return fft_lines<INV, LMAX>(A, B, nl, P, tw_s, tab_s, scr);
+}
+
 // Shared-memory layout of an FFT kernel: ping-pong line buffers A and B
 // (n * nl float2 each), the twiddle table (n), the radix tables (ntab),
 // then MM_FFT_SCR_PER_WARP float4 of scratch per warp for the lane stages
@@ -864,6 +916,13 @@ static inline int pick_nl(const FftPlan &P, int maxnl, FftCfg c = kFftWide) {
     ((P).lclass == 0 ? (const void *)KERNEL_TMPL<__VA_ARGS__ 0>             \
      : (P).lclass == 63 ? (const void *)KERNEL_TMPL<__VA_ARGS__ 63>         \
                         : (const void *)KERNEL_TMPL<__VA_ARGS__ 127>)
+// The kernel instantiation for plan P at nl lines per CTA: the specialised
+// engine for 678 and 478 at NLF lines, else the run-time engine of the plan's
+// lane class.
+#define MM_FFT_KERNEL(P, nl, NLF, KERNEL_TMPL, ...)                                           \
+    ((P).n == 678 && (nl) == NLF   ? (const void *)KERNEL_TMPL<__VA_ARGS__ 127, 678, NLF>    \
+     : (P).n == 478 && (nl) == NLF ? (const void *)KERNEL_TMPL<__VA_ARGS__ 127, 478, NLF>    \
+                                   : MM_BY_CLASS(P, KERNEL_TMPL, __VA_ARGS__))
 // SMs of the current device (cached per device)
 static inline int mm_sm_count() {
     static int cache[64] = {0};
