@@ -110,11 +110,19 @@ __device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {
     return c;
 }
 
-template <bool V16>
+// ZC > 0: the tile height known at compile time (Z = 50, the depth of every
+// channel of the benchmark FOV), so the chunk and row bounds fold; a multiple
+// of kJC and kTI drops the tail checks.
+template <bool V16, int ZC>
 __global__ void __launch_bounds__(kApplyMaxThreads, 2)
 k_zop_apply(float2 *__restrict__ S, const float2 *__restrict__ w, int Z, int Zp, long long plane, int nt, int ign,
             int tgn, const ZopTab tab) {
     extern __shared__ __align__(16) float2 sm[];
+    if constexpr (ZC > 0) {
+        Z = ZC;
+        ign = (ZC + kTI - 1) / kTI;
+    }
+    constexpr bool kFullChunks = ZC > 0 && ZC % kJC == 0 && ZC % kTI == 0;
     const int rowsM = ign * kTI, TC = tgn * kTT;
     const int msw = Z * kPB + 4;       // M row stride
     float2 *ws = sm;                   // Zp x kPB
@@ -234,12 +242,12 @@ k_zop_apply(float2 *__restrict__ S, const float2 *__restrict__ w, int Z, int Zp,
             __syncthreads();  // chunk c (and M) visible; chunk c - 1's buffer free
             if (c + 2 < nch) load_x(tc0, c + 2, (c + 2) % kNBuf);
             const int j0 = c * kJC;
-            const int jn = Z - j0 < kJC ? Z - j0 : kJC;
+            const int jn = kFullChunks ? kJC : (Z - j0 < kJC ? Z - j0 : kJC);
             const float2 *mr = Ms + (ig * kTI) * msw + j0 * kPB + p;
             const float2 *xr = Xb + (c % kNBuf) * TC * kXS + (tg * kTT) * kXS + p;
 #pragma unroll
             for (int jj = 0; jj < kJC; ++jj) {
-                if (jj >= jn) break;
+                if (!kFullChunks && jj >= jn) break;
                 float2 m[kTI], x[kTT];
 #pragma unroll
                 for (int a = 0; a < kTI; ++a) m[a] = mr[a * msw + jj * kPB];
@@ -255,7 +263,7 @@ k_zop_apply(float2 *__restrict__ S, const float2 *__restrict__ w, int Z, int Zp,
 #pragma unroll
             for (int a = 0; a < kTI; ++a) {
                 const int i = ig * kTI + a;
-                if (i >= Z) break;
+                if (!kFullChunks && i >= Z) break;
 #pragma unroll
                 for (int b = 0; b < kTT; ++b) {
                     const int t = tc0 + tg * kTT + b;
@@ -427,7 +435,8 @@ int mm_launch_zop_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, lon
     const size_t sm = sizeof(float2) * ((size_t)Zp * kPB + (size_t)ign * kTI * (Z * kPB + 4) +
                                         (size_t)kNBuf * tgn * kTT * kXS);
     MM_REQUIRE(sm <= 227 * 1024, "z operator shared memory %zu bytes exceeds the limit", sm);
-    const void *fn = (plane % 2 == 0) ? (const void *)k_zop_apply<true> : (const void *)k_zop_apply<false>;
+    const void *fn = Z == 50 ? ((plane % 2 == 0) ? (const void *)k_zop_apply<true, 50> : (const void *)k_zop_apply<false, 50>)
+                             : ((plane % 2 == 0) ? (const void *)k_zop_apply<true, 0> : (const void *)k_zop_apply<false, 0>);
     MM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     dim3 grid((unsigned)((plane + kPB - 1) / kPB));
     void *args[] = {&S, &w, &Z, &Zp, &plane, &nt, &ign, &tgn, &tab};
