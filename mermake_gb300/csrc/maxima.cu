@@ -129,16 +129,70 @@ __device__ __forceinline__ float raw_at(const Vols &V, int vi, const TileDesc &d
 // A warp per (z, x) row, lanes along y: every row index is split once, loads
 // are coalesced, and each lane keeps kMaxY values of the row in flight.  The
 // voxels above the threshold (a few percent) are queued per warp in shared
-// memory and their neighbourhoods tested one voxel per lane, so the test does
-// not run with most lanes idle.
+// memory across rows; whenever 32 are queued, their neighbourhoods are tested
+// one voxel per lane (and the last partial round at the end), so the test
+// runs with full warps.  Each voxel's neighbours are loaded kNbBatch at a
+// time before they are compared, so a test waits for one load latency per
+// batch instead of one per neighbour.
 constexpr int kMaxY = 4;
 constexpr int kMaxWarps = 8;
+constexpr int kQueue = 32 * kMaxY + 32;  // < 32 left over + one chunk of 32 kMaxY
+constexpr int kNbBatch = 8;
+
+// 1 when v is not below any in-range neighbour of (z, x, y) in the sphere
+__device__ __forceinline__ bool max_test(const float *__restrict__ img, const Vols &V, Xform t, int Z, int X,
+                                         int Y, int z, int x, int y, float v, const char4 *sph, int nn) {
+    for (int q0 = 0; q0 < nn; q0 += kNbBatch) {
+        float nb[kNbBatch];
+#pragma unroll
+        for (int u = 0; u < kNbBatch; ++u) {
+            nb[u] = -INFINITY;  // no neighbour: never above v
+            const int q = q0 + u;
+            if (q < nn) {
+                const char4 o = sph[q];
+                const int nz = refl(z + o.x, Z), nx = refl(x + o.y, X), ny = refl(y + o.z, Y);
+                if (nz >= 0 && nz < Z && nx >= 0 && nx < X && ny >= 0 && ny < Y)
+                    nb[u] = xf(img[nz * V.isz + nx * V.isx + ny], t);
+            }
+        }
+        bool below = false;
+#pragma unroll
+        for (int u = 0; u < kNbBatch; ++u) below |= v < nb[u];
+        if (below) return false;
+    }
+    return true;
+}
+
+// tests the queue entries (k, y, v)[0, cnt), cnt <= 32, one per lane, and
+// appends the maxima to cand
+__device__ __forceinline__ void test_round(const float *__restrict__ img, const Vols &V, Xform t, int Z, int X,
+                                           int Y, const char4 *sph, int nn, const unsigned *k, const int *yq,
+                                           const float *vq, int cnt, unsigned lane, int vi, uint2 *__restrict__ cand,
+                                           unsigned cap, unsigned *__restrict__ count) {
+    bool is_max = false;
+    unsigned key = 0;
+    int y = 0;
+    if ((int)lane < cnt) {
+        key = k[lane];
+        y = yq[lane];
+        is_max = max_test(img, V, t, Z, X, Y, (int)(key & 0xffffu), (int)(key >> 16), y, vq[lane], sph, nn);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, is_max);
+    if (m) {
+        unsigned slot = 0;
+        const int leader = __ffs(m) - 1;
+        if ((int)lane == leader) slot = atomicAdd(count, __popc(m));
+        slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(m & ((1u << lane) - 1));
+        if (is_max && slot < cap) cand[slot] = make_uint2(key, (unsigned)y | ((unsigned)vi << 16));
+    }
+}
 
 __global__ void __launch_bounds__(32 * kMaxWarps)
 k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigned cap,
          unsigned *__restrict__ count) {
-    __shared__ int qy[kMaxWarps][32 * kMaxY];
-    __shared__ float qv[kMaxWarps][32 * kMaxY];
+    __shared__ unsigned qk[kMaxWarps][kQueue];  // z | x << 16
+    __shared__ int qy[kMaxWarps][kQueue];
+    __shared__ float qv[kMaxWarps][kQueue];
     t = xf_resolve(t);
     const int vi = blockIdx.y;
     int X, Y;
@@ -151,10 +205,14 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
     const char4 *sph = g_sphere[delta];
     const unsigned lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    unsigned *my_k = qk[warp];
     int *my_y = qy[warp];
     float *my_v = qv[warp];
+
+    int qn = 0;
     for (int row = blockIdx.x * wpb + warp; row < rows; row += gridDim.x * wpb) {
         const int z = row / X, x = row - z * X;
+        const unsigned key = (unsigned)z | ((unsigned)x << 16);
         const float *rp = img + z * V.isz + x * V.isx;
         for (int y0 = 0; y0 < Y; y0 += 32 * kMaxY) {
             float vals[kMaxY];
@@ -165,7 +223,6 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
             }
             // queue the voxels above the threshold (maxima.cu:19; a NaN
             // threshold admits every voxel)
-            int qn = 0;
 #pragma unroll
             for (int k = 0; k < kMaxY; ++k) {
                 const int y = y0 + 32 * k + (int)lane;
@@ -174,43 +231,32 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
                 const unsigned m = __ballot_sync(0xffffffffu, up);
                 if (up) {
                     const int at = qn + __popc(m & ((1u << lane) - 1));
+                    my_k[at] = key;
                     my_y[at] = y;
                     my_v[at] = v;
                 }
                 qn += __popc(m);
             }
             __syncwarp();
-            for (int q0 = 0; q0 < qn; q0 += 32) {
-                const int qi = q0 + (int)lane;
-                bool is_max = false;
-                int y = 0;
-                if (qi < qn) {
-                    y = my_y[qi];
-                    const float v = my_v[qi];
-                    is_max = true;
-                    for (int q = 0; q < nn; ++q) {
-                        const char4 o = sph[q];
-                        const int nz = refl(z + o.x, Z), nx = refl(x + o.y, X), ny = refl(y + o.z, Y);
-                        if (nz < 0 || nz >= Z || nx < 0 || nx >= X || ny < 0 || ny >= Y) continue;
-                        if (v < xf(img[nz * V.isz + nx * V.isx + ny], t)) {
-                            is_max = false;
-                            break;
-                        }
-                    }
+            if (qn >= 32) {
+                const int full = qn & ~31;
+                for (int q0 = 0; q0 < full; q0 += 32)
+                    test_round(img, V, t, Z, X, Y, sph, nn, my_k + q0, my_y + q0, my_v + q0, 32, lane, vi, cand, cap,
+                               count);
+                const int rem = qn - full;
+                __syncwarp();
+                // the remainder (< 32 entries from index full >= 32) to the front
+                if ((int)lane < rem) {
+                    my_k[lane] = my_k[full + lane];
+                    my_y[lane] = my_y[full + lane];
+                    my_v[lane] = my_v[full + lane];
                 }
-                const unsigned m = __ballot_sync(0xffffffffu, is_max);
-                if (m) {
-                    unsigned slot = 0;
-                    const int leader = __ffs(m) - 1;
-                    if ((int)lane == leader) slot = atomicAdd(count, __popc(m));
-                    slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(m & ((1u << lane) - 1));
-                    if (is_max && slot < cap)
-                        cand[slot] = make_uint2((unsigned)z | ((unsigned)x << 16), (unsigned)y | ((unsigned)vi << 16));
-                }
+                __syncwarp();
+                qn = rem;
             }
-            __syncwarp();
         }
     }
+    if (qn > 0) test_round(img, V, t, Z, X, Y, sph, nn, my_k, my_y, my_v, qn, lane, vi, cand, cap, count);
 }
 
 // Sums 16 per-lane values over the warp with a reduce-scatter (16 + 15
