@@ -138,6 +138,7 @@ constexpr int kMaxY = 4;
 constexpr int kMaxWarps = 8;
 constexpr int kQueue = 32 * kMaxY + 32;  // < 32 left over + one chunk of 32 kMaxY
 constexpr int kNbBatch = 8;
+constexpr int kFitU = 2;  // fit sample rounds whose loads are in flight together (4 costs occupancy)
 
 // 1 when v is not below any in-range neighbour of (z, x, y) in the sphere
 __device__ __forceinline__ bool max_test(const float *__restrict__ img, const Vols &V, Xform t, int Z, int X,
@@ -326,24 +327,58 @@ k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand
 #pragma unroll
         for (int i = 0; i < 16; ++i) acc[i] = 0.f;
         float vmin = 1e20f;
+        auto add = [&](float v, float r, float g, int dz, int dx, int dy) {
+            const float dv = v - cv, dr = r - crw;
+            acc[0] += 1.f;
+            acc[1] += dv; acc[2] += dv * dv;
+            acc[3] += g; acc[4] += g * g; acc[5] += dv * g;
+            acc[6] += dr; acc[7] += dr * dr; acc[8] += dr * g;
+            acc[9] += (float)dz; acc[10] += (float)dx; acc[11] += (float)dy;
+            acc[12] += dv * dz; acc[13] += dv * dx; acc[14] += dv * dy;
+            vmin = fminf(vmin, v);
+        };
+        if (table) {
+            // at most 515 samples, so the reference's cap of 600 (maxima.cu:194)
+            // never binds: kFitU rounds of loads in flight, then their sums in
+            // the same per-lane order as one round at a time
+            for (int c0 = 0; c0 < nsamp; c0 += 32 * kFitU) {
+                float vv[kFitU], rr[kFitU], gg[kFitU];
+                char4 oo[kFitU];
+                bool okk[kFitU];
+#pragma unroll
+                for (int u = 0; u < kFitU; ++u) {
+                    const int ci = c0 + 32 * u + (int)lane;
+                    okk[u] = false;
+                    vv[u] = rr[u] = gg[u] = 0.f;
+                    oo[u] = make_char4(0, 0, 0, 0);
+                    if (ci < nsamp) {
+                        const char4 o = otab[ci];
+                        const int zz = refl(z0 + o.x, Z), xx = refl(x0 + o.y, X), yy = refl(y0 + o.z, Y);
+                        if (zz >= 0 && zz < Z && xx >= 0 && xx < X && yy >= 0 && yy < Y) {
+                            okk[u] = true;
+                            oo[u] = o;
+                            vv[u] = xf(img[zz * V.isz + xx * V.isx + yy], t);
+                            rr[u] = raw_at(V, vi, d, zz, xx, yy);
+                            gg[u] = gtab[ci];
+                        }
+                    }
+                }
+#pragma unroll
+                for (int u = 0; u < kFitU; ++u)
+                    if (okk[u]) add(vv[u], rr[u], gg[u], oo[u].x, oo[u].y, oo[u].z);
+            }
+        }
         int taken = 0;  // in-range samples before this chunk (cap 600, maxima.cu:194)
-        for (int c0 = 0; c0 < nsamp && taken < 600; c0 += 32) {
+        for (int c0 = 0; !table && c0 < nsamp && taken < 600; c0 += 32) {
             const int ci = c0 + (int)lane;
             int dz = 0, dx = 0, dy = 0;
             bool ok = false;
             int zz = 0, xx = 0, yy = 0;
             if (ci < nsamp) {
-                bool in;
-                if (table) {
-                    const char4 o = otab[ci];
-                    dz = o.x; dx = o.y; dy = o.z;
-                    in = true;
-                } else {
-                    dz = ci / (side * side) - delta_fit;
-                    dx = (ci / side) % side - delta_fit;
-                    dy = ci % side - delta_fit;
-                    in = dz * dz + dx * dx + dy * dy <= df2;
-                }
+                dz = ci / (side * side) - delta_fit;
+                dx = (ci / side) % side - delta_fit;
+                dy = ci % side - delta_fit;
+                const bool in = dz * dz + dx * dx + dy * dy <= df2;
                 if (in) {
                     zz = refl(z0 + dz, Z);
                     xx = refl(x0 + dx, X);
@@ -357,15 +392,7 @@ k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand
             if (ok && rank < 600) {
                 const float v = xf(img[zz * V.isz + xx * V.isx + yy], t);
                 const float r = raw_at(V, vi, d, zz, xx, yy);
-                const float g = table ? gtab[ci] : expf(-(dz * dz / gz + dx * dx / gxy + dy * dy / gxy));
-                const float dv = v - cv, dr = r - crw;
-                acc[0] += 1.f;
-                acc[1] += dv; acc[2] += dv * dv;
-                acc[3] += g; acc[4] += g * g; acc[5] += dv * g;
-                acc[6] += dr; acc[7] += dr * dr; acc[8] += dr * g;
-                acc[9] += (float)dz; acc[10] += (float)dx; acc[11] += (float)dy;
-                acc[12] += dv * dz; acc[13] += dv * dx; acc[14] += dv * dy;
-                vmin = fminf(vmin, v);
+                add(v, r, expf(-(dz * dz / gz + dx * dx / gxy + dy * dy / gxy)), dz, dx, dy);
             }
         }
         warp_sum16(acc, lane);
