@@ -357,11 +357,23 @@ k_blur_x_sub(TileGeom g, const float *__restrict__ res, const float *__restrict_
     const long long pbase = ((long long)blockIdx.z * g.Z + z) * P * P;
     float *rtab = colbuf + P * 32;  // 1 / count for counts 0..2 delta + 1
     if (delta >= 0) {
-        for (int x = warp; x < P; x += nw) {
-            if (y < P)
-                cp_async4(&colbuf[x * 32 + lane], &tmp[pbase + (long long)x * P + y]);
-            else
-                colbuf[x * 32 + lane] = 0.f;
+        // two rows of 32 columns per warp instruction, 8 bytes a lane when P is
+        // even (every row then starts 8-byte aligned: P * 4 and y0 * 4 are
+        // multiples of 8), else element by element
+        const int hr = lane >> 4, c2 = (lane & 15) * 2;
+        const bool even = (P & 1) == 0;
+        for (int x = 2 * warp + hr; x < P; x += 2 * nw) {
+            const int yy = y0 + c2;
+            float *dst = &colbuf[x * 32 + c2];
+            if (even && yy + 1 < P) {
+                cp_async8(dst, &tmp[pbase + (long long)x * P + yy]);
+            } else if (yy + 1 < P) {
+                cp_async4(dst, &tmp[pbase + (long long)x * P + yy]);
+                cp_async4(dst + 1, &tmp[pbase + (long long)x * P + yy + 1]);
+            } else {
+                dst[0] = yy < P ? tmp[pbase + (long long)x * P + yy] : 0.f;
+                dst[1] = 0.f;
+            }
         }
         for (int c = threadIdx.x; c <= 2 * delta + 1; c += blockDim.x) rtab[c] = c ? 1.0f / (float)c : 0.f;
         cp_async_wait_all();
@@ -375,7 +387,7 @@ k_blur_x_sub(TileGeom g, const float *__restrict__ res, const float *__restrict_
         for (int i = lo; i <= hi; ++i) sum += colbuf[i * 32 + lane];
     }
     const bool yok = y < P;
-    constexpr int U = 8;  // rows of res loaded ahead of the in-place stores
+    constexpr int U = 16;  // rows of res loaded ahead of the in-place stores
     for (int xb = x0; xb < x1; xb += U) {
         float v[U];
 #pragma unroll
