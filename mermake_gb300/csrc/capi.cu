@@ -490,7 +490,9 @@ int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t
         if ((rc = ws_get(c, WS_CAND, cap * sizeof(uint2), &cand))) return rc;
         cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
         MM_CUDA_TRY(cudaMemsetAsync(&sm->overflow, 0, sizeof(unsigned), st));
-        for (int sign = 0; sign < 2; ++sign) {
+        {
+            // v / rms and -v / rms in one maxima pass: the candidates of each
+            // sign in one half of the list, counted in rows / rows2
             MaximaArgs a = {};
             a.img = buffer; a.isz = (long long)X * Y; a.isx = Y; a.ivol = 0;
             a.Z = Z; a.X = X; a.Y = Y; a.nvol = 1;
@@ -498,17 +500,16 @@ int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t
             a.raw_kind = 1; a.raw = image; a.rsz = isz; a.rsx = isx; a.rvol = 0;
             a.th = threshold; a.delta = delta; a.delta_fit = delta_fit;
             a.sigmaZ = sigmaZ; a.sigmaXY = sigmaXY;
-            a.div = 0.f; a.divp = &sm->div; a.neg = sign; a.keep_filter = 0;
-            float *o = sign ? out_minus : out_plus;
-            unsigned oc = sign ? cap_minus : cap_plus;
+            a.div = 0.f; a.divp = &sm->div; a.neg = 0; a.keep_filter = 0;
+            const unsigned half = (unsigned)(cap / 2);
             {
                 StageTimer tm(c, ST_MAXIMA_FIT, 4.0 * N, st);
-                if ((rc = mm_launch_maxima_fit(a, (uint2 *)cand, (unsigned)cap, &sm->cand, o, oc, nullptr, 0, st)))
+                if ((rc = mm_launch_maxima_fit_pm(a, (uint2 *)cand, half, &sm->rows, &sm->rows2, out_plus, cap_plus,
+                                                  out_minus, cap_minus, st)))
                     return rc;
             }
-            unsigned *dst = sign ? &sm->rows2 : &sm->rows;
-            MM_CUDA_TRY(cudaMemcpyAsync(dst, &sm->cand, sizeof(unsigned), cudaMemcpyDeviceToDevice, st));
-            if ((rc = mm_launch_note_overflow(&sm->cand, (unsigned)cap, &sm->overflow, st))) return rc;
+            if ((rc = mm_launch_note_overflow(&sm->rows, half, &sm->overflow, st))) return rc;
+            if ((rc = mm_launch_note_overflow(&sm->rows2, half, &sm->overflow, st))) return rc;
         }
         MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters, &sm->rows, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
         float hdiv = 0.f;
@@ -521,7 +522,7 @@ int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t
             *count_minus = c->h_counters[1];
             return (*count_plus > cap_plus || *count_minus > cap_minus) ? MM_EOVERFLOW : MM_OK;
         }
-        if ((rc = ws_get(c, WS_CAND, (size_t)c->h_counters[2] * sizeof(uint2), &cand))) return rc;
+        if ((rc = ws_get(c, WS_CAND, 2 * (size_t)c->h_counters[2] * sizeof(uint2), &cand))) return rc;
     }
     mm_set_error("candidate list did not converge");
     return MM_EDEVICE;

@@ -169,6 +169,9 @@ struct MaximaArgs {
 int mm_maxima_ensure_init(cudaStream_t st);
 int mm_launch_maxima_fit(const MaximaArgs &a, uint2 *cand, unsigned cand_cap, unsigned *ncand, float *out,
                          unsigned out_cap, unsigned *out_count, int zero_out_count, cudaStream_t st);
+int mm_launch_maxima_fit_pm(const MaximaArgs &a, uint2 *cand, unsigned cap, unsigned *ncand_plus,
+                            unsigned *ncand_minus, float *out_plus, unsigned cap_plus, float *out_minus,
+                            unsigned cap_minus, cudaStream_t st);
 int mm_launch_note_overflow(const unsigned *ncand, unsigned cap, unsigned *overflow, cudaStream_t st);
 // largest number of per-block partial sums (grid cap of the elementwise kernels)
 #define MM_SUM_PARTS 4864

@@ -136,7 +136,7 @@ __device__ __forceinline__ float raw_at(const Vols &V, int vi, const TileDesc &d
 // batch instead of one per neighbour.
 constexpr int kMaxY = 4;
 constexpr int kMaxWarps = 8;
-constexpr int kQueue = 32 * kMaxY + 32;  // < 32 left over + one chunk of 32 kMaxY
+constexpr int kQueue = 2 * 32 * kMaxY + 32;  // < 32 left over + one chunk of both signs
 constexpr int kNbBatch = 8;
 constexpr int kFitU = 2;  // fit sample rounds whose loads are in flight together (4 costs occupancy)
 
@@ -164,33 +164,48 @@ __device__ __forceinline__ bool max_test(const float *__restrict__ img, const Vo
     return true;
 }
 
-// tests the queue entries (k, y, v)[0, cnt), cnt <= 32, one per lane, and
-// appends the maxima to cand
-__device__ __forceinline__ void test_round(const float *__restrict__ img, const Vols &V, Xform t, int Z, int X,
-                                           int Y, const char4 *sph, int nn, const unsigned *k, const int *yq,
-                                           const float *vq, int cnt, unsigned lane, int vi, uint2 *__restrict__ cand,
-                                           unsigned cap, unsigned *__restrict__ count) {
-    bool is_max = false;
-    unsigned key = 0;
-    int y = 0;
-    if ((int)lane < cnt) {
-        key = k[lane];
-        y = yq[lane];
-        is_max = max_test(img, V, t, Z, X, Y, (int)(key & 0xffffu), (int)(key >> 16), y, vq[lane], sph, nn);
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, is_max);
+// appends the lanes with `hit` to cand (warp-aggregated atomic on count)
+__device__ __forceinline__ void append_cand(bool hit, unsigned key, int y, int vi, unsigned lane,
+                                            uint2 *__restrict__ cand, unsigned cap, unsigned *__restrict__ count) {
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
     if (m) {
         unsigned slot = 0;
         const int leader = __ffs(m) - 1;
         if ((int)lane == leader) slot = atomicAdd(count, __popc(m));
         slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(m & ((1u << lane) - 1));
-        if (is_max && slot < cap) cand[slot] = make_uint2(key, (unsigned)y | ((unsigned)vi << 16));
+        if (hit && slot < cap) cand[slot] = make_uint2(key, (unsigned)y | ((unsigned)vi << 16));
     }
 }
 
+// tests the queue entries (k, y, v)[0, cnt), cnt <= 32, one per lane, and
+// appends the maxima to cand, or to cand2 for the entries of the negated
+// volume (bit 30 of y, queued by the two-sign pass)
+__device__ __forceinline__ void test_round(const float *__restrict__ img, const Vols &V, Xform t, int Z, int X,
+                                           int Y, const char4 *sph, int nn, const unsigned *k, const int *yq,
+                                           const float *vq, int cnt, unsigned lane, int vi, uint2 *__restrict__ cand,
+                                           unsigned cap, unsigned *__restrict__ count, uint2 *__restrict__ cand2,
+                                           unsigned *__restrict__ count2, bool both) {
+    bool is_max = false, neg = false;
+    unsigned key = 0;
+    int y = 0;
+    if ((int)lane < cnt) {
+        key = k[lane];
+        const int e = yq[lane];
+        neg = (e >> 30) & 1;
+        y = e & 0x3fffffff;
+        Xform ts = t;
+        if (neg) ts.neg = !ts.neg;
+        is_max = max_test(img, V, ts, Z, X, Y, (int)(key & 0xffffu), (int)(key >> 16), y, vq[lane], sph, nn);
+    }
+    append_cand(is_max && !neg, key, y, vi, lane, cand, cap, count);
+    if (both) append_cand(is_max && neg, key, y, vi, lane, cand2, cap, count2);
+}
+
+// both: the maxima of the volume and of its negation in one pass (the DAPI
+// block's two signs), into cand / count and cand2 / count2
 __global__ void __launch_bounds__(32 * kMaxWarps)
 k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigned cap,
-         unsigned *__restrict__ count) {
+         unsigned *__restrict__ count, uint2 *__restrict__ cand2, unsigned *__restrict__ count2, int both) {
     __shared__ unsigned qk[kMaxWarps][kQueue];  // z | x << 16
     __shared__ int qy[kMaxWarps][kQueue];
     __shared__ float qv[kMaxWarps][kQueue];
@@ -228,22 +243,25 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
             for (int k = 0; k < kMaxY; ++k) {
                 const int y = y0 + 32 * k + (int)lane;
                 const float v = xf(vals[k], t);
-                const bool up = y < Y && !(v <= th);
-                const unsigned m = __ballot_sync(0xffffffffu, up);
-                if (up) {
-                    const int at = qn + __popc(m & ((1u << lane) - 1));
-                    my_k[at] = key;
-                    my_y[at] = y;
-                    my_v[at] = v;
+                for (int sgn = 0; sgn < (both ? 2 : 1); ++sgn) {
+                    const float sv = sgn ? -v : v;
+                    const bool up = y < Y && !(sv <= th);
+                    const unsigned m = __ballot_sync(0xffffffffu, up);
+                    if (up) {
+                        const int at = qn + __popc(m & ((1u << lane) - 1));
+                        my_k[at] = key;
+                        my_y[at] = y | (sgn << 30);
+                        my_v[at] = sv;
+                    }
+                    qn += __popc(m);
                 }
-                qn += __popc(m);
             }
             __syncwarp();
             if (qn >= 32) {
                 const int full = qn & ~31;
                 for (int q0 = 0; q0 < full; q0 += 32)
                     test_round(img, V, t, Z, X, Y, sph, nn, my_k + q0, my_y + q0, my_v + q0, 32, lane, vi, cand, cap,
-                               count);
+                               count, cand2, count2, both);
                 const int rem = qn - full;
                 __syncwarp();
                 // the remainder (< 32 entries from index full >= 32) to the front
@@ -257,7 +275,9 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
             }
         }
     }
-    if (qn > 0) test_round(img, V, t, Z, X, Y, sph, nn, my_k, my_y, my_v, qn, lane, vi, cand, cap, count);
+    if (qn > 0)
+        test_round(img, V, t, Z, X, Y, sph, nn, my_k, my_y, my_v, qn, lane, vi, cand, cap, count, cand2, count2,
+                   both);
 }
 
 // Sums 16 per-lane values over the warp with a reduce-scatter (16 + 15
@@ -473,11 +493,7 @@ int mm_maxima_ensure_init(cudaStream_t st) {
 
 
 
-// Launches maxima + fit.  cand/ncand: scratch list and its device counter;
-// out/out_count: rows and their device counter (keep mode) -- counters are
-// zeroed here.
-int mm_launch_maxima_fit(const MaximaArgs &a, uint2 *cand, unsigned cand_cap, unsigned *ncand, float *out,
-                         unsigned out_cap, unsigned *out_count, int zero_out_count, cudaStream_t st) {
+static Vols make_vols(const MaximaArgs &a) {
     Vols V = {};
     V.img = a.img; V.isz = a.isz; V.isx = a.isx; V.ivol = a.ivol;
     V.Z = a.Z; V.X = a.X; V.Y = a.Y;
@@ -485,19 +501,55 @@ int mm_launch_maxima_fit(const MaximaArgs &a, uint2 *cand, unsigned cand_cap, un
     if (a.tiles) V.g = *a.tiles;
     V.raw_kind = a.raw_kind; V.raw = a.raw; V.rsz = a.rsz; V.rsx = a.rsx; V.rvol = a.rvol;
     V.chan = a.chan; V.flat = a.flat;
-    Xform t = {a.div, a.neg, a.divp};
-    MM_CUDA_TRY(cudaMemsetAsync(ncand, 0, sizeof(unsigned), st));
-    if (out_count && zero_out_count) MM_CUDA_TRY(cudaMemsetAsync(out_count, 0, sizeof(unsigned), st));
+    return V;
+}
+
+static dim3 maxima_grid(const MaximaArgs &a) {
     // a warp per (z, x) row, 8 rows per CTA
     long long rows = (long long)a.Z * (a.tiles ? (long long)a.tiles->P : (long long)a.X);
     int gx = (int)((rows + 7) / 8);
     if (gx > 152 * 16) gx = 152 * 16;
     if (gx < 1) gx = 1;
-    dim3 grid(gx, a.nvol);
-    k_maxima<<<grid, 32 * kMaxWarps, 0, st>>>(V, a.th, a.delta, t, cand, cand_cap, ncand);
+    return dim3(gx, a.nvol);
+}
+
+// Launches maxima + fit.  cand/ncand: scratch list and its device counter;
+// out/out_count: rows and their device counter (keep mode) -- counters are
+// zeroed here.
+int mm_launch_maxima_fit(const MaximaArgs &a, uint2 *cand, unsigned cand_cap, unsigned *ncand, float *out,
+                         unsigned out_cap, unsigned *out_count, int zero_out_count, cudaStream_t st) {
+    const Vols V = make_vols(a);
+    Xform t = {a.div, a.neg, a.divp};
+    MM_CUDA_TRY(cudaMemsetAsync(ncand, 0, sizeof(unsigned), st));
+    if (out_count && zero_out_count) MM_CUDA_TRY(cudaMemsetAsync(out_count, 0, sizeof(unsigned), st));
+    k_maxima<<<maxima_grid(a), 32 * kMaxWarps, 0, st>>>(V, a.th, a.delta, t, cand, cand_cap, ncand, nullptr, nullptr,
+                                                         0);
     MM_CHECK_LAUNCH();
     k_fit<<<152 * 8, 256, 0, st>>>(V, cand, ncand, cand_cap, a.delta_fit, a.sigmaZ, a.sigmaXY, t, out, out_cap,
                                    out_count, a.keep_filter);
+    MM_CHECK_LAUNCH();
+    return MM_OK;
+}
+
+// Maxima + fit of the volume (a.neg is the plus sign) and of its negation, the
+// maxima in one pass: candidates of the plus sign in cand[0, cap), of the minus
+// sign in cand[cap, 2 cap), counted in ncand_plus / ncand_minus (zeroed here);
+// fit rows i of each sign into out_plus / out_minus (no keep filter).
+int mm_launch_maxima_fit_pm(const MaximaArgs &a, uint2 *cand, unsigned cap, unsigned *ncand_plus,
+                            unsigned *ncand_minus, float *out_plus, unsigned cap_plus, float *out_minus,
+                            unsigned cap_minus, cudaStream_t st) {
+    const Vols V = make_vols(a);
+    Xform tp = {a.div, a.neg, a.divp}, tm = {a.div, !a.neg, a.divp};
+    MM_CUDA_TRY(cudaMemsetAsync(ncand_plus, 0, sizeof(unsigned), st));
+    MM_CUDA_TRY(cudaMemsetAsync(ncand_minus, 0, sizeof(unsigned), st));
+    k_maxima<<<maxima_grid(a), 32 * kMaxWarps, 0, st>>>(V, a.th, a.delta, tp, cand, cap, ncand_plus, cand + cap,
+                                                         ncand_minus, 1);
+    MM_CHECK_LAUNCH();
+    k_fit<<<152 * 8, 256, 0, st>>>(V, cand, ncand_plus, cap, a.delta_fit, a.sigmaZ, a.sigmaXY, tp, out_plus, cap_plus,
+                                   nullptr, 0);
+    MM_CHECK_LAUNCH();
+    k_fit<<<152 * 8, 256, 0, st>>>(V, cand + cap, ncand_minus, cap, a.delta_fit, a.sigmaZ, a.sigmaXY, tm, out_minus,
+                                   cap_minus, nullptr, 0);
     MM_CHECK_LAUNCH();
     return MM_OK;
 }

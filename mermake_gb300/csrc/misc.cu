@@ -3,6 +3,7 @@
 //   box_1d       blur.cu:1-52       truncated-window mean along one axis (any layout)
 //   subtract     math.py:4-33       uint16 saturating / reflecting subtraction
 //   sumsq        __main__.py:221    sum of squares for the DAPI RMS (double accumulation)
+#include <stdint.h>
 #include "deconv.cuh"
 
 namespace {
@@ -80,10 +81,25 @@ __global__ void k_subtract_u16(const uint16_t *__restrict__ x, const uint16_t *_
 
 // Sums of squares in a fixed order (the result does not depend on block
 // timing): each block writes its partial sum, k_sum_parts adds the partials.
+// Four squares are added in float (one 16-byte load) and the group goes into
+// the double accumulator, so the FP64 pipe (a small fraction of the FP32 rate
+// on this part) sees one add per four elements; the relative error of a
+// group is below 3e-7 and the groups add in double.
 __global__ void k_sumsq(const float *__restrict__ x, long long n, double *__restrict__ parts) {
     double acc = 0.0;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        double v = x[i];
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x, nth = (long long)gridDim.x * blockDim.x;
+    long long done = 0;
+    if ((reinterpret_cast<uintptr_t>(x) & 15) == 0) {
+        const float4 *x4 = reinterpret_cast<const float4 *>(x);
+        const long long n4 = n / 4;
+        for (long long i = tid; i < n4; i += nth) {
+            const float4 v = x4[i];
+            acc += (double)fmaf(v.w, v.w, fmaf(v.z, v.z, fmaf(v.y, v.y, v.x * v.x)));
+        }
+        done = n4 * 4;
+    }
+    for (long long i = done + tid; i < n; i += nth) {
+        const double v = x[i];
         acc += v * v;
     }
     acc = mm_block_sum(acc);
