@@ -23,7 +23,7 @@ namespace {
 
 constexpr int kThreads = kFftThreads;  // k_rows_fwd_f32
 constexpr int kSmemLimit = kFftSmemLimit;
-constexpr FftCfg kRowsFwdCfg = kFftWide;  // its raw-row staging wants 2 nl rows per CTA
+constexpr FftCfg kRowsFwdCfg = kFftPair;
 constexpr FftCfg kRowsInvCfg = kFftPair;
 constexpr int kBlurThreads = 512;  // k_blur_x_sub, k_make_raw
 
@@ -474,8 +474,8 @@ int mm_launch_rows_fwd_img(const TileGeom &g, const void *img, int dtype, const 
     const void *imga = img;
     const float *fa = flat;
     void *args[] = {&ga, &imga, &fa, &S, &P, &nl, &gx, &ngroups};
-    const void *fn = dtype == MM_DTYPE_U16 ? MM_FFT_KERNEL(P, nl, 16, k_rows_fwd_img, uint16_t,)
-                                          : MM_FFT_KERNEL(P, nl, 16, k_rows_fwd_img, float,);
+    const void *fn = dtype == MM_DTYPE_U16 ? MM_FFT_KERNEL(P, nl, 8, k_rows_fwd_img, uint16_t,)
+                                          : MM_FFT_KERNEL(P, nl, 8, k_rows_fwd_img, float,);
     return launch_fft_kernel(fn, grid, sm, st, args, kRowsFwdCfg.threads);
 }
 
