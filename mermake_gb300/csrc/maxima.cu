@@ -134,9 +134,12 @@ __device__ __forceinline__ float raw_at(const Vols &V, int vi, const TileDesc &d
 // runs with full warps.  Each voxel's neighbours are loaded kNbBatch at a
 // time before they are compared, so a test waits for one load latency per
 // batch instead of one per neighbour.
-constexpr int kMaxY = 4;
 constexpr int kMaxWarps = 8;
-constexpr int kQueue = 2 * 32 * kMaxY + 32;  // < 32 left over + one chunk of both signs
+// values in flight per lane: 8 for one sign, 4 for both (the queue holds < 32
+// left over + one chunk of 32 values per lane and sign: 288 entries either way)
+constexpr int kMaxY1 = 8, kMaxY2 = 4;
+constexpr int kQueue = 32 * kMaxY1 + 32;
+static_assert(2 * 32 * kMaxY2 + 32 <= kQueue, "queue too small for the two-sign pass");
 constexpr int kNbBatch = 8;
 constexpr int kFitU = 2;  // fit sample rounds whose loads are in flight together (4 costs occupancy)
 
@@ -201,11 +204,14 @@ __device__ __forceinline__ void test_round(const float *__restrict__ img, const 
     if (both) append_cand(is_max && neg, key, y, vi, lane, cand2, cap, count2);
 }
 
-// both: the maxima of the volume and of its negation in one pass (the DAPI
+// BOTH: the maxima of the volume and of its negation in one pass (the DAPI
 // block's two signs), into cand / count and cand2 / count2
+template <bool BOTH>
 __global__ void __launch_bounds__(32 * kMaxWarps)
 k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigned cap,
-         unsigned *__restrict__ count, uint2 *__restrict__ cand2, unsigned *__restrict__ count2, int both) {
+         unsigned *__restrict__ count, uint2 *__restrict__ cand2, unsigned *__restrict__ count2) {
+    constexpr int kMaxY = BOTH ? kMaxY2 : kMaxY1;
+    constexpr bool both = BOTH;
     __shared__ unsigned qk[kMaxWarps][kQueue];  // z | x << 16
     __shared__ int qy[kMaxWarps][kQueue];
     __shared__ float qv[kMaxWarps][kQueue];
@@ -522,8 +528,8 @@ int mm_launch_maxima_fit(const MaximaArgs &a, uint2 *cand, unsigned cand_cap, un
     Xform t = {a.div, a.neg, a.divp};
     MM_CUDA_TRY(cudaMemsetAsync(ncand, 0, sizeof(unsigned), st));
     if (out_count && zero_out_count) MM_CUDA_TRY(cudaMemsetAsync(out_count, 0, sizeof(unsigned), st));
-    k_maxima<<<maxima_grid(a), 32 * kMaxWarps, 0, st>>>(V, a.th, a.delta, t, cand, cand_cap, ncand, nullptr, nullptr,
-                                                         0);
+    k_maxima<false><<<maxima_grid(a), 32 * kMaxWarps, 0, st>>>(V, a.th, a.delta, t, cand, cand_cap, ncand, nullptr,
+                                                                nullptr);
     MM_CHECK_LAUNCH();
     k_fit<<<152 * 8, 256, 0, st>>>(V, cand, ncand, cand_cap, a.delta_fit, a.sigmaZ, a.sigmaXY, t, out, out_cap,
                                    out_count, a.keep_filter);
@@ -542,8 +548,8 @@ int mm_launch_maxima_fit_pm(const MaximaArgs &a, uint2 *cand, unsigned cap, unsi
     Xform tp = {a.div, a.neg, a.divp}, tm = {a.div, !a.neg, a.divp};
     MM_CUDA_TRY(cudaMemsetAsync(ncand_plus, 0, sizeof(unsigned), st));
     MM_CUDA_TRY(cudaMemsetAsync(ncand_minus, 0, sizeof(unsigned), st));
-    k_maxima<<<maxima_grid(a), 32 * kMaxWarps, 0, st>>>(V, a.th, a.delta, tp, cand, cap, ncand_plus, cand + cap,
-                                                         ncand_minus, 1);
+    k_maxima<true><<<maxima_grid(a), 32 * kMaxWarps, 0, st>>>(V, a.th, a.delta, tp, cand, cap, ncand_plus, cand + cap,
+                                                               ncand_minus);
     MM_CHECK_LAUNCH();
     k_fit<<<152 * 8, 256, 0, st>>>(V, cand, ncand_plus, cap, a.delta_fit, a.sigmaZ, a.sigmaXY, tp, out_plus, cap_plus,
                                    nullptr, 0);
