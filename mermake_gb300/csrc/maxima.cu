@@ -317,7 +317,7 @@ __device__ __forceinline__ void warp_sum16(float (&v)[16], unsigned lane) {
 // precision, the quotients and roots in float, as the reference).  The
 // Gaussian weights depend only on the offset and the sigmas, so a block
 // tabulates them once.
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, 4)
 k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand, unsigned cap, int delta_fit,
       float sigmaZ, float sigmaXY, Xform t, float *__restrict__ out, unsigned out_cap,
       unsigned *__restrict__ out_count, int keep_filter) {
