@@ -237,6 +237,28 @@ def run_fov(s, form, chans=None, dapi=None):
     return out
 
 
+def zpass_flops(w, s):
+    """FP32 flops of one FOV's z passes, by the form each channel's batch runs
+    (the library's choice in run_tiles): one Z x Z complex matrix per frequency
+    and tile when one spectrum serves a batch of >= 10 tiles of height <= 64,
+    else the direct sum over the padded planes (outputs and planes in blocks of
+    8).  A complex FMA is 8 flops."""
+    shape = (w["Z"], w["X"], w["Y"])
+    out = 0.0
+    for dec, n in ((s["dec_h"], w["colours"]), (s["dec_d"], 1 if s["dec_d"] is not None else 0)):
+        if not n:
+            continue
+        nt, Z, plane = dec.n_tiles(shape), dec.tile_height, dec.P * dec.H
+        if dec.z_operator is None:
+            continue
+        if dec.psf_fft.shape[0] == 1 and nt >= 10 and Z <= 64:
+            per = Z * Z
+        else:
+            per = -(-Z // 8) * 8 * (-(-dec.Zp // 8) * 8)
+        out += n * nt * plane * per * 8.0
+    return out
+
+
 def timed(fn, K, W, barrier, before_timed=None):
     import torch
     for _ in range(W):
@@ -319,7 +341,7 @@ def gpu_arm(args, rank, world, local):
     peak = peak or 6800.0
     achieved = (dbytes / dl) / ((dms / dl) / 1e3) / 1e9
     # DRAM traffic of the dominant kernel per launch: ncu's bytes per tile on
-    # the quad workload, scaled by the tiles one launch of this run processes
+    # the ten-tile workload, scaled by the tiles one launch of this run processes
     traffic = None
     tp = os.path.join(ROOT, "profiles", "dram_traffic_ten.json")
     if os.path.exists(tp):
@@ -360,6 +382,16 @@ def gpu_arm(args, rank, world, local):
                      "stage_share": stage_share},
         "clocks": clk.summary(),
     }
+    if dom == "zpass" and args.form == "batched":
+        # the z pass is FP32-FMA bound: its arithmetic against the nominal FP32
+        # peak (SMs x 128 lanes x 2 flops x the sampled maximum SM clock)
+        props = torch.cuda.get_device_properties(dev)
+        mhz = line["clocks"].get("sm_max_mhz") or peaks.get("sm_max_mhz") or 2070.0
+        fpeak = props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
+        fl = zpass_flops(w, s) * args.steps / dl
+        line["roofline"]["fp32"] = {"achieved": fl / ((dms / dl) / 1e3) / 1e12, "peak_nominal": fpeak,
+                                    "unit": "TFLOP/s", "frac": fl / ((dms / dl) / 1e3) / 1e12 / fpeak,
+                                    "flops_per_launch": fl}
 
     if not args.no_e2e:
         import torch
