@@ -124,10 +124,10 @@ int mm_launch_zpass(const TileGeom &g, float2 *S, const float2 *W, long long wst
 // W along z (zop.cu): as a matrix per frequency over a batch that shares one
 // spectrum (mm_launch_zop_apply), or as the direct sum per tile
 // (mm_launch_zconv).
-// The z operator's cost per launch is dominated by summing M (Z x Z per
-// frequency) and hardly depends on the batch; below this many tiles the
-// padded-depth transforms are cheaper (about 0.4 ms per 678 x 678 tile
-// against about 3.9 ms per launch at Z = 50).
+// The matrix form's CTAs shrink with the batch (threads = 4 frequencies x
+// ceil(Z / 5) row groups x ceil(nt / 5) tile groups), so a launch costs nearly
+// as much for 10 tiles as for 25 (3.5 against 3.9 ms at Z = 50, P = 678);
+// batches of fewer tiles than this take the direct sum.
 #define MM_ZOP_MIN_TILES 10
 #define MM_ZOP_MAX_Z 64
 #define MM_ZOP_MAX_ZP 400
