@@ -237,6 +237,22 @@ def run_fov(s, form, chans=None, dapi=None):
     return out
 
 
+def max_over_ranks(x, pg, device="cpu"):
+    """The largest of the ranks' x (a replica job's time is its slowest rank's);
+    pg: torch.distributed (any backend) or None for one process."""
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    if pg is not None:
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, units_per_rank, steps, total_ms):
+    """Whole-job units per second: each of the world replicas processed
+    units_per_rank per step, the job took total_ms (its slowest rank)."""
+    return world * units_per_rank * steps / (total_ms / 1e3)
+
+
 def zpass_flops(w, s):
     """FP32 flops of one FOV's z passes, by the form each channel's batch runs
     (the library's choice in run_tiles): one Z x Z complex matrix per frequency
@@ -321,12 +337,9 @@ def gpu_arm(args, rank, world, local):
     prof = _lib.profile_read()
     _lib.profile_enable(False)
     spots = [int(o.shape[0]) for o in run_fov(s, args.form)]
-    t = torch.tensor([total_ms], device=dev)
-    if pg:
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-    total_ms = float(t.item())
+    total_ms = max_over_ranks(total_ms, pg, dev)
     ms_step = total_ms / args.steps
-    value = world * vox * args.steps / (total_ms / 1e3)
+    value = job_rate(world, vox, args.steps, total_ms)
 
     # dominant kernel
     stages = {k: v for k, v in prof.items() if v[2] > 0}
@@ -445,11 +458,8 @@ def gpu_arm(args, rank, world, local):
                 io["d2h"] = sum(h.numel() * h.element_size() for h in hb)
 
             e_ms, _ = timed(e2e_step, args.steps, 1, barrier)
-        t = torch.tensor([e_ms], device=dev)
-        if pg:
-            pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e_ms = float(t.item())
-        line["e2e"] = {"value": world * vox * args.steps / (e_ms / 1e3), "unit": "voxels/s",
+        e_ms = max_over_ranks(e_ms, pg, dev)
+        line["e2e"] = {"value": job_rate(world, vox, args.steps, e_ms), "unit": "voxels/s",
                        "h2d_bytes_per_step": io["h2d"], "d2h_bytes_per_step": io["d2h"],
                        "ms_per_step": e_ms / args.steps}
 
