@@ -120,6 +120,33 @@ def test_apply_float_image_and_multi_psf(dc):
         assert np.abs(got[ok] - want[ok]).max() <= REL * np.abs(want[ok]).max()
 
 
+@pytest.mark.parametrize("ts", [500, 300])
+def test_tile_wise_float_image_at_the_specialised_lengths(dc, ts):
+    """float32 images through the FFT engine compiled for the benchmark tile
+    lengths (P = 678 at tile 500, 478 at tile 300), with a flat field and blur,
+    against the FP64 oracle: every yielded tile of a 2 x 2 grid (one thin edge)."""
+    rng = np.random.default_rng(ts)
+    Z, X = 4, ts + 100
+    img = (1000 * rng.random((Z, X, X))).astype(np.float32)
+    fl = (0.8 + 0.2 * rng.random((X, X))).astype(np.float32)
+    psf = np.zeros((5, 5, 5), np.float32)
+    psf[2, 2, 2] = 1.0
+    psf[1:4, 1:4, 1:4] += 0.1 * rng.random((3, 3, 3)).astype(np.float32)
+    args = dict(tile_size=ts, zpad=3, overlap=89, beta=0.01)
+    d = dc.Deconvolver(psf, img.shape, **args)
+    o = od.Deconvolver(psf, img.shape, **args)
+    assert d.P == ts + 178
+    n = 0
+    for (x, y, res, raw), (xo, yo, rres, rraw) in zip(d.tile_wise(torch.from_numpy(img).cuda(),
+                                                                   torch.from_numpy(fl).cuda(), 15),
+                                                      o.tile_wise(img, fl, 15)):
+        assert (x, y) == (xo, yo)
+        g = res.cpu().numpy().astype(np.float64)
+        assert np.abs(g - rres).max() <= REL * np.abs(rres).max()
+        n += 1
+    assert n == 4
+
+
 def test_full_deconv_signature(dc):
     """test_deconvolver.py:436-470: shapes and intensity."""
     img = torch.zeros((10, 50, 50), dtype=torch.float64, device="cuda")
