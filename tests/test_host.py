@@ -140,3 +140,92 @@ def test_spot_capacity_grows_from_counts_seen():
     pipeline._seen(dec, key, 1000)                       # a smaller count keeps the largest
     assert pipeline._capacity(dec, key, 1 << 18) == 322214 + 322214 // 4
     assert pipeline._capacity(dec, ("dapi+", 40, 3000, 3000), 1 << 16) == 1 << 16
+
+
+def _map_z(z, Z, zpad, Zp):
+    """mm_map_z (csrc/deconv.cuh): padded plane z -> real plane, or -1."""
+    i2 = zpad + Z - 1
+    q = z
+    if z > i2 and 2 * i2 - z >= 0:
+        q = 2 * i2 - z
+    if q < zpad and 2 * zpad - q < Zp:
+        q = 2 * zpad - q
+    return q - zpad if zpad <= q < zpad + Z else -1
+
+
+@pytest.mark.parametrize("Z,zpad", [(13, 12), (50, 49), (50, 24), (7, 2), (5, 9), (40, 39), (1, 1), (80, 79),
+                                    (128, 1)])
+def test_z_sum_index_algebra_matches_the_padded_transforms(Z, zpad):
+    """The index arithmetic of k_zconv (csrc/zop.cu) restated in NumPy: the
+    staged kernel run wx[u] = w[(u + zpad + 1 - Tpad) mod Zp] of
+    ceil(Z/8)*8 + Tpad - 1 rows, the 15-value window at i0 - zb + Tpad - 8, the
+    zero row for unmapped planes; against reflect padding, FFT over Zp, times
+    W, inverse FFT and the crop.  Every window read stays inside the run."""
+    kCI = 8
+    Zp = Z + 2 * zpad
+    rng = np.random.default_rng(Z * 1000 + zpad)
+    X = rng.standard_normal(Z) + 1j * rng.standard_normal(Z)
+    W = rng.standard_normal(Zp) + 1j * rng.standard_normal(Zp)
+    w = np.fft.ifft(W)  # the z kernel: inverse DFT of W (W carries 1 / Zp here)
+    Tpad = -(-Zp // kCI) * kCI
+    G = -(-Z // kCI)
+    Lw = G * kCI + Tpad - 1
+    wx = np.array([w[(u + zpad + 1 - Tpad) % Zp] for u in range(Lw)])
+    xs = np.concatenate([X, [0]])
+    zm = [(_map_z(z, Z, zpad, Zp) if z < Zp else -1) for z in range(Tpad)]
+    zm = [Z if m < 0 else m for m in zm]
+    Y = np.zeros(Z, complex)
+    for g in range(G):
+        i0 = g * kCI
+        acc = np.zeros(kCI, complex)
+        for zb in range(0, Tpad, kCI):
+            base = i0 - zb + Tpad - kCI
+            assert 0 <= base and base + 2 * kCI - 2 < Lw
+            wr = wx[base:base + 2 * kCI - 1]
+            for s_ in range(kCI):
+                acc += wr[kCI - 1 - s_:2 * kCI - 1 - s_] * xs[zm[zb + s_]]
+        n = min(kCI, Z - i0)
+        Y[i0:i0 + n] = acc[:n]
+    xp = np.array([X[m] if (m := _map_z(z, Z, zpad, Zp)) >= 0 else 0 for z in range(Zp)])
+    want = np.fft.ifft(np.fft.fft(xp) * W)[zpad:zpad + Z]
+    assert np.abs(Y - want).max() <= 1e-12 * np.abs(want).max()
+
+
+@pytest.mark.parametrize("R,N1,N2,g", [(113, 16, 7, 3), (239, 14, 17, 7)])
+@pytest.mark.parametrize("inverse", [False, True])
+def test_rader_split_matches_the_dft(R, N1, N2, g, inverse):
+    """The three passes of stage_rader<R, N1, N2> (csrc/fft.cuh) with the tables
+    of rader_tables (csrc/fft_plan.cu), restated in NumPy for one butterfly:
+    gather u[q1 + N1 q2] = x[g^-(q1 + N1 q2)] and an N2-point DFT times
+    wM^(q1 k2); per k2 an N1-point DFT, the product with H[k2 + N2 k1] and the
+    inverse N1-point DFT times wM^-(q1 k2); an inverse N2-point DFT and the
+    scatter to X[g^(q1 + N1 q2)], with X[0] = x0 + sum u."""
+    M = R - 1
+    ginv = pow(g, R - 2, R)
+    gp = [pow(g, q, R) for q in range(M)]
+    gi = [pow(ginv, q, R) for q in range(M)]
+    assert len(set(gp)) == M  # g is a primitive root
+    sgn = 1 if inverse else -1
+    H = np.fft.fft(np.exp(sgn * 2j * np.pi * np.array(gp) / R)) / M
+    wM = np.exp(-2j * np.pi * np.arange(M) / M)
+    x = np.random.default_rng(R).standard_normal(R) + 1j * np.random.default_rng(R + 1).standard_normal(R)
+    T = np.zeros(M, complex)
+    for q1 in range(N1):
+        v = np.fft.fft([x[gi[q1 + N1 * q2]] for q2 in range(N2)])
+        T[q1 * N2:(q1 + 1) * N2] = v * np.array([wM[q1 * k2] if k2 else 1 for k2 in range(N2)])
+    for k2 in range(N2):
+        v = np.fft.fft(T[k2::N2][:N1])
+        if k2 == 0:
+            s0 = v[0]
+        v = np.fft.ifft(v * H[k2 + N2 * np.arange(N1)]) * N1
+        T[k2] = v[0]
+        for q1 in range(1, N1):
+            T[q1 * N2 + k2] = v[q1] * np.conj(wM[q1 * k2])
+    X = np.zeros(R, complex)
+    for q1 in range(N1):
+        v = np.fft.ifft(T[q1 * N2:(q1 + 1) * N2]) * N2
+        for q2 in range(N2):
+            X[gp[q1 + N1 * q2]] = x[0] + v[q2]
+    X[0] = x[0] + s0
+    want = np.fft.ifft(x) * R if inverse else np.fft.fft(x)
+    assert np.abs(X - want).max() <= 1e-12 * np.abs(want).max()
