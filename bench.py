@@ -39,7 +39,8 @@ A step is one FOV of the workload, inputs resident in HBM:
 ``value`` is FOV input voxels per second (all channels) of the batched form
 (tiles of a colour in one batch, spots kept and offset on the device);
 ``--form plain`` times the per-tile loop of ``Deconvolver.tile_wise`` +
-``find_local_maxima`` instead.  ``e2e`` is the same metric through the same
+``find_local_maxima`` instead; ``--form graph`` replays the whole FOV captured
+once as a CUDA graph (``pipeline.FovGraph``) on the resident channels.  ``e2e`` is the same metric through the same
 public calls with the channels copied from pinned host memory every step and
 the spot tables read back; in the batched form through ``pipeline.FovRunner``,
 which copies the next FOV on a side stream while the current one computes.  ``roofline`` reports the dominant kernel (largest
@@ -100,7 +101,7 @@ def parse():
                     help="served: requests in the stream (FOV id = i mod 20, round = i div 20)")
     ap.add_argument("--interval", type=float, default=1.5, help="served: mean Poisson arrival interval (s)")
     ap.add_argument("--workers", type=int, default=2, help="served: concurrent requests on the device")
-    ap.add_argument("--form", default="batched", choices=["batched", "plain"])
+    ap.add_argument("--form", default="batched", choices=["batched", "plain", "graph"])
     ap.add_argument("--batch", type=int, default=0,
                     help="batched form: tiles per batch (0: the tuned / L2-rule size, -1: all tiles)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -212,6 +213,16 @@ def run_fov(s, form, chans=None, dapi=None):
     w = s["w"]
     chans = s["chans"] if chans is None else chans
     dapi = s["dapi"] if dapi is None else dapi
+    if form == "graph":
+        # one replay of the captured FOV (DAPI block and colours) on the
+        # graph's resident inputs
+        g = s["graph"]
+        g.replay()
+        got = g.results()
+        if got is None:
+            raise RuntimeError("a graph output overflowed")
+        plus, minus, rows = got
+        return ([plus, minus] if plus is not None else []) + rows
     out = []
     if w["dapi"]:
         p, m, buf, _ = pipeline.dapi_spots(s["dec_d"], dapi, None, buffer=s.get("buffer"), batch=s["batch"],
@@ -320,6 +331,14 @@ def gpu_arm(args, rank, world, local):
 
     s = setup(w, dev, seed=1000 + rank)
     s["batch"] = args.batch
+    if args.form == "graph":
+        from mermake_gb300 import pipeline
+        # sizes the rows from an eager FOV, then captures on the resident channels
+        run_fov(s, "batched")
+        torch.cuda.synchronize()
+        s["graph"] = pipeline.FovGraph(s["dec_h"], s["dec_d"], (w["Z"], w["X"], w["Y"]), w["colours"], w["hyb"],
+                                       w.get("dapi_args"), flats=s["flats"], batch=args.batch,
+                                       inputs=(s["dapi"], s["chans"]))
     vox = fov_voxels(w)
 
     # device-resident timed region, with per-stage events live
@@ -334,6 +353,8 @@ def gpu_arm(args, rank, world, local):
     with ClockSampler(local) as clk:
         total_ms, per = timed(lambda: run_fov(s, args.form), args.steps, args.warmup, barrier, start_counting)
     launches = _lib.launch_count() - n0[0]
+    if args.form == "graph":  # replays bypass the host-side launch counter
+        launches += s["graph"].launches * args.steps
     prof = _lib.profile_read()
     _lib.profile_enable(False)
     spots = [int(o.shape[0]) for o in run_fov(s, args.form)]
@@ -341,10 +362,11 @@ def gpu_arm(args, rank, world, local):
     ms_step = total_ms / args.steps
     value = job_rate(world, vox, args.steps, total_ms)
 
-    # dominant kernel
+    # dominant kernel (the graph form records no per-stage events: its line
+    # points at the batched form's roofline, the same kernels)
     stages = {k: v for k, v in prof.items() if v[2] > 0}
-    dom = max(stages, key=lambda k: stages[k][0])
-    dms, dbytes, dl = stages[dom]
+    dom = max(stages, key=lambda k: stages[k][0]) if stages else None
+    dms, dbytes, dl = stages[dom] if stages else (0.0, 0.0, 1)
     peaks = {}
     pp = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pp):
@@ -352,20 +374,20 @@ def gpu_arm(args, rank, world, local):
     peak = peaks.get("hbm_gbs")
     peak_src = "measured" if peak else "fallback"
     peak = peak or 6800.0
-    achieved = (dbytes / dl) / ((dms / dl) / 1e3) / 1e9
+    achieved = (dbytes / dl) / ((dms / dl) / 1e3) / 1e9 if stages else None
     # DRAM traffic of the dominant kernel per launch: ncu's bytes per tile on
     # the ten-tile workload, scaled by the tiles one launch of this run processes
     traffic = None
     tp = os.path.join(ROOT, "profiles", "dram_traffic_ten.json")
     if os.path.exists(tp):
-        e = json.load(open(tp))["stages"].get(dom)
+        e = json.load(open(tp))["stages"].get(dom) if dom else None
         if e:
             shape = (w["Z"], w["X"], w["Y"])
             tiles = len(s["dec_h"].tile_boxes(shape)) * w["colours"]
             if s["dec_d"] is not None:
                 tiles += len(s["dec_d"].tile_boxes(shape))
             traffic = e["per_tile"] * tiles * args.steps / dl + e["per_launch"]
-    stage_share = {k: round(v[0] / sum(x[0] for x in stages.values()), 4) for k, v in stages.items()}
+    stage_share = {k: round(v[0] / sum(x[0] for x in stages.values()), 4) for k, v in stages.items()} if stages else {}
 
     line = {
         "metric": "FOV voxels/s deconv+blur+maxima+fit",
@@ -389,10 +411,11 @@ def gpu_arm(args, rank, world, local):
         "spots_per_fov": spots,
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
+                     "frac": achieved / peak if achieved else None, "peak_source": peak_src, "traffic": traffic,
                      "traffic_source": "profiles/dram_traffic_ten.json scaled by tiles per launch" if traffic else None,
-                     "bytes_per_launch": dbytes / dl, "ms_per_launch": dms / dl,
-                     "stage_share": stage_share},
+                     "bytes_per_launch": dbytes / dl if stages else None, "ms_per_launch": dms / dl if stages else None,
+                     "stage_share": stage_share} if stages else
+                    {"note": "no per-stage events inside the graph; the batched form's line has the roofline"},
         "clocks": clk.summary(),
     }
     if dom == "zpass" and args.form == "batched":
@@ -443,8 +466,11 @@ def gpu_arm(args, rank, world, local):
             barrier()
             e_ms = e0.elapsed_time(e1)
         else:
-            dev_ch = [torch.empty_like(c) for c in s["chans"]]
-            dev_dapi = torch.empty_like(s["dapi"]) if s["dapi"] is not None else None
+            if args.form == "graph":  # the graph reads the channels it was captured on
+                dev_ch, dev_dapi = s["chans"], s["dapi"]
+            else:
+                dev_ch = [torch.empty_like(c) for c in s["chans"]]
+                dev_dapi = torch.empty_like(s["dapi"]) if s["dapi"] is not None else None
 
             def e2e_step():
                 for h, d in zip(host_ch, dev_ch):

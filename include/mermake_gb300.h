@@ -177,6 +177,29 @@ int mm_dapi_spots(mm_ctx *ctx, const uint16_t *image, int Z, int X, int Y, int64
                   float sigmaXY, int batch, float *buffer, float *out_plus, uint32_t cap_plus, uint32_t *count_plus,
                   float *out_minus, uint32_t cap_minus, uint32_t *count_minus, float *rms, void *stream);
 
+/* mm_hyb_spots / mm_dapi_spots without a host synchronisation, for capture in
+ * a CUDA graph (no counterpart in the reference): the counts stay on the
+ * device and nothing is retried.
+ *   mm_hyb_spots_async: *count_dev = rows (rows past out_cap are dropped);
+ *     *overflow_dev = 0, or the candidate count that did not fit the list.
+ *   mm_dapi_spots_async: counts_dev[0..2] = rows (+), rows (-), candidate
+ *     overflow (0 when none); *rms_dev (may be NULL) = the divisor.
+ * A result is complete when the overflow is 0 and every count is within its
+ * capacity; otherwise rerun with the synchronous call.  The context's scratch
+ * is sized by the first call: capture a graph only after one eager call with
+ * the same shapes, on a context that no other call grows while the graph
+ * lives (its workspace addresses are baked into the graph). */
+int mm_hyb_spots_async(mm_ctx *ctx, const uint16_t *image, int Z, int X, int Y, int64_t isz, int64_t isx,
+                       const float *flat, int64_t fsx, const void *W, int npsf, const void *zop, int tile_size,
+                       int zpad, int overlap, int blur_radius, float threshold, int delta, int delta_fit,
+                       float sigmaZ, float sigmaXY, int batch, float *out, uint32_t out_cap, uint32_t *count_dev,
+                       uint32_t *overflow_dev, void *stream);
+int mm_dapi_spots_async(mm_ctx *ctx, const uint16_t *image, int Z, int X, int Y, int64_t isz, int64_t isx,
+                        const float *flat, int64_t fsx, const void *W, int npsf, const void *zop, int tile_size,
+                        int zpad, int overlap, int blur_radius, float threshold, int delta, int delta_fit,
+                        float sigmaZ, float sigmaXY, int batch, float *buffer, float *out_plus, uint32_t cap_plus,
+                        float *out_minus, uint32_t cap_minus, uint32_t *counts_dev, float *rms_dev, void *stream);
+
 /* Tile layout of Deconvolver.tiled / tile_wise (mermake/deconvolver.py:117-148,
  * 186-206), host only (no device work).  tile < 0 returns the number of tiles.
  * desc (13 int32): x, y, x0, y0, xd, yd, xstart, ystart, xend, yend, psf index,

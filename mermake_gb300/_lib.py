@@ -61,6 +61,11 @@ _SIGS = {
                       _i32, _i32, _f32, _f32, _i32, _vp, _u32, _pu32, _vp], _i32),
     "mm_dapi_spots": ([_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i64, _vp, _i32, _vp, _i32, _i32, _i32, _i32,
                        _f32, _i32, _i32, _f32, _f32, _i32, _vp, _vp, _u32, _pu32, _vp, _u32, _pu32, _pf32, _vp], _i32),
+    "mm_hyb_spots_async": ([_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i64, _vp, _i32, _vp, _i32, _i32, _i32,
+                            _i32, _f32, _i32, _i32, _f32, _f32, _i32, _vp, _u32, _vp, _vp, _vp], _i32),
+    "mm_dapi_spots_async": ([_vp, _vp, _i32, _i32, _i32, _i64, _i64, _vp, _i64, _vp, _i32, _vp, _i32, _i32, _i32,
+                             _i32, _f32, _i32, _i32, _f32, _f32, _i32, _vp, _vp, _u32, _vp, _u32, _vp, _vp, _vp],
+                            _i32),
     "mm_tile_geometry": ([_i32] * 8 + [_vp] * 4, _i32),
     "mm_fft_c2c": ([_vp, _i32, _i32, _i32, _vp], _i32),
     "mm_median_f32": ([_vp, _vp, _i64, _pf32, _vp, _vp], _i32),

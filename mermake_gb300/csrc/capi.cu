@@ -5,7 +5,9 @@
 #include <string.h>
 
 #include <atomic>
+#include <map>
 #include <mutex>
+#include <utility>
 
 #include "deconv.cuh"
 
@@ -17,6 +19,19 @@ enum Slot { WS_SPEC = 0, WS_RES, WS_TMP, WS_VOL, WS_CAND, WS_SMALL, WS_SELECT, W
 
 static std::atomic<unsigned long long> g_launches{0};
 void mm_launch_counter_add() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+int mm_set_smem(const void *fn, size_t bytes) {
+    static std::mutex mu;
+    static std::map<std::pair<int, const void *>, size_t> done;
+    int dev = 0;
+    MM_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    size_t &cur = done[{dev, fn}];
+    if (bytes <= cur) return MM_OK;
+    MM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
+    return MM_OK;
+}
 unsigned long long mm_launch_counter_get() { return g_launches.load(); }
 
 void mm_set_error(const char *fmt, ...) {
@@ -383,6 +398,62 @@ int mm_find_local_maxima(mm_ctx *c, const float *image, int Z, int X, int Y, int
     return MM_EDEVICE;
 }
 
+}  // extern "C"
+
+// The tile batches of one colour into out / sm->rows (candidates through
+// cand[0, cap), overflow noted in sm->overflow): the body of mm_hyb_spots and
+// mm_hyb_spots_async.
+static int hyb_pass(mm_ctx *c, const TileGeom &g, int batch, const uint16_t *image, const float *flat,
+                    const void *W, const void *zop, int blur_radius, float threshold, int delta, int delta_fit,
+                    float sigmaZ, float sigmaXY, float *out, uint32_t out_cap, void *cand, size_t cap, Small *sm,
+                    cudaStream_t st) {
+    int rc;
+    const int nt = ntiles_of(g);
+    MM_CUDA_TRY(cudaMemsetAsync(&sm->overflow, 0, sizeof(unsigned), st));
+    for (int t0 = 0; t0 < nt; t0 += batch) {
+        TileGeom gb = g;
+        gb.t0 = t0;
+        gb.nt = (t0 + batch <= nt) ? batch : nt - t0;
+        if ((rc = run_tiles(c, gb, image, MM_DTYPE_U16, flat, (const float2 *)W, (const float2 *)zop, blur_radius,
+                            nullptr, nullptr, nullptr, 0, 0, st)))
+            return rc;
+        MaximaArgs a = {};
+        a.img = (const float *)c->ws[WS_RES];
+        a.isz = (long long)g.P * g.P; a.isx = g.P; a.ivol = (long long)g.Z * g.P * g.P;
+        a.Z = g.Z; a.X = 0; a.Y = 0; a.nvol = gb.nt;
+        a.tiles = &gb;
+        a.raw_kind = 2; a.chan = image; a.flat = flat;
+        a.th = threshold; a.delta = delta; a.delta_fit = delta_fit;
+        a.sigmaZ = sigmaZ; a.sigmaXY = sigmaXY;
+        a.div = 0.f; a.divp = nullptr; a.neg = 0; a.keep_filter = 1;
+        {
+            double vb = 0;
+            for (int t = gb.t0; t < gb.t0 + gb.nt; ++t) {
+                TileDesc d = mm_tile_desc(gb, t);
+                vb += 4.0 * g.Z * d.xend * d.yend;
+            }
+            StageTimer tm(c, ST_MAXIMA_FIT, vb, st);
+            if ((rc = mm_launch_maxima_fit(a, (uint2 *)cand, (unsigned)cap, &sm->cand, out, out_cap, &sm->rows,
+                                           t0 == 0, st)))
+                return rc;
+        }
+        if ((rc = mm_launch_note_overflow(&sm->cand, (unsigned)cap, &sm->overflow, st))) return rc;
+    }
+    return MM_OK;
+}
+
+// the candidate list: at least 1 M entries, as large as any earlier call made it
+static int cand_list(mm_ctx *c, void **cand, size_t *cap) {
+    size_t n = c->ws_bytes[WS_CAND] / sizeof(uint2);
+    if (n < (1u << 20)) n = 1u << 20;
+    int rc = ws_get(c, WS_CAND, n * sizeof(uint2), cand);
+    if (rc) return rc;
+    *cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
+    return MM_OK;
+}
+
+extern "C" {
+
 int mm_hyb_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t isz, int64_t isx,
                  const float *flat, int64_t fsx, const void *W, int npsf, const void *zop, int tile_size, int zpad,
                  int overlap, int blur_radius, float threshold, int delta, int delta_fit, float sigmaZ, float sigmaXY,
@@ -401,41 +472,12 @@ int mm_hyb_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t 
     if ((rc = small_get(c, &sm))) return rc;
     *count = 0;
     for (int attempt = 0; attempt < 2; ++attempt) {
-        size_t cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
-        if (cap < (1u << 20)) cap = 1u << 20;
         void *cand;
-        if ((rc = ws_get(c, WS_CAND, cap * sizeof(uint2), &cand))) return rc;
-        cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
-        MM_CUDA_TRY(cudaMemsetAsync(&sm->overflow, 0, sizeof(unsigned), st));
-        for (int t0 = 0; t0 < nt; t0 += batch) {
-            TileGeom gb = g;
-            gb.t0 = t0;
-            gb.nt = (t0 + batch <= nt) ? batch : nt - t0;
-            if ((rc = run_tiles(c, gb, image, MM_DTYPE_U16, flat, (const float2 *)W, (const float2 *)zop, blur_radius,
-                                nullptr, nullptr, nullptr, 0, 0, st)))
-                return rc;
-            MaximaArgs a = {};
-            a.img = (const float *)c->ws[WS_RES];
-            a.isz = (long long)g.P * g.P; a.isx = g.P; a.ivol = (long long)g.Z * g.P * g.P;
-            a.Z = Z; a.X = 0; a.Y = 0; a.nvol = gb.nt;
-            a.tiles = &gb;
-            a.raw_kind = 2; a.chan = image; a.flat = flat;
-            a.th = threshold; a.delta = delta; a.delta_fit = delta_fit;
-            a.sigmaZ = sigmaZ; a.sigmaXY = sigmaXY;
-            a.div = 0.f; a.divp = nullptr; a.neg = 0; a.keep_filter = 1;
-            {
-                double vb = 0;
-                for (int t = gb.t0; t < gb.t0 + gb.nt; ++t) {
-                    TileDesc d = mm_tile_desc(gb, t);
-                    vb += 4.0 * Z * d.xend * d.yend;
-                }
-                StageTimer tm(c, ST_MAXIMA_FIT, vb, st);
-                if ((rc = mm_launch_maxima_fit(a, (uint2 *)cand, (unsigned)cap, &sm->cand, out, out_cap, &sm->rows,
-                                               t0 == 0, st)))
-                    return rc;
-            }
-            if ((rc = mm_launch_note_overflow(&sm->cand, (unsigned)cap, &sm->overflow, st))) return rc;
-        }
+        size_t cap;
+        if ((rc = cand_list(c, &cand, &cap))) return rc;
+        if ((rc = hyb_pass(c, g, batch, image, flat, W, zop, blur_radius, threshold, delta, delta_fit, sigmaZ,
+                           sigmaXY, out, out_cap, cand, cap, sm, st)))
+            return rc;
         MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters, &sm->rows, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
         MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters + 2, &sm->overflow, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
         MM_CUDA_TRY(cudaStreamSynchronize(st));
@@ -449,6 +491,87 @@ int mm_hyb_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t 
     mm_set_error("candidate list did not converge");
     return MM_EDEVICE;
 }
+
+int mm_hyb_spots_async(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t isz, int64_t isx,
+                       const float *flat, int64_t fsx, const void *W, int npsf, const void *zop, int tile_size,
+                       int zpad, int overlap, int blur_radius, float threshold, int delta, int delta_fit,
+                       float sigmaZ, float sigmaXY, int batch, float *out, uint32_t out_cap, uint32_t *count_dev,
+                       uint32_t *overflow_dev, void *stream) {
+    MM_REQUIRE(c && image && W && count_dev && overflow_dev, "null argument");
+    MM_REQUIRE(delta <= 5, "Delta must be an less than or equal to 5 due to MAX_KERNEL_POINTS");
+    MM_REQUIRE(delta >= 0 && delta_fit >= 0, "negative delta");
+    TileGeom g;
+    int rc = fill_geom(g, Z, X, Y, isz, isx, fsx, tile_size, zpad, overlap, npsf);
+    if (rc) return rc;
+    const int nt = ntiles_of(g);
+    if (batch <= 0) batch = nt;
+    std::lock_guard<std::mutex> lock(c->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    Small *sm;
+    if ((rc = small_get(c, &sm))) return rc;
+    void *cand;
+    size_t cap;
+    if ((rc = cand_list(c, &cand, &cap))) return rc;
+    if ((rc = hyb_pass(c, g, batch, image, flat, W, zop, blur_radius, threshold, delta, delta_fit, sigmaZ, sigmaXY,
+                       out, out_cap, cand, cap, sm, st)))
+        return rc;
+    MM_CUDA_TRY(cudaMemcpyAsync(count_dev, &sm->rows, sizeof(unsigned), cudaMemcpyDeviceToDevice, st));
+    MM_CUDA_TRY(cudaMemcpyAsync(overflow_dev, &sm->overflow, sizeof(unsigned), cudaMemcpyDeviceToDevice, st));
+    return MM_OK;
+}
+
+}  // extern "C"
+
+// The DAPI block into out_plus / sm->rows and out_minus / sm->rows2 (stitched
+// deconvolution into buffer, the RMS divisor in sm->div, both signs' maxima
+// through the two halves of cand[0, cap), overflow noted in sm->overflow): the
+// body of mm_dapi_spots and mm_dapi_spots_async.
+static int dapi_pass(mm_ctx *c, const TileGeom &g, int batch, const uint16_t *image, int64_t isz, int64_t isx,
+                     const float *flat, const void *W, const void *zop, int blur_radius, float threshold, int delta,
+                     int delta_fit, float sigmaZ, float sigmaXY, float *buffer, float *out_plus, uint32_t cap_plus,
+                     float *out_minus, uint32_t cap_minus, void *cand, size_t cap, Small *sm, cudaStream_t st) {
+    int rc;
+    const int nt = ntiles_of(g);
+    const int Z = g.Z, X = g.X, Y = g.Y;
+    const long long N = (long long)Z * X * Y;
+    MM_CUDA_TRY(cudaMemsetAsync(buffer, 0, sizeof(float) * N, st));
+    for (int t0 = 0; t0 < nt; t0 += batch) {
+        TileGeom gb = g;
+        gb.t0 = t0;
+        gb.nt = (t0 + batch <= nt) ? batch : nt - t0;
+        if ((rc = run_tiles(c, gb, image, MM_DTYPE_U16, flat, (const float2 *)W, (const float2 *)zop, blur_radius,
+                            nullptr, nullptr, buffer, (long long)X * Y, Y, st)))
+            return rc;
+    }
+    {
+        StageTimer tm(c, ST_SUMSQ, 4.0 * N, st);
+        if ((rc = mm_launch_sumsq(buffer, N, sm->parts, &sm->sumsq, st))) return rc;
+    }
+    if ((rc = mm_launch_rms_div(&sm->sumsq, N, &sm->div, st))) return rc;
+    MM_CUDA_TRY(cudaMemsetAsync(&sm->overflow, 0, sizeof(unsigned), st));
+    // v / rms and -v / rms in one maxima pass: the candidates of each sign in
+    // one half of the list, counted in rows / rows2
+    MaximaArgs a = {};
+    a.img = buffer; a.isz = (long long)X * Y; a.isx = Y; a.ivol = 0;
+    a.Z = Z; a.X = X; a.Y = Y; a.nvol = 1;
+    a.tiles = nullptr;
+    a.raw_kind = 1; a.raw = image; a.rsz = isz; a.rsx = isx; a.rvol = 0;
+    a.th = threshold; a.delta = delta; a.delta_fit = delta_fit;
+    a.sigmaZ = sigmaZ; a.sigmaXY = sigmaXY;
+    a.div = 0.f; a.divp = &sm->div; a.neg = 0; a.keep_filter = 0;
+    const unsigned half = (unsigned)(cap / 2);
+    {
+        StageTimer tm(c, ST_MAXIMA_FIT, 4.0 * N, st);
+        if ((rc = mm_launch_maxima_fit_pm(a, (uint2 *)cand, half, &sm->rows, &sm->rows2, out_plus, cap_plus,
+                                          out_minus, cap_minus, st)))
+            return rc;
+    }
+    if ((rc = mm_launch_note_overflow(&sm->rows, half, &sm->overflow, st))) return rc;
+    if ((rc = mm_launch_note_overflow(&sm->rows2, half, &sm->overflow, st))) return rc;
+    return MM_OK;
+}
+
+extern "C" {
 
 int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t isz, int64_t isx,
                   const float *flat, int64_t fsx, const void *W, int npsf, const void *zop, int tile_size, int zpad,
@@ -468,49 +591,13 @@ int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t
     cudaStream_t st = (cudaStream_t)stream;
     Small *sm;
     if ((rc = small_get(c, &sm))) return rc;
-    const long long N = (long long)Z * X * Y;
-    MM_CUDA_TRY(cudaMemsetAsync(buffer, 0, sizeof(float) * N, st));
-    for (int t0 = 0; t0 < nt; t0 += batch) {
-        TileGeom gb = g;
-        gb.t0 = t0;
-        gb.nt = (t0 + batch <= nt) ? batch : nt - t0;
-        if ((rc = run_tiles(c, gb, image, MM_DTYPE_U16, flat, (const float2 *)W, (const float2 *)zop, blur_radius,
-                            nullptr, nullptr, buffer, (long long)X * Y, Y, st)))
-            return rc;
-    }
-    {
-        StageTimer tm(c, ST_SUMSQ, 4.0 * N, st);
-        if ((rc = mm_launch_sumsq(buffer, N, sm->parts, &sm->sumsq, st))) return rc;
-    }
-    if ((rc = mm_launch_rms_div(&sm->sumsq, N, &sm->div, st))) return rc;
     for (int attempt = 0; attempt < 2; ++attempt) {
-        size_t cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
-        if (cap < (1u << 20)) cap = 1u << 20;
         void *cand;
-        if ((rc = ws_get(c, WS_CAND, cap * sizeof(uint2), &cand))) return rc;
-        cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
-        MM_CUDA_TRY(cudaMemsetAsync(&sm->overflow, 0, sizeof(unsigned), st));
-        {
-            // v / rms and -v / rms in one maxima pass: the candidates of each
-            // sign in one half of the list, counted in rows / rows2
-            MaximaArgs a = {};
-            a.img = buffer; a.isz = (long long)X * Y; a.isx = Y; a.ivol = 0;
-            a.Z = Z; a.X = X; a.Y = Y; a.nvol = 1;
-            a.tiles = nullptr;
-            a.raw_kind = 1; a.raw = image; a.rsz = isz; a.rsx = isx; a.rvol = 0;
-            a.th = threshold; a.delta = delta; a.delta_fit = delta_fit;
-            a.sigmaZ = sigmaZ; a.sigmaXY = sigmaXY;
-            a.div = 0.f; a.divp = &sm->div; a.neg = 0; a.keep_filter = 0;
-            const unsigned half = (unsigned)(cap / 2);
-            {
-                StageTimer tm(c, ST_MAXIMA_FIT, 4.0 * N, st);
-                if ((rc = mm_launch_maxima_fit_pm(a, (uint2 *)cand, half, &sm->rows, &sm->rows2, out_plus, cap_plus,
-                                                  out_minus, cap_minus, st)))
-                    return rc;
-            }
-            if ((rc = mm_launch_note_overflow(&sm->rows, half, &sm->overflow, st))) return rc;
-            if ((rc = mm_launch_note_overflow(&sm->rows2, half, &sm->overflow, st))) return rc;
-        }
+        size_t cap;
+        if ((rc = cand_list(c, &cand, &cap))) return rc;
+        if ((rc = dapi_pass(c, g, batch, image, isz, isx, flat, W, zop, blur_radius, threshold, delta, delta_fit,
+                            sigmaZ, sigmaXY, buffer, out_plus, cap_plus, out_minus, cap_minus, cand, cap, sm, st)))
+            return rc;
         MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters, &sm->rows, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
         float hdiv = 0.f;
         MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters + 4, &sm->div, sizeof(float), cudaMemcpyDeviceToHost, st));
@@ -526,6 +613,36 @@ int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t
     }
     mm_set_error("candidate list did not converge");
     return MM_EDEVICE;
+}
+
+int mm_dapi_spots_async(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t isz, int64_t isx,
+                        const float *flat, int64_t fsx, const void *W, int npsf, const void *zop, int tile_size,
+                        int zpad, int overlap, int blur_radius, float threshold, int delta, int delta_fit,
+                        float sigmaZ, float sigmaXY, int batch, float *buffer, float *out_plus, uint32_t cap_plus,
+                        float *out_minus, uint32_t cap_minus, uint32_t *counts_dev, float *rms_dev, void *stream) {
+    MM_REQUIRE(c && image && W && buffer && counts_dev, "null argument");
+    MM_REQUIRE(delta <= 5, "Delta must be an less than or equal to 5 due to MAX_KERNEL_POINTS");
+    MM_REQUIRE(delta >= 0 && delta_fit >= 0, "negative delta");
+    MM_REQUIRE(overlap >= 1, "stitching needs overlap >= 1");
+    TileGeom g;
+    int rc = fill_geom(g, Z, X, Y, isz, isx, fsx, tile_size, zpad, overlap, npsf);
+    if (rc) return rc;
+    const int nt = ntiles_of(g);
+    if (batch <= 0) batch = nt;
+    std::lock_guard<std::mutex> lock(c->mu);
+    cudaStream_t st = (cudaStream_t)stream;
+    Small *sm;
+    if ((rc = small_get(c, &sm))) return rc;
+    void *cand;
+    size_t cap;
+    if ((rc = cand_list(c, &cand, &cap))) return rc;
+    if ((rc = dapi_pass(c, g, batch, image, isz, isx, flat, W, zop, blur_radius, threshold, delta, delta_fit, sigmaZ,
+                        sigmaXY, buffer, out_plus, cap_plus, out_minus, cap_minus, cand, cap, sm, st)))
+        return rc;
+    // rows, rows2 and overflow are consecutive in Small
+    MM_CUDA_TRY(cudaMemcpyAsync(counts_dev, &sm->rows, 3 * sizeof(unsigned), cudaMemcpyDeviceToDevice, st));
+    if (rms_dev) MM_CUDA_TRY(cudaMemcpyAsync(rms_dev, &sm->div, sizeof(float), cudaMemcpyDeviceToDevice, st));
+    return MM_OK;
 }
 
 }  // extern "C"

@@ -29,8 +29,7 @@ constexpr int kBlurThreads = 512;  // k_blur_x_sub, k_make_raw
 
 template <typename K>
 int set_smem(K *kernel, size_t bytes) {
-    MM_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-    return MM_OK;
+    return mm_set_smem((const void *)kernel, bytes);
 }
 
 // ---------------------------------------------------------------------------

@@ -945,7 +945,7 @@ static inline unsigned fft_grid(long long ngroups, FftCfg c) {
 
 static inline int launch_fft_kernel(const void *fn, dim3 grid, size_t sm, cudaStream_t st, void **args,
                                     int threads = kFftThreads) {
-    MM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    if (int rc = mm_set_smem(fn, sm)) return rc;
     MM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(threads), args, sm, st));
     mm_launch_counter_add();
     return MM_OK;

@@ -127,7 +127,7 @@ int mm_launch_zpass(const TileGeom &g, float2 *S, const float2 *W, long long wst
     TileGeom ga = g;
     void *args[] = {&ga, &S, &W, &wstride, &P, &nl, &tg};
     const void *fn = MM_BY_CLASS(P, k_zpass, );
-    MM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    if ((rc = mm_set_smem(fn, sm))) return rc;
     MM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(kZThreads), args, sm, st));
     mm_launch_counter_add();
     return MM_OK;

@@ -38,6 +38,11 @@
 void mm_set_error(const char *fmt, ...);
 // Counts kernel launches made by this library (mm_launch_count()).
 void mm_launch_counter_add();
+// Raises a kernel's dynamic shared-memory limit to `bytes` once per (device,
+// kernel) and size: later launches make no attribute call, so launches
+// recorded into a CUDA graph after one eager pass make no driver call but the
+// launch itself.
+int mm_set_smem(const void *fn, size_t bytes);
 unsigned long long mm_launch_counter_get();
 
 static inline int mm_cdiv(long a, long b) { return (int)((a + b - 1) / b); }

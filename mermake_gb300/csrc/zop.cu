@@ -386,7 +386,7 @@ int mm_launch_zconv(float2 *S, const float2 *w, long long wstride, int Z, int zp
                Z, zpad);
     if (nt <= 0) return MM_OK;
     const size_t sm = mm_zconv_smem(Z, Zp);
-    MM_CUDA_TRY(cudaFuncSetAttribute(k_zconv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    if (int rc = mm_set_smem((const void *)k_zconv, sm)) return rc;
     const int threads = (Z + kCI - 1) / kCI * 32;
     dim3 grid((unsigned)((plane + kCq - 1) / kCq), (unsigned)nt);
     k_zconv<<<grid, threads, sm, st>>>(S, w, wstride, Z, zpad, Zp, plane, t0, npsf);
@@ -397,7 +397,7 @@ int mm_launch_zconv(float2 *S, const float2 *w, long long wstride, int Z, int zp
 int mm_zker_build_impl(const float2 *W, int Zp, long long plane, float2 *w, cudaStream_t st) {
     MM_REQUIRE(Zp >= 1 && Zp <= MM_ZOP_MAX_ZP, "z kernel needs 1 <= Zp <= %d (got %d)", MM_ZOP_MAX_ZP, Zp);
     const size_t sm = sizeof(float2) * (size_t)Zp * (kBuildP + 1);
-    MM_CUDA_TRY(cudaFuncSetAttribute(k_zker_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    if (int rc = mm_set_smem((const void *)k_zker_build, sm)) return rc;
     k_zker_build<<<(unsigned)((plane + kBuildP - 1) / kBuildP), kBuildThreads, sm, st>>>(W, w, Zp, plane);
     MM_CHECK_LAUNCH();
     return MM_OK;
@@ -437,7 +437,7 @@ int mm_launch_zop_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, lon
     MM_REQUIRE(sm <= 227 * 1024, "z operator shared memory %zu bytes exceeds the limit", sm);
     const void *fn = Z == 50 ? ((plane % 2 == 0) ? (const void *)k_zop_apply<true, 50> : (const void *)k_zop_apply<false, 50>)
                              : ((plane % 2 == 0) ? (const void *)k_zop_apply<true, 0> : (const void *)k_zop_apply<false, 0>);
-    MM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    if (int rc = mm_set_smem(fn, sm)) return rc;
     dim3 grid((unsigned)((plane + kPB - 1) / kPB));
     void *args[] = {&S, &w, &Z, &Zp, &plane, &nt, &ign, &tgn, &tab};
     MM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(threads), args, sm, st));

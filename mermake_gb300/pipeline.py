@@ -206,3 +206,155 @@ class FovRunner:
         done.record(cur)
         self._slots[ticket["slot"]]["free"] = done
         return out_plus, out_minus, rows
+
+
+def _settings(args):
+    """The driver settings of a TOML section (defaults as hyb_spots')."""
+    a = dict(args or {})
+    th = a.get("threshold")
+    br = a.get("blur_radius")
+    delta = int(a.get("delta", 1))
+    _check_delta(delta)
+    return dict(th=float("nan") if th is None else float(th), br=-1 if br is None else int(br), delta=delta,
+                dfit=int(a.get("delta_fit", 0)), sz=float(a.get("sigmaZ", 1)), sxy=float(a.get("sigmaXY", 1.5)))
+
+
+class FovGraph:
+    """One whole FOV -- the DAPI block and every colour -- captured once as a
+    CUDA graph and replayed for each FOV of the same shape (no counterpart in
+    the reference, whose loop launches every kernel from Python;
+    mermake/__main__.py:211-283).
+
+    The graph runs ``mm_dapi_spots_async`` and ``mm_hyb_spots_async`` on a
+    library context of its own (nothing else grows its scratch, whose addresses
+    the graph holds) into static buffers: inputs ``dapi`` (Z, X, Y) and
+    ``colours`` (n, Z, X, Y) uint16 -- the caller's device tensors when given
+    as ``inputs=(dapi, [colours])``, else buffers of the graph's own that
+    ``run`` fills -- and per-output row buffers sized from the counts the
+    Deconvolvers have seen (``hyb_spots``' rule).  One eager pass sizes the
+    context's scratch before capture.  ``run`` replays and reads every count
+    in one transfer; a FOV whose rows or candidates did not fit falls back to
+    the synchronous drivers (``fallbacks`` counts them).  Flat fields are fixed
+    at construction.
+    """
+
+    def __init__(self, dec_hyb, dec_dapi, shape, n_colours, hyb_args=None, dapi_args=None, flats=None,
+                 dapi_flat=None, batch=0, inputs=None):
+        self.shape = tuple(int(v) for v in shape)
+        Z, X, Y = self.shape
+        self.dec_hyb, self.dec_dapi = dec_hyb, dec_dapi
+        self.hyb_args, self.dapi_args = dict(hyb_args or {}), dict(dapi_args or {})
+        self._h, self._d = _settings(self.hyb_args), _settings(self.dapi_args)
+        self.n = int(n_colours)
+        self.fallbacks = 0
+        self.dev = torch.cuda.current_device()
+        dev = torch.device("cuda", self.dev)
+        self._ctx = _lib._vp()
+        _lib.check(_lib.lib().mm_ctx_create(C.byref(self._ctx)))
+        if inputs is not None:
+            self.dapi = _u16_channel(inputs[0]) if dec_dapi is not None else None
+            self.colours = [_u16_channel(t) for t in inputs[1]]
+        else:
+            self.dapi = torch.zeros(self.shape, dtype=torch.uint16, device=dev) if dec_dapi is not None else None
+            self.colours = [torch.zeros(self.shape, dtype=torch.uint16, device=dev) for _ in range(self.n)]
+        if len(self.colours) != self.n or any(tuple(t.shape) != self.shape for t in self.colours):
+            raise ValueError("colour inputs must be n_colours tensors of the FOV shape")
+        self.flats = [_flat(f, self.shape) for f in (flats if flats is not None else [None] * self.n)]
+        self.dapi_flat = _flat(dapi_flat, self.shape)
+        self.batch_h = max(int(tune.batch_for(dec_hyb, self.shape) if batch == 0 else batch), 0)
+        self.cap = _capacity(dec_hyb, ("hyb", Z, X, Y), 1 << 18)
+        self.rows = [torch.empty((self.cap, 8), dtype=torch.float32, device=dev) for _ in range(self.n)]
+        # counts: [rows (+), rows (-), DAPI candidate overflow] + [rows, overflow] per colour
+        self.counts = torch.zeros(3 + 2 * self.n, dtype=torch.int32, device=dev)
+        self.rms = torch.zeros(1, dtype=torch.float32, device=dev)
+        if dec_dapi is not None:
+            self.batch_d = max(int(tune.batch_for(dec_dapi, self.shape, dapi=True) if batch == 0 else batch), 0)
+            self.cap_p = _capacity(dec_dapi, ("dapi+", Z, X, Y), 1 << 16)
+            self.cap_m = _capacity(dec_dapi, ("dapi-", Z, X, Y), 1 << 16)
+            self.plus = torch.empty((self.cap_p, 8), dtype=torch.float32, device=dev)
+            self.minus = torch.empty((self.cap_m, 8), dtype=torch.float32, device=dev)
+            self.buffer = torch.empty(self.shape, dtype=torch.float32, device=dev)
+        self._stream = torch.cuda.Stream(device=dev)
+        with torch.cuda.stream(self._stream):
+            self._issue()  # eager: sizes the context's scratch and the transform plans
+        self._stream.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        n0 = _lib.launch_count()
+        with torch.cuda.graph(self.graph, stream=self._stream, capture_error_mode="thread_local"):
+            self._issue()
+        self._stream.synchronize()
+        self.launches = _lib.launch_count() - n0  # library kernels one replay runs
+
+    def _issue(self):
+        L = _lib.lib()
+        Z, X, Y = self.shape
+        sp = _lib.stream_ptr(torch.cuda.current_stream())
+        cbase = self.counts.data_ptr()
+        if self.dec_dapi is not None:
+            d, a, img, fl = self.dec_dapi, self._d, self.dapi, self.dapi_flat
+            _lib.check(L.mm_dapi_spots_async(
+                self._ctx, _lib.ptr(img), Z, X, Y, img.stride(0), img.stride(1), _lib.ptr(fl),
+                fl.stride(0) if fl is not None else 0, _lib.ptr(d.psf_fft), d.psf_fft.shape[0],
+                _lib.ptr(d.z_operator), d.tile_size, d.zpad, d.overlap, a["br"], a["th"], a["delta"], a["dfit"],
+                a["sz"], a["sxy"], self.batch_d, _lib.ptr(self.buffer), _lib.ptr(self.plus), self.cap_p,
+                _lib.ptr(self.minus), self.cap_m, _lib._vp(cbase), _lib.ptr(self.rms), sp))
+        d, a = self.dec_hyb, self._h
+        for c in range(self.n):
+            img, fl = self.colours[c], self.flats[c]
+            _lib.check(L.mm_hyb_spots_async(
+                self._ctx, _lib.ptr(img), Z, X, Y, img.stride(0), img.stride(1), _lib.ptr(fl),
+                fl.stride(0) if fl is not None else 0, _lib.ptr(d.psf_fft), d.psf_fft.shape[0],
+                _lib.ptr(d.z_operator), d.tile_size, d.zpad, d.overlap, a["br"], a["th"], a["delta"], a["dfit"],
+                a["sz"], a["sxy"], self.batch_h, _lib.ptr(self.rows[c]), self.cap, _lib._vp(cbase + 4 * (3 + 2 * c)),
+                _lib._vp(cbase + 4 * (4 + 2 * c)), sp))
+
+    def replay(self):
+        """Replays the graph on the current stream (inputs already in place)."""
+        self.graph.replay()
+
+    def results(self):
+        """Device views of the last replay: (Xh_plus, Xh_minus, [Xh per colour]),
+        or None when an output or a candidate list overflowed."""
+        cnt = self.counts.cpu().tolist()
+        if self.dec_dapi is not None and (cnt[2] or cnt[0] > self.cap_p or cnt[1] > self.cap_m):
+            return None
+        if any(cnt[4 + 2 * c] or cnt[3 + 2 * c] > self.cap for c in range(self.n)):
+            return None
+        plus = self.plus[:cnt[0]] if self.dec_dapi is not None else None
+        minus = self.minus[:cnt[1]] if self.dec_dapi is not None else None
+        return plus, minus, [self.rows[c][:cnt[3 + 2 * c]] for c in range(self.n)]
+
+    def run(self, dapi=None, colours=None):
+        """(Xh_plus, Xh_minus, [Xh per colour]) host arrays of one FOV: copies
+        the channels given (host or device) into the graph's inputs, replays,
+        and falls back to the synchronous drivers when a result overflowed."""
+        if dapi is not None and self.dapi is not None:
+            self.dapi.copy_(torch.as_tensor(dapi), non_blocking=True)
+        for c, h in enumerate(colours or []):
+            self.colours[c].copy_(torch.as_tensor(h), non_blocking=True)
+        self.replay()
+        got = self.results()
+        if got is None:
+            self.fallbacks += 1
+            plus = minus = None
+            if self.dec_dapi is not None:
+                plus, minus, _, _ = dapi_spots(self.dec_dapi, self.dapi, self.dapi_flat, **self.dapi_args)
+            got = (plus, minus, [hyb_spots(self.dec_hyb, self.colours[c], self.flats[c], **self.hyb_args)
+                                 for c in range(self.n)])
+        plus, minus, xh = got
+        return (plus.cpu().numpy() if plus is not None else None, minus.cpu().numpy() if minus is not None else None,
+                [r.cpu().numpy() for r in xh])
+
+    def close(self):
+        """Frees the graph and the context's scratch."""
+        if self._ctx:
+            torch.cuda.synchronize(self.dev)
+            self.graph = None
+            _lib.check(_lib.lib().mm_ctx_destroy(self._ctx))
+            self._ctx = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

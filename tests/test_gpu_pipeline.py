@@ -170,3 +170,32 @@ def test_autotune_picks_a_batch_and_keeps_rows(mm):
     want = ck.sort_rows(mm["pl"].hyb_spots(dec, dimg, dflat, batch=-1, **HYB).cpu().numpy())
     got = ck.sort_rows(mm["pl"].hyb_spots(dec, dimg, dflat, **HYB).cpu().numpy())
     np.testing.assert_array_equal(got, want)
+
+
+def test_fov_graph_replays_match_direct_calls(mm):
+    """FovGraph (the DAPI block and every colour captured once as a CUDA graph)
+    gives the rows of the direct dapi_spots / hyb_spots calls, for two FOVs of
+    different content replayed through the same graph, without falling back."""
+    Z, X, Y = 12, 170, 150
+    fovs = []
+    for k in range(2):
+        dapi = mm["synth"].dapi_stack(Z, X, Y, 5 + k, n_nuclei=12, radii=(3.0, 12.0, 12.0))
+        cols, flats = [], []
+        for seed in (1 + 10 * k, 2 + 10 * k):
+            img, flat, psf = hyb_case(mm, seed=seed, Z=Z, X=X, Y=Y)
+            cols.append(img)
+            flats.append(torch.from_numpy(flat).cuda())
+        fovs.append((dapi, cols, flats))
+    dh = mm["dc"].Deconvolver(psf, (Z, X, Y), zpad=Z - 1, **HYB)
+    dd = mm["dc"].Deconvolver(psf, (Z, X, Y), zpad=(Z - 1) // 2, **DAPI)
+    flats = fovs[0][2]  # flat fields are fixed per graph
+    with mm["pl"].FovGraph(dh, dd, (Z, X, Y), 2, HYB, DAPI, flats=flats) as g:
+        for dapi, cols, _ in fovs:
+            want_p, want_m, _, _ = mm["pl"].dapi_spots(dd, dapi.cuda(), None, **DAPI)
+            want = [mm["pl"].hyb_spots(dh, c.cuda(), f, **HYB) for c, f in zip(cols, flats)]
+            p, m, rows = g.run(dapi, cols)
+            np.testing.assert_array_equal(ck.sort_rows(p), ck.sort_rows(want_p.cpu().numpy()))
+            np.testing.assert_array_equal(ck.sort_rows(m), ck.sort_rows(want_m.cpu().numpy()))
+            for got, w in zip(rows, want):
+                np.testing.assert_array_equal(ck.sort_rows(got), ck.sort_rows(w.cpu().numpy()))
+        assert g.fallbacks == 0
