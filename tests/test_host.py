@@ -229,3 +229,36 @@ def test_rader_split_matches_the_dft(R, N1, N2, g, inverse):
     X[0] = x[0] + s0
     want = np.fft.ifft(x) * R if inverse else np.fft.fft(x)
     assert np.abs(X - want).max() <= 1e-12 * np.abs(want).max()
+
+
+def test_fov_graph_settings_follow_the_driver_defaults():
+    """FovGraph reads a TOML section as hyb_spots does: None threshold -> NaN
+    (every voxel), None blur -> -1 (no blur), delta > 5 -> TypeError."""
+    from mermake_gb300 import pipeline
+    a = pipeline._settings({"threshold": None, "blur_radius": None})
+    assert np.isnan(a["th"]) and a["br"] == -1 and a["delta"] == 1 and a["dfit"] == 0
+    b = pipeline._settings(dict(threshold=3600, blur_radius=30, delta=1, delta_fit=3, sigmaZ=1, sigmaXY=1.5))
+    assert (b["th"], b["br"], b["dfit"], b["sxy"]) == (3600.0, 30, 3, 1.5)
+    with pytest.raises(TypeError, match="Delta must be"):
+        pipeline._settings({"delta": 6})
+
+
+def test_zpass_flop_model_follows_the_z_pass_form():
+    """bench.zpass_flops: the matrix form (Z x Z complex FMAs per frequency and
+    tile) for one spectrum and >= 10 tiles of height <= 64, else the direct sum
+    (outputs and padded planes in blocks of 8); 8 flops a complex FMA."""
+    import sys
+    import types
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+
+    def dec(Z, zpad, P, npsf, nt):
+        return types.SimpleNamespace(tile_height=Z, Zp=Z + 2 * zpad, P=P, H=P // 2 + 1, z_operator=object(),
+                                     psf_fft=np.zeros((npsf, 1)), n_tiles=lambda shape: nt)
+
+    w = dict(Z=50, X=2048, Y=2048, colours=3)
+    s = dict(dec_h=dec(50, 49, 678, 1, 25), dec_d=dec(50, 24, 678, 1, 25))
+    assert bench.zpass_flops(w, s) == 4 * 25 * 678 * 340 * 2500 * 8.0
+    w = dict(Z=40, X=3000, Y=3000, colours=1)
+    s = dict(dec_h=dec(40, 39, 478, 100, 100), dec_d=None)
+    assert bench.zpass_flops(w, s) == 100 * 478 * 240 * 40 * 120 * 8.0
