@@ -146,10 +146,14 @@ int mm_find_local_maxima(mm_ctx *ctx, const float *image, int Z, int X, int Y, i
  * no allocating routine.  Same arguments and results as mm_find_local_maxima;
  * the caller still owns image, raw, out and count.  Limit: Z*X*Y <= 2,097,152
  * voxels (MM_EINVAL beyond); the array (16 MiB) is held by every GPU that
- * loads the library until the process exits.  The first call on a device
- * looks the array up (cudaGetSymbolAddress) and initialises a table, so make
- * it before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race and must be serialised by the caller. */
+ * loads it until the process exits.  The CUDA runtime loads the library's
+ * device code lazily, so the first call on a device (or the first use of any
+ * maxima entry point there) reserves the array's device memory, uploads the
+ * neighbour tables, looks the array up (cudaGetSymbolAddress) and synchronises
+ * the device: make that first call at start-up, before any stream capture and
+ * before the code that must not allocate.  Later calls allocate nothing.  All
+ * calls share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller. */
 int mm_find_local_maxima_noalloc(const float *image, int Z, int X, int Y, int64_t isz, int64_t isx,
                                  const void *raw, int raw_dtype, int64_t rsz, int64_t rsx, float threshold,
                                  int delta, int delta_fit, float sigmaZ, float sigmaXY, float norm_div, int negate,

@@ -24,6 +24,7 @@
 //            (delta_fit = 0) gives NaN for hn and a, as in the reference.
 //            In tile mode the row is kept only if overlap <= xc < xend-overlap and
 //            the same for yc, then shifted by the tile origin (__main__.py:256-260).
+#include <atomic>
 #include <mutex>
 
 #include "deconv.cuh"
@@ -34,21 +35,27 @@ constexpr int kMaxDelta = 5;
 constexpr int kSphereCap = 515;
 __device__ char4 g_sphere[kMaxDelta + 1][kSphereCap];  // neighbour offsets, nearest first
 __device__ int g_sphere_n[kMaxDelta + 1];
-__device__ int g_sphere_ready;
 // fit samples: the sphere |d|^2 <= df^2 incl. the centre, in the reference's
 // (dz, dx, dy) loop order (maxima.cu:190-193)
 __device__ char4 g_fit_sphere[kMaxDelta + 1][kSphereCap];
 __device__ int g_fit_sphere_n[kMaxDelta + 1];
 
-__global__ void k_init_sphere() {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+// Host-side construction of the two tables (the same on every device).
+struct SphereTables {
+    char4 fit[kMaxDelta + 1][kSphereCap];
+    int fit_n[kMaxDelta + 1];
+    char4 nb[kMaxDelta + 1][kSphereCap];
+    int nb_n[kMaxDelta + 1];
+};
+
+void build_sphere_tables(SphereTables &t) {
     for (int d = 0; d <= kMaxDelta; ++d) {
         int n = 0;
         for (int dz = -d; dz <= d; ++dz)
             for (int dx = -d; dx <= d; ++dx)
                 for (int dy = -d; dy <= d; ++dy)
-                    if (dz * dz + dx * dx + dy * dy <= d * d) g_fit_sphere[d][n++] = make_char4(dz, dx, dy, 0);
-        g_fit_sphere_n[d] = n;
+                    if (dz * dz + dx * dx + dy * dy <= d * d) t.fit[d][n++] = make_char4(dz, dx, dy, 0);
+        t.fit_n[d] = n;
     }
     for (int d = 0; d <= kMaxDelta; ++d) {
         int n = 0;
@@ -56,10 +63,9 @@ __global__ void k_init_sphere() {
             for (int dz = -d; dz <= d; ++dz)
                 for (int dx = -d; dx <= d; ++dx)
                     for (int dy = -d; dy <= d; ++dy)
-                        if (dz * dz + dx * dx + dy * dy == r2) g_sphere[d][n++] = make_char4(dz, dx, dy, 0);
-        g_sphere_n[d] = n;
+                        if (dz * dz + dx * dx + dy * dy == r2) t.nb[d][n++] = make_char4(dz, dx, dy, 0);
+        t.nb_n[d] = n;
     }
-    g_sphere_ready = 1;
 }
 
 struct Xform {
@@ -485,15 +491,31 @@ int mm_launch_note_overflow(const unsigned *ncand, unsigned cap, unsigned *overf
     return MM_OK;
 }
 
+// Uploads the neighbour and fit tables to the current device once.  Callers on
+// several host threads may race here for a new device: the per-device flag is
+// atomic and the upload runs under a lock, so exactly one of them uploads and
+// the others wait for it.
 int mm_maxima_ensure_init(cudaStream_t st) {
-    static int done_dev[64] = {0};
+    static std::atomic<int> done_dev[64];
+    static std::mutex mu;
     int dev = 0;
     MM_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 64 && done_dev[dev]) return MM_OK;
-    k_init_sphere<<<1, 1, 0, st>>>();
-    MM_CHECK_LAUNCH();
+    MM_REQUIRE(dev >= 0 && dev < 64, "device index %d out of range", dev);
+    if (done_dev[dev].load(std::memory_order_acquire)) return MM_OK;
+    std::lock_guard<std::mutex> lock(mu);
+    if (done_dev[dev].load(std::memory_order_relaxed)) return MM_OK;
+    static SphereTables tab;
+    static bool built = false;
+    if (!built) {
+        build_sphere_tables(tab);
+        built = true;
+    }
+    MM_CUDA_TRY(cudaMemcpyToSymbolAsync(g_fit_sphere, tab.fit, sizeof(tab.fit), 0, cudaMemcpyHostToDevice, st));
+    MM_CUDA_TRY(cudaMemcpyToSymbolAsync(g_fit_sphere_n, tab.fit_n, sizeof(tab.fit_n), 0, cudaMemcpyHostToDevice, st));
+    MM_CUDA_TRY(cudaMemcpyToSymbolAsync(g_sphere, tab.nb, sizeof(tab.nb), 0, cudaMemcpyHostToDevice, st));
+    MM_CUDA_TRY(cudaMemcpyToSymbolAsync(g_sphere_n, tab.nb_n, sizeof(tab.nb_n), 0, cudaMemcpyHostToDevice, st));
     MM_CUDA_TRY(cudaStreamSynchronize(st));
-    if (dev < 64) done_dev[dev] = 1;
+    done_dev[dev].store(1, std::memory_order_release);
     return MM_OK;
 }
 
@@ -567,13 +589,17 @@ int mm_launch_maxima_fit_pm(const MaximaArgs &a, uint2 *cand, unsigned cap, unsi
 // inside another framework's memory pool or under a fixed device-memory
 // budget, and real-time loops that must not take cudaMalloc's implicit device
 // synchronisation.  For them the candidate list and its counter live in this
-// file-scope array, reserved once when the library is loaded on a device and
-// kept by every GPU that loads the library until the process exits.  Host code
-// may not use the array's name as a device address, so the address is fetched
-// with cudaGetSymbolAddress once per device, with that device current, on the
-// first call; that first call should come before any stream capture.  Every
-// call shares the array: calls whose work overlaps on the GPU (other streams,
-// other host threads) race on it and must be serialised by the caller.
+// file-scope array, which every GPU that loads it keeps until the process
+// exits.  The CUDA runtime loads a module lazily by default (at the first use
+// of one of its kernels or symbols on a device), so the device memory of the
+// array is reserved, and the neighbour tables uploaded, by the first call on
+// each device (or by the first use of any maxima kernel there): that first
+// call allocates and synchronises the device.  Make it at start-up, before any
+// stream capture and before the code that must not allocate.  Host code may
+// not use the array's name as a device address, so that first call fetches
+// the address with cudaGetSymbolAddress, with its device current.  Every call
+// shares the array: calls whose work overlaps on the GPU (other streams, other
+// host threads) race on it and must be serialised by the caller.
 // ---------------------------------------------------------------------------
 #define MM_NOALLOC_MAX_VOXELS (1u << 21)  // 2,097,152 voxels -> 16 MiB of candidates
 #define MM_NOALLOC_HEAD 256               // counter block before the candidate list

@@ -22,7 +22,14 @@ dapi_features.npz
 drift_kat.json
     The drift pickle ``drift_Conv_zscan__020--_set1.pkl`` decoded without CuPy:
     the self-alignment of the dapiFeatures fixture (t = 0, N+ = 621, N- = 261).
+output_layout.json
+    The layout of the reference's output files in ``tests/examples/single/out``:
+    for each ``.npz`` its name, keys, dtypes and shapes and the ``args`` table;
+    for the drift ``.pkl`` the types of its nested structure; and the settings
+    the ``args`` table was written from, as TOML text (values typed back from
+    their ``str`` form).
 """
+import ast
 import bz2
 import json
 import os
@@ -100,5 +107,57 @@ def main(ref):
         json.dump(kat, f, indent=1)
 
 
+def _toml_value(v):
+    if isinstance(v, bool):
+        return "true" if v else "false"
+    if isinstance(v, (int, float)):
+        return repr(v)
+    if isinstance(v, list):
+        return "[" + ", ".join(_toml_value(x) for x in v) + "]"
+    # literal strings (no escapes), triple-quoted where the value holds a quote
+    return ("'''" + v + "'''") if "'" in v else ("'" + v + "'")
+
+
+def _typed(text):
+    try:
+        v = ast.literal_eval(text)
+    except (ValueError, SyntaxError):
+        return text
+    return v if isinstance(v, (bool, int, float, list)) and str(v) == text else text
+
+
+def _structure(obj):
+    if isinstance(obj, (list, tuple)):
+        return [type(obj).__name__] + [_structure(x) for x in obj]
+    if isinstance(obj, np.ndarray):
+        return "array"
+    return type(obj).__name__
+
+
+def output_layout(ref):
+    out_dir = os.path.join(ref, "tests", "examples", "single", "out")
+    lay = {}
+    for kind, name in (("hyb", "Conv_zscan__020--H1_TEST_set1--col0__Xhfits.npz"),
+                       ("dapi", "Conv_zscan__020--H1_TEST_set1--dapiFeatures.npz")):
+        d = np.load(os.path.join(out_dir, name))
+        lay[kind] = {"file": name, "keys": {k: [d[k].dtype.str, list(d[k].shape)] for k in d.files},
+                     "version": str(d["version"])}
+        args = d["args"].tolist()
+        lay["args"] = args
+    blocks = {}
+    for block, key, val in lay["args"]:
+        blocks.setdefault(block, {})[key] = _typed(val)
+    lay["settings_toml"] = "\n".join(
+        "[%s]\n" % b + "".join("%s = %s\n" % (k, _toml_value(v)) for k, v in kv.items()) for b, kv in blocks.items())
+    name = "drift_Conv_zscan__020--_set1.pkl"
+    with open(os.path.join(out_dir, name), "rb") as f:
+        obj = _CupyFree(f).load()
+    lay["drift"] = {"file": name, "structure": _structure(obj)}
+    with open(os.path.join(HERE, "output_layout.json"), "w") as f:
+        json.dump(lay, f, indent=1)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MERMAKE_REF", "/root/reference")
+    main(ref)
+    output_layout(ref)

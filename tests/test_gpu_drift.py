@@ -94,3 +94,30 @@ def test_translation_many_points_matches_oracle(al, npts, shift):
     assert ng == no
     np.testing.assert_allclose(tg, to, atol=0.01)
     np.testing.assert_allclose(tg, shift, atol=0.5)
+
+
+def test_drift_save_round_trip_matches_reference_pickle(al, feats, golden_dir, tmp_path):
+    """drift() -> drift_save (align.py:158-176) -> a plain pickle load: the
+    reference pickle's nesting and values (N+ = 621, N- = 261, zero shift),
+    with NumPy arrays in place of CuPy ones."""
+    import pickle
+    kat = json.load(open(os.path.join(golden_dir, "drift_kat.json")))
+    lay = json.load(open(os.path.join(golden_dir, "output_layout.json")))["drift"]
+    im = types.SimpleNamespace(Xh_plus=torch.from_numpy(feats[0]).cuda(), Xh_minus=torch.from_numpy(feats[1]).cuda(),
+                               path=kat["ref_path"])
+    data, _ = al.drift([im])
+    path = tmp_path / lay["file"]
+    al.drift_save(data, str(path))
+
+    class NoCupy(pickle.Unpickler):
+        def find_class(self, module, name):
+            assert not module.startswith("cupy")
+            return super().find_class(module, name)
+
+    with open(path, "rb") as f:
+        drifts, files, ifov, ref_path = NoCupy(f).load()
+    tf, tp, tm, Np, Nm = drifts[0]
+    assert all(isinstance(a, np.ndarray) and a.shape == (3,) for a in (tf, tp, tm))
+    assert isinstance(Np, int) and isinstance(Nm, int) and (Np, Nm) == (621, 261)
+    np.testing.assert_array_equal(tf, kat["drifts"][0][0])
+    assert files == kat["files"] and ref_path == kat["ref_path"]

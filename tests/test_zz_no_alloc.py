@@ -72,3 +72,34 @@ def test_noalloc_reports_overflow_and_rejects_large_volumes(lib):
     rc, _, _ = call(lib, L.mm_find_local_maxima_noalloc, big, rbig, 4, 0.5, 1, 1, False)
     assert rc == lib.MM_EINVAL
     assert "limit" in lib.last_error()
+
+
+def test_noalloc_allocates_no_device_memory_after_first_call(lib):
+    """The property the entry point exists for: once its first call on the
+    device has loaded the device code and reserved the static array, further
+    calls -- of other shapes and settings -- leave the device's free memory
+    unchanged.  Inputs and outputs are allocated before the measurement."""
+    L = lib.lib()
+    cases = [(4, (12, 50, 60), 0.5, 1, 3), (5, (20, 64, 48), 0.55, 2, 2), (6, (8, 100, 90), 0.6, 3, 1)]
+    prepared = []
+    for seed, shape, th, delta, dfit in cases:
+        img, raw = volume(seed, shape)
+        out = torch.zeros((1 << 15, 8), dtype=torch.float32, device="cuda")
+        prepared.append((img, raw, out, th, delta, dfit))
+
+    def run(img, raw, out, th, delta, dfit):
+        n = C.c_uint32(0)
+        rc = L.mm_find_local_maxima_noalloc(lib.ptr(img), *img.shape, img.stride(0), img.stride(1), lib.ptr(raw), 1,
+                                            raw.stride(0), raw.stride(1), th, delta, dfit, 1.0, 1.5, 0.0, 0,
+                                            lib.ptr(out), out.shape[0], C.byref(n), lib.stream_ptr())
+        assert rc == 0, lib.last_error()
+        return n.value
+
+    run(*prepared[0])  # first call: may load the module and reserve the array
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    counts = [run(*p) for p in prepared[1:]] + [run(*prepared[0])]
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert all(c > 0 for c in counts)
+    assert free1 == free0, (free0, free1)
