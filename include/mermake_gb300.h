@@ -54,6 +54,28 @@ const char *mm_last_error(void);
 int mm_ctx_create(mm_ctx **out);
 int mm_ctx_destroy(mm_ctx *ctx);
 
+/* Context options (no reference counterpart).  MM_OPT_BLUR_MODE selects how
+ * the blur subtraction of tile_wise (mermake/deconvolver.py:160-163: the
+ * result minus its box mean along x and y, the window truncated at the
+ * padded tile's edges, mermake/blur.cu:1-52) is computed:
+ *   MM_BLUR_AUTO (default): mm_hyb_spots / mm_dapi_spots (and their _async
+ *     forms) fold it into the z step as the factor 1 - D(kx) D(ky) of each
+ *     frequency (D: the box mean's frequency response), with no box means
+ *     taken on the result, whenever they run the z kernel and every voxel
+ *     they read lies at least the box half-width d inside the tile (hyb:
+ *     overlap >= d + 1 + delta_fit + max(delta, delta_fit); DAPI: overlap >=
+ *     d + 1).  There the truncated box mean equals the circular one, so the
+ *     spots and the stitched buffer are those of the truncated blur up to
+ *     float32 rounding.  mm_deconv_tiles keeps the truncated blur, whose
+ *     edge voxels it returns.
+ *   MM_BLUR_EXACT: every call takes the truncated box means on the result.
+ *   MM_BLUR_SPECTRAL: as AUTO, and mm_deconv_tiles folds as well (overlap >=
+ *     d + 1), so that it returns the volumes the drivers compute (its voxels
+ *     within d of a tile edge then differ from the truncated blur's). */
+enum { MM_OPT_BLUR_MODE = 1 };
+enum { MM_BLUR_AUTO = 0, MM_BLUR_EXACT = 1, MM_BLUR_SPECTRAL = 2 };
+int mm_ctx_set_option(mm_ctx *ctx, int option, int value);
+
 /* fill.reflect (mermake/fill.py:54-111, kernel `mirror` fill.py:6-52), in place.
  * mode 0 = "out" (a[j] = a[2i-j] for j > i), 1 = "in" (for j < i).
  * shape/strides are host arrays of ndim int64 (strides in elements). */

@@ -15,6 +15,8 @@ import torch
 from . import _build
 
 MM_OK, MM_EINVAL, MM_ENOMEM, MM_EOVERFLOW, MM_ETIMEOUT, MM_EDEVICE = range(6)
+MM_OPT_BLUR_MODE = 1
+MM_BLUR_AUTO, MM_BLUR_EXACT, MM_BLUR_SPECTRAL = range(3)
 
 _lock = threading.Lock()
 _lib = None
@@ -45,6 +47,7 @@ _SIGS = {
     "mm_last_error": ([], C.c_char_p),
     "mm_ctx_create": ([C.POINTER(_vp)], _i32),
     "mm_ctx_destroy": ([_vp], _i32),
+    "mm_ctx_set_option": ([_vp, _i32, _i32], _i32),
     "mm_reflect_f32": ([_vp, _i32, _pi64, _pi64, _i32, _i32, _i32, _vp], _i32),
     "mm_box_1d_f32": ([_vp, _pi64, _vp, _pi64, _i32, _i32, _i32, _i32, _i32, _vp], _i32),
     "mm_subtract_u16": ([_vp, _pi64, _vp, _pi64, _vp, _pi64, _i32, _pi64, _i32, _vp], _i32),
@@ -186,3 +189,19 @@ def profile_read(device=None):
 
 def launch_count():
     return int(lib().mm_launch_count())
+
+
+class blur_mode:
+    """Context manager: the calling thread's library context runs with the
+    given blur mode (MM_BLUR_AUTO / MM_BLUR_EXACT / MM_BLUR_SPECTRAL, see
+    mm_ctx_set_option) inside the block and with MM_BLUR_AUTO after it."""
+
+    def __init__(self, mode, device=None):
+        self.mode, self.device = int(mode), device
+
+    def __enter__(self):
+        check(lib().mm_ctx_set_option(ctx(self.device), MM_OPT_BLUR_MODE, self.mode))
+        return self
+
+    def __exit__(self, *exc):
+        check(lib().mm_ctx_set_option(ctx(self.device), MM_OPT_BLUR_MODE, MM_BLUR_AUTO))

@@ -69,6 +69,7 @@ struct mm_ctx {
     size_t ws_bytes[WS_N] = {};
     unsigned *h_counters = nullptr;  // pinned: [0] candidates, [1] rows, [2] rows (2nd set)
     int device = 0;
+    int blur_mode = MM_BLUR_AUTO;    // mm_ctx_set_option(MM_OPT_BLUR_MODE)
     Prof prof;
 };
 
@@ -188,19 +189,43 @@ int fill_geom(TileGeom &g, int Z, int X, int Y, long long isz, long long isx, lo
 }
 
 
-// tile_wise core for tiles [g.t0, g.t0 + g.nt)
+// Whether a call may fold the blur subtraction into the z step (the
+// spectrum times 1 - D(kx) D(ky), mm_blur_response_get): the z step runs from
+// the z kernel, and every voxel the caller reads lies at least delta (the
+// box half-width) from the tile's edges, where the truncated box mean of the
+// reference equals the circular one.  `reach` is how far inside the overlap
+// the caller reads: the stitched centres start at the overlap (reach 0); the
+// kept spots of a hyb tile have centroids inside it and read their maxima and
+// fit neighbourhoods, at most delta_fit + max(delta, delta_fit) closer to the
+// edge.
+bool fold_allowed(const mm_ctx *c, const TileGeom &g, int blur_radius, const float2 *zop, bool driver, int reach) {
+    if (blur_radius < 0 || !zop || c->blur_mode == MM_BLUR_EXACT) return false;
+    if (!driver && c->blur_mode != MM_BLUR_SPECTRAL) return false;
+    const bool zk = (g.npsf == 1 && g.nt >= MM_ZOP_MIN_TILES && mm_zop_supported(g.Z, g.zpad)) ||
+                    mm_zconv_supported(g.Z, g.zpad);
+    return zk && g.ov - reach >= blur_radius / 2 + 1 && 2 * (blur_radius / 2) + 1 <= g.P;
+}
+
+// tile_wise core for tiles [g.t0, g.t0 + g.nt); fold: the blur subtraction
+// runs as a factor of the z step's output (fold_allowed) instead of the y and
+// x box means of the result
 int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *flat, const float2 *W,
               const float2 *zop, int blur_radius, float *res_out, float *raw_out, float *stitch, long long osz,
-              long long osx, cudaStream_t st) {
+              long long osx, cudaStream_t st, bool fold = false) {
     const long long plane_c = (long long)g.P * g.H;
     const long long tile_c = (long long)g.Z * plane_c;
     const long long tile_r = (long long)g.Z * g.P * g.P;
     void *spec, *res, *tmp = nullptr;
     int rc;
+    const int delta = blur_radius >= 0 ? blur_radius / 2 : -1;
+    const float *fresp = nullptr;
+    if (fold && delta >= 0 && (rc = mm_blur_response_get(g.P, delta, &fresp))) return rc;
+    // the box means still to take on the result
+    const int rdelta = fresp ? -1 : delta;
     if ((rc = ws_get(c, WS_SPEC, sizeof(float2) * tile_c * g.nt, &spec))) return rc;
     res = res_out;
     if (!res && (rc = ws_get(c, WS_RES, sizeof(float) * tile_r * g.nt, &res))) return rc;
-    if (blur_radius >= 0 && (rc = ws_get(c, WS_TMP, sizeof(float) * tile_r * g.nt, &tmp))) return rc;
+    if (rdelta >= 0 && (rc = ws_get(c, WS_TMP, sizeof(float) * tile_r * g.nt, &tmp))) return rc;
     float2 *S = (float2 *)spec;
     const long long wstride = (long long)g.Zp * plane_c;
     // algorithmic bytes of each stage for this batch (its inputs read once, outputs written once)
@@ -221,12 +246,14 @@ int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *
     if (zop && g.npsf == 1 && g.nt >= MM_ZOP_MIN_TILES && mm_zop_supported(g.Z, g.zpad)) {
         // the z kernel (Zp per frequency, the size of W) is read once per batch
         StageTimer t(c, ST_ZPASS, 2 * spec_b + 8.0 * wstride, st);
-        if ((rc = mm_launch_zop_apply(S, zop, g.Z, g.zpad, g.Zp, plane_c, g.nt, st))) return rc;
+        if ((rc = mm_launch_zop_apply(S, zop, g.Z, g.zpad, g.Zp, plane_c, g.nt, fresp, st))) return rc;
     } else if (zop && mm_zconv_supported(g.Z, g.zpad)) {
         // each tile's z kernel read once (once per batch when shared)
         StageTimer t(c, ST_ZPASS, 2 * spec_b + (g.npsf == 1 ? 8.0 * wstride : w_b), st);
-        if ((rc = mm_launch_zconv(S, zop, wstride, g.Z, g.zpad, g.Zp, plane_c, g.t0, g.nt, g.npsf, st))) return rc;
+        if ((rc = mm_launch_zconv(S, zop, wstride, g.Z, g.zpad, g.Zp, plane_c, g.t0, g.nt, g.npsf, fresp, st)))
+            return rc;
     } else {
+        MM_REQUIRE(!fresp, "the blur fold needs the z kernel");
         StageTimer t(c, ST_ZPASS, 2 * spec_b + w_b, st);
         if ((rc = mm_launch_zpass(g, S, W, wstride, st))) return rc;
     }
@@ -234,15 +261,17 @@ int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *
         StageTimer t(c, ST_COLS_INV, 2 * spec_b, st);
         if ((rc = mm_launch_cols(S, g.P, g.H, g.H, plane_c, g.nt * g.Z, true, st))) return rc;
     }
-    const int delta = blur_radius >= 0 ? blur_radius / 2 : -1;
     {
-        StageTimer t(c, ST_ROWS_INV, spec_b + real_b * (delta >= 0 ? 2 : 1), st);
-        if ((rc = mm_launch_rows_inv(S, g.nt * g.Z * g.P, g.P, g.H, (float *)res, (float *)tmp, delta, st)))
+        StageTimer t(c, ST_ROWS_INV, spec_b + real_b * (rdelta >= 0 ? 2 : 1), st);
+        if ((rc = mm_launch_rows_inv(S, g.nt * g.Z * g.P, g.P, g.H, (float *)res, (float *)tmp, rdelta, st)))
             return rc;
     }
-    if (delta >= 0 || stitch) {
-        StageTimer t(c, ST_BLUR_X, (delta >= 0 ? 3 : 2) * real_b, st);
-        if ((rc = mm_launch_blur_x_sub(g, (float *)res, (float *)tmp, delta, (float *)res, stitch, osz, osx, st)))
+    if (rdelta >= 0 || stitch) {
+        // with no box mean left to take, only the stitch: the result is final
+        // in res already and is not written back
+        StageTimer t(c, ST_BLUR_X, (rdelta >= 0 ? 3 : 2) * real_b, st);
+        if ((rc = mm_launch_blur_x_sub(g, (float *)res, (float *)tmp, rdelta, rdelta >= 0 ? (float *)res : nullptr,
+                                       stitch, osz, osx, st)))
             return rc;
     }
     if (raw_out) {
@@ -349,8 +378,9 @@ int mm_deconv_tiles(mm_ctx *c, const void *image, int image_dtype, int Z, int X,
     g.t0 = tile_begin;
     g.nt = tile_count;
     std::lock_guard<std::mutex> lock(c->mu);
+    const bool fold = fold_allowed(c, g, blur_radius, (const float2 *)zop, false, 0);
     return run_tiles(c, g, image, image_dtype, flat, (const float2 *)W, (const float2 *)zop, blur_radius, res_out,
-                     raw_out, stitch_out, osz, osx, (cudaStream_t)stream);
+                     raw_out, stitch_out, osz, osx, (cudaStream_t)stream, fold);
 }
 
 int mm_find_local_maxima(mm_ctx *c, const float *image, int Z, int X, int Y, int64_t isz, int64_t isx,
@@ -414,8 +444,10 @@ static int hyb_pass(mm_ctx *c, const TileGeom &g, int batch, const uint16_t *ima
         TileGeom gb = g;
         gb.t0 = t0;
         gb.nt = (t0 + batch <= nt) ? batch : nt - t0;
+        const int reach = delta_fit + (delta > delta_fit ? delta : delta_fit);
+        const bool fold = fold_allowed(c, gb, blur_radius, (const float2 *)zop, true, reach);
         if ((rc = run_tiles(c, gb, image, MM_DTYPE_U16, flat, (const float2 *)W, (const float2 *)zop, blur_radius,
-                            nullptr, nullptr, nullptr, 0, 0, st)))
+                            nullptr, nullptr, nullptr, 0, 0, st, fold)))
             return rc;
         MaximaArgs a = {};
         a.img = (const float *)c->ws[WS_RES];
@@ -539,8 +571,9 @@ static int dapi_pass(mm_ctx *c, const TileGeom &g, int batch, const uint16_t *im
         TileGeom gb = g;
         gb.t0 = t0;
         gb.nt = (t0 + batch <= nt) ? batch : nt - t0;
+        const bool fold = fold_allowed(c, gb, blur_radius, (const float2 *)zop, true, 0);
         if ((rc = run_tiles(c, gb, image, MM_DTYPE_U16, flat, (const float2 *)W, (const float2 *)zop, blur_radius,
-                            nullptr, nullptr, buffer, (long long)X * Y, Y, st)))
+                            nullptr, nullptr, buffer, (long long)X * Y, Y, st, fold)))
             return rc;
     }
     {
@@ -646,6 +679,16 @@ int mm_dapi_spots_async(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, i
 }
 
 }  // extern "C"
+
+extern "C" int mm_ctx_set_option(mm_ctx *c, int option, int value) {
+    MM_REQUIRE(c, "null context");
+    MM_REQUIRE(option == MM_OPT_BLUR_MODE, "unknown option %d", option);
+    MM_REQUIRE(value == MM_BLUR_AUTO || value == MM_BLUR_EXACT || value == MM_BLUR_SPECTRAL,
+               "unknown blur mode %d", value);
+    std::lock_guard<std::mutex> lock(c->mu);
+    c->blur_mode = value;
+    return MM_OK;
+}
 
 extern "C" int mm_tile_geometry(int Z, int X, int Y, int tile_size, int zpad, int overlap, int npsf, int tile,
                                 int32_t *desc, int32_t *map_z, int32_t *map_x, int32_t *map_y) {

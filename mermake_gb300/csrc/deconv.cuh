@@ -134,11 +134,16 @@ int mm_launch_zpass(const TileGeom &g, float2 *S, const float2 *W, long long wst
 #define MM_ZOP_MAX_COPIES 4
 int mm_zop_supported(int Z, int zpad);
 int mm_zker_build_impl(const float2 *W, int Zp, long long plane, float2 *w, cudaStream_t st);
+// fresp: NULL, or a per-frequency factor (plane entries) applied to the
+// result, the blur subtraction folded into the z step (mm_blur_response_get)
 int mm_launch_zop_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, long long plane, int nt,
-                        cudaStream_t st);
+                        const float *fresp, cudaStream_t st);
 int mm_zconv_supported(int Z, int zpad);
 int mm_launch_zconv(float2 *S, const float2 *w, long long wstride, int Z, int zpad, int Zp, long long plane, int t0,
-                    int nt, int npsf, cudaStream_t st);
+                    int nt, int npsf, const float *fresp, cudaStream_t st);
+// 1 - D(kx) D(ky) per half-spectrum frequency of a P x P plane, D the
+// frequency response of the box mean of width 2 delta + 1 (zop.cu)
+int mm_blur_response_get(int P, int delta, const float **out);
 int mm_launch_zfwd(float2 *S, int Zp, int plane, cudaStream_t st);
 int mm_launch_rows_inv(const float2 *S, int nrows, int P, int H, float *out, float *blur, int delta,
                        cudaStream_t st);

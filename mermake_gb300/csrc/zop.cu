@@ -18,6 +18,13 @@
 // uses the same M_p, so the z pass of nt tiles is, per p, a (Z x Z) by
 // (Z x nt) complex product: regular FP32 FMA work with register blocking, in
 // place of two transforms over the padded depth.
+#include <math.h>
+
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
 #include "deconv.cuh"
 
 namespace {
@@ -116,7 +123,7 @@ __device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {
 template <bool V16, int ZC>
 __global__ void __launch_bounds__(kApplyMaxThreads, 2)
 k_zop_apply(float2 *__restrict__ S, const float2 *__restrict__ w, int Z, int Zp, long long plane, int nt, int ign,
-            int tgn, const ZopTab tab) {
+            int tgn, const ZopTab tab, const float *__restrict__ fresp) {
     extern __shared__ __align__(16) float2 sm[];
     if constexpr (ZC > 0) {
         Z = ZC;
@@ -260,6 +267,8 @@ k_zop_apply(float2 *__restrict__ S, const float2 *__restrict__ w, int Z, int Zp,
             }
         }
         if (p0 + p < plane) {
+            // the blur subtraction as a factor of this frequency (1 when not folded)
+            const float f = fresp ? fresp[p0 + p] : 1.f;
 #pragma unroll
             for (int a = 0; a < kTI; ++a) {
                 const int i = ig * kTI + a;
@@ -267,7 +276,7 @@ k_zop_apply(float2 *__restrict__ S, const float2 *__restrict__ w, int Z, int Zp,
 #pragma unroll
                 for (int b = 0; b < kTT; ++b) {
                     const int t = tc0 + tg * kTT + b;
-                    if (t < nt) S[((long long)t * Z + i) * plane + p0 + p] = acc[a][b];
+                    if (t < nt) S[((long long)t * Z + i) * plane + p0 + p] = cscale(acc[a][b], f);
                 }
             }
         }
@@ -303,7 +312,7 @@ __device__ __host__ __forceinline__ int zconv_wx_rows(int Z, int Zp) {
 
 __global__ void __launch_bounds__(kConvMaxThreads)
 k_zconv(float2 *__restrict__ S, const float2 *__restrict__ w, long long wstride, int Z, int zpad, int Zp,
-        long long plane, int t0, int npsf) {
+        long long plane, int t0, int npsf, const float *__restrict__ fresp) {
     extern __shared__ __align__(16) float2 sm[];
     const int Lw = zconv_wx_rows(Z, Zp);
     const int Tpad = zconv_tpad(Zp);
@@ -361,9 +370,10 @@ k_zconv(float2 *__restrict__ S, const float2 *__restrict__ w, long long wstride,
             for (int a = 0; a < kCI; ++a) acc[a] = cfma(wr[kCI - 1 - s + a], x[s], acc[a]);
     }
     if (pv) {
+        const float f = fresp ? fresp[p] : 1.f;
 #pragma unroll
         for (int a = 0; a < kCI; ++a)
-            if (i0 + a < Z) Sp[(long long)(i0 + a) * plane + p] = acc[a];
+            if (i0 + a < Z) Sp[(long long)(i0 + a) * plane + p] = cscale(acc[a], f);
     }
 }
 
@@ -380,7 +390,7 @@ int mm_zconv_supported(int Z, int zpad) {
 }
 
 int mm_launch_zconv(float2 *S, const float2 *w, long long wstride, int Z, int zpad, int Zp, long long plane, int t0,
-                    int nt, int npsf, cudaStream_t st) {
+                    int nt, int npsf, const float *fresp, cudaStream_t st) {
     MM_REQUIRE(Zp == Z + 2 * zpad && mm_zconv_supported(Z, zpad),
                "z convolution needs Z <= %d and Zp <= %d (Z %d, zpad %d)", kConvMaxThreads / 32 * kCI, MM_ZOP_MAX_ZP,
                Z, zpad);
@@ -389,7 +399,7 @@ int mm_launch_zconv(float2 *S, const float2 *w, long long wstride, int Z, int zp
     if (int rc = mm_set_smem((const void *)k_zconv, sm)) return rc;
     const int threads = (Z + kCI - 1) / kCI * 32;
     dim3 grid((unsigned)((plane + kCq - 1) / kCq), (unsigned)nt);
-    k_zconv<<<grid, threads, sm, st>>>(S, w, wstride, Z, zpad, Zp, plane, t0, npsf);
+    k_zconv<<<grid, threads, sm, st>>>(S, w, wstride, Z, zpad, Zp, plane, t0, npsf, fresp);
     MM_CHECK_LAUNCH();
     return MM_OK;
 }
@@ -415,7 +425,7 @@ int mm_zop_supported(int Z, int zpad) {
 }
 
 int mm_launch_zop_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, long long plane, int nt,
-                        cudaStream_t st) {
+                        const float *fresp, cudaStream_t st) {
     MM_REQUIRE(Zp == Z + 2 * zpad && mm_zop_supported(Z, zpad),
                "z operator needs Z <= %d, Zp <= %d and at most %d copies of a plane (Z %d, zpad %d)", MM_ZOP_MAX_Z,
                MM_ZOP_MAX_ZP, MM_ZOP_MAX_COPIES, Z, zpad);
@@ -439,8 +449,51 @@ int mm_launch_zop_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, lon
                              : ((plane % 2 == 0) ? (const void *)k_zop_apply<true, 0> : (const void *)k_zop_apply<false, 0>);
     if (int rc = mm_set_smem(fn, sm)) return rc;
     dim3 grid((unsigned)((plane + kPB - 1) / kPB));
-    void *args[] = {&S, &w, &Z, &Zp, &plane, &nt, &ign, &tgn, &tab};
+    void *args[] = {&S, &w, &Z, &Zp, &plane, &nt, &ign, &tgn, &tab, &fresp};
     MM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(threads), args, sm, st));
     mm_launch_counter_add();
+    return MM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The blur subtraction of tile_wise (deconvolver.py:160-163: res minus its box
+// mean along x, then y, window 2 d + 1, blur.cu:1-52) as a frequency response.
+// At a voxel at least d from every edge of the P x P plane the truncated box
+// mean is the circular one, so there res - box_x(box_y(res)) is the inverse
+// transform of the spectrum times
+//   f(kx, ky) = 1 - D(kx) D(ky),   D(k) = (1 / (2d + 1)) sum_{e=-d..d} cos(2 pi k e / P)
+// over the half spectrum (kx < P, ky < P/2 + 1).  The table (float, P x H) is
+// computed in double on the host and cached per (device, P, d); the first
+// request uploads it synchronously.
+// ---------------------------------------------------------------------------
+int mm_blur_response_get(int P, int delta, const float **out) {
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int>, float *> cache;
+    MM_REQUIRE(P >= 1 && delta >= 0 && 2 * delta + 1 <= P, "blur window %d too wide for a plane of %d", 2 * delta + 1,
+               P);
+    int dev = 0;
+    MM_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    auto key = std::make_tuple(dev, P, delta);
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+        *out = it->second;
+        return MM_OK;
+    }
+    const int H = P / 2 + 1;
+    std::vector<double> D(P);
+    for (int k = 0; k < P; ++k) {
+        double acc = 0.0;
+        for (int e = -delta; e <= delta; ++e) acc += cos(2.0 * M_PI * (double)(((long long)k * e) % P) / (double)P);
+        D[k] = acc / (double)(2 * delta + 1);
+    }
+    std::vector<float> f((size_t)P * H);
+    for (int kx = 0; kx < P; ++kx)
+        for (int ky = 0; ky < H; ++ky) f[(size_t)kx * H + ky] = (float)(1.0 - D[kx] * D[ky]);
+    float *d = nullptr;
+    MM_CUDA_TRY(cudaMalloc(&d, sizeof(float) * f.size()));
+    MM_CUDA_TRY(cudaMemcpy(d, f.data(), sizeof(float) * f.size(), cudaMemcpyHostToDevice));
+    cache[key] = d;
+    *out = d;
     return MM_OK;
 }

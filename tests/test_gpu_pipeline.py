@@ -17,7 +17,8 @@ def mm():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     from mermake_gb300 import deconvolver, maxima, pipeline, synth
-    return dict(dc=deconvolver, mx=maxima, pl=pipeline, synth=synth)
+    from mermake_gb300 import _lib
+    return dict(dc=deconvolver, mx=maxima, pl=pipeline, synth=synth, lib=_lib)
 
 
 HYB = dict(tile_size=60, overlap=12, beta=1e-4, threshold=3600, blur_radius=10, delta=1, delta_fit=3,
@@ -49,17 +50,52 @@ def plain_loop(mm, dec, img, flat, a):
 
 @pytest.mark.parametrize("X,Y", [(170, 150), (130, 130)])
 def test_hyb_batched_equals_plain_loop(mm, X, Y):
-    """Also at X = Y = 130, where the second tile has xd = 82 > P - overlap, so
-    xd + overlap is clipped to the padded size P = 84 in the yielded view."""
+    """With the truncated box blur on both sides (MM_BLUR_EXACT) the batched
+    driver gives the rows of the plain loop exactly.  Also at X = Y = 130,
+    where the second tile has xd = 82 > P - overlap, so xd + overlap is
+    clipped to the padded size P = 84 in the yielded view."""
     img, flat, psf = hyb_case(mm, X=X, Y=Y)
     Z = img.shape[0]
     dec = mm["dc"].Deconvolver(psf, img.shape, zpad=Z - 1, **HYB)
     dimg, dflat = img.cuda(), torch.from_numpy(flat).cuda()
     want = ck.sort_rows(plain_loop(mm, dec, dimg, dflat, HYB).cpu().numpy())
-    for batch in (1, 4, 0):
-        got = ck.sort_rows(mm["pl"].hyb_spots(dec, dimg, dflat, batch=batch, **HYB).cpu().numpy())
-        assert len(want) > 20
-        np.testing.assert_array_equal(got, want)
+    with mm["lib"].blur_mode(mm["lib"].MM_BLUR_EXACT):
+        for batch in (1, 4, 0):
+            got = ck.sort_rows(mm["pl"].hyb_spots(dec, dimg, dflat, batch=batch, **HYB).cpu().numpy())
+            assert len(want) > 20
+            np.testing.assert_array_equal(got, want)
+
+
+def test_folded_blur_volumes_and_rows(mm):
+    """The drivers' default: the blur subtraction folded into the z step
+    (1 - D(kx) D(ky) per frequency).  Its volumes (mm_deconv_tiles under
+    MM_BLUR_SPECTRAL) equal the truncated blur's at every voxel at least the
+    box half-width from a tile edge, within float32 rounding, and the
+    driver's rows are the oracle's maxima + fit on those volumes."""
+    from tests.test_gpu_configs import assert_kept_rows_match, oracle_rows_on_gpu_tiles
+    img, flat, psf = hyb_case(mm, seed=4)
+    Z = img.shape[0]
+    dec = mm["dc"].Deconvolver(psf, img.shape, zpad=Z - 1, **HYB)
+    dimg, dflat = img.cuda(), torch.from_numpy(flat).cuda()
+    nt, P = dec.n_tiles(img.shape), dec.P
+    vols = {}
+    for mode in (mm["lib"].MM_BLUR_EXACT, mm["lib"].MM_BLUR_SPECTRAL):
+        res = torch.empty((nt, Z, P, P), device="cuda")
+        raw = torch.empty_like(res)
+        with mm["lib"].blur_mode(mode):
+            dec._call(dimg, mm["dc"].MM_DTYPE_U16, dflat, 0, nt, HYB["blur_radius"], res_out=res, raw_out=raw)
+        vols[mode] = res.cpu().numpy(), raw.cpu().numpy()
+    ex, sp = vols[mm["lib"].MM_BLUR_EXACT][0], vols[mm["lib"].MM_BLUR_SPECTRAL][0]
+    d = HYB["blur_radius"] // 2
+    inner = (slice(None), slice(None), slice(d, P - d), slice(d, P - d))
+    err = np.abs(sp[inner] - ex[inner]).max() / np.abs(ex[inner]).max()
+    print("folded vs truncated blur, voxels >= %d from the edges: %.3g of max" % (d, err))
+    assert err < 1e-5
+    rows = mm["pl"].hyb_spots(dec, dimg, dflat, **HYB).cpu().numpy()
+    sure, edge = oracle_rows_on_gpu_tiles(dec, dec.tile_boxes(img.shape), sp, vols[mm["lib"].MM_BLUR_SPECTRAL][1],
+                                          HYB)
+    assert len(sure) > 20
+    assert_kept_rows_match(rows, sure, edge)
 
 
 def test_hyb_spots_match_oracle_on_same_volumes(mm):
@@ -106,15 +142,22 @@ DAPI = dict(tile_size=60, overlap=12, beta=0.01, threshold=3.0, blur_radius=20, 
 
 
 def test_dapi_batched_equals_stepwise(mm):
-    """__main__.py:215-225: apply -> RMS -> maxima(+) -> negate -> maxima(-)."""
+    """__main__.py:215-225: apply -> RMS -> maxima(+) -> negate -> maxima(-),
+    bit-identical with the truncated blur on both sides."""
     Z, X, Y = 10, 130, 140
     img = mm["synth"].dapi_stack(Z, X, Y, 5, n_nuclei=12, radii=(3.0, 12.0, 12.0))
     psf = mm["synth"].gaussian_psf((9, 9, 9), 2.0, 1.3)
     dec = mm["dc"].Deconvolver(psf, img.shape, zpad=(Z - 1) // 2, **DAPI)
     dimg = img.cuda()
-    plus, minus, buf, rms = mm["pl"].dapi_spots(dec, dimg, None, **DAPI)
+    folded = mm["pl"].dapi_spots(dec, dimg, None, **DAPI)[2].cpu().numpy()
+    with mm["lib"].blur_mode(mm["lib"].MM_BLUR_EXACT):
+        plus, minus, buf, rms = mm["pl"].dapi_spots(dec, dimg, None, **DAPI)
     ref_buf = dec.apply(dimg, None, **DAPI)
     np.testing.assert_array_equal(buf.cpu().numpy(), ref_buf.cpu().numpy())
+    # the default folds the blur into the z step: the stitched centres lie at
+    # least the overlap inside their tiles, where the two blurs agree
+    r = ref_buf.cpu().numpy()
+    assert np.abs(folded - r).max() <= 1e-5 * np.abs(r).max()
     v = ref_buf.double()
     rms_ref = np.float32(np.float32(np.sqrt(float((v * v).sum()))) / np.sqrt(v.numel()))
     assert abs(rms - rms_ref) <= 2e-7 * rms_ref
