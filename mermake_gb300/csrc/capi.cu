@@ -209,9 +209,14 @@ bool fold_allowed(const mm_ctx *c, const TileGeom &g, int blur_radius, const flo
 // tile_wise core for tiles [g.t0, g.t0 + g.nt); fold: the blur subtraction
 // runs as a factor of the z step's output (fold_allowed) instead of the y and
 // x box means of the result
+//
+// win: with the blur folded, the caller reads only a window of each tile (a
+// driver's keep band, win >= 0 its reach, or the stitched centre, win == -1):
+// the inverse y pass then transforms and writes only the rows and columns of
+// that window (k_rows_inv_win).  win < -1: whole tiles.
 int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *flat, const float2 *W,
               const float2 *zop, int blur_radius, float *res_out, float *raw_out, float *stitch, long long osz,
-              long long osx, cudaStream_t st, bool fold = false) {
+              long long osx, cudaStream_t st, bool fold = false, int win = -2) {
     const long long plane_c = (long long)g.P * g.H;
     const long long tile_c = (long long)g.Z * plane_c;
     const long long tile_r = (long long)g.Z * g.P * g.P;
@@ -261,7 +266,10 @@ int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *
         StageTimer t(c, ST_COLS_INV, 2 * spec_b, st);
         if ((rc = mm_launch_cols(S, g.P, g.H, g.H, plane_c, g.nt * g.Z, true, st))) return rc;
     }
-    {
+    if (fresp && win >= -1 && !res_out) {
+        StageTimer t(c, ST_ROWS_INV, spec_b + real_b, st);
+        if ((rc = mm_launch_rows_inv_win(S, g, win, (float *)res, st))) return rc;
+    } else {
         StageTimer t(c, ST_ROWS_INV, spec_b + real_b * (rdelta >= 0 ? 2 : 1), st);
         if ((rc = mm_launch_rows_inv(S, g.nt * g.Z * g.P, g.P, g.H, (float *)res, (float *)tmp, rdelta, st)))
             return rc;
@@ -446,8 +454,11 @@ static int hyb_pass(mm_ctx *c, const TileGeom &g, int batch, const uint16_t *ima
         gb.nt = (t0 + batch <= nt) ? batch : nt - t0;
         const int reach = delta_fit + (delta > delta_fit ? delta : delta_fit);
         const bool fold = fold_allowed(c, gb, blur_radius, (const float2 *)zop, true, reach);
+        // the maxima scan covers the keep band (delta_fit + 1 past the kept
+        // region, maxima.cu scan_range) and reads max(delta, delta_fit) around it
+        const int win = delta_fit + 1 + (delta > delta_fit ? delta : delta_fit);
         if ((rc = run_tiles(c, gb, image, MM_DTYPE_U16, flat, (const float2 *)W, (const float2 *)zop, blur_radius,
-                            nullptr, nullptr, nullptr, 0, 0, st, fold)))
+                            nullptr, nullptr, nullptr, 0, 0, st, fold, win)))
             return rc;
         MaximaArgs a = {};
         a.img = (const float *)c->ws[WS_RES];
@@ -573,7 +584,7 @@ static int dapi_pass(mm_ctx *c, const TileGeom &g, int batch, const uint16_t *im
         gb.nt = (t0 + batch <= nt) ? batch : nt - t0;
         const bool fold = fold_allowed(c, gb, blur_radius, (const float2 *)zop, true, 0);
         if ((rc = run_tiles(c, gb, image, MM_DTYPE_U16, flat, (const float2 *)W, (const float2 *)zop, blur_radius,
-                            nullptr, nullptr, buffer, (long long)X * Y, Y, st, fold)))
+                            nullptr, nullptr, buffer, (long long)X * Y, Y, st, fold, -1)))
             return rc;
     }
     {

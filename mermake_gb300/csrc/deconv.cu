@@ -52,6 +52,25 @@ __device__ __forceinline__ void rows_fwd_group(const TileGeom &g, const T *__res
     const long long nrows = (long long)g.Z * g.P;
     const long long row0 = (long long)bx * 2 * nl;  // in (x, z) order
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    {
+        // a group whose padded rows are all zero (x beyond the reflected data
+        // of a thin tile, deconvolver.py:135-137) transforms to zero: write it
+        const long long rl = min(row0 + 2 * nl, nrows) - 1;
+        bool zero = true;
+        for (int xp = (int)(row0 / g.Z); xp <= (int)(rl / g.Z); ++xp) zero &= mm_map_xy(xp, d.x == 0, d.xd, g.P, g.ov) < 0;
+        if (zero) {
+            const int H = NF > 0 ? NF / 2 + 1 : g.H;
+            float2 *Sb = S + (long long)by * nrows * H;
+            const int nr = (int)(rl - row0 + 1);
+            for (int it = threadIdx.x; it < nr * H; it += blockDim.x) {
+                const int q = it / H, k = it - q * H;
+                const long long r = row0 + q;
+                const int xp = (int)(r / g.Z);
+                Sb[((r - (long long)xp * g.Z) * g.P + xp) * H + k] = make_float2(0.f, 0.f);
+            }
+            return;
+        }
+    }
     float *Af = reinterpret_cast<float *>(L.A);
     // the y map of the tile (same for every row), after the scratch
     int *ymap = reinterpret_cast<int *>(L.scr + fft_scr_f4(P, nl, nw));
@@ -237,13 +256,15 @@ k_rows_fwd_f32(const float *__restrict__ vol, long long nrows, float2 *__restric
 template <int LMAX, int NF, int NLF>
 __device__ __forceinline__ void rows_inv_group(const float2 *__restrict__ S, long long nrows, int H,
                                                float *__restrict__ out, float *__restrict__ blur, int delta,
-                                               const FftPlan &P, int nl, const FftSmem &L, int bx) {
+                                               const FftPlan &P, int nl, const FftSmem &L, long long row0,
+                                               int ylo = 0, int yhi = 1 << 30) {
+    // rows [row0, nrows) of the group exist (nrows: the end of the group's
+    // window, or of the batch); only columns [ylo, yhi) are stored
     if constexpr (NF > 0) {
         nl = NLF;
         H = NF / 2 + 1;
     }
     const int n = NF > 0 ? NF : P.n;
-    const long long row0 = (long long)bx * 2 * nl;
     const bool even = (n % 2) == 0;
     const float invH = 1.0f / (float)H, invn = 1.0f / (float)n;
     constexpr int U = 4;
@@ -279,7 +300,7 @@ __device__ __forceinline__ void rows_inv_group(const float2 *__restrict__ S, lon
     for (int it = threadIdx.x; it < 2 * nl * n; it += blockDim.x) {
         const int q = fdiv_i(it, n, invn), e = it - q * n;
         const long long row = row0 + q;
-        if (row < nrows) out[row * n + e] = Rf[2 * sidx(e, q >> 1, nl) + (q & 1)];
+        if (row < nrows && e >= ylo && e < yhi) out[row * n + e] = Rf[2 * sidx(e, q >> 1, nl) + (q & 1)];
     }
     if (delta < 0) return;
     // y blur: the free ping-pong buffer holds 2 nl rows of n floats
@@ -329,7 +350,71 @@ k_rows_inv(const float2 *__restrict__ S, long long nrows, int H, float *__restri
     const FftSmem L = fft_smem_layout(smem_raw, P, nl);
     fft_load_tables(P, L.tw, L.tab);
     for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
-        rows_inv_group<LMAX, NF, NLF>(S, nrows, H, out, blur, delta, P, nl, L, grp);
+        rows_inv_group<LMAX, NF, NLF>(S, nrows, H, out, blur, delta, P, nl, L, (long long)grp * 2 * nl);
+        __syncthreads();
+    }
+}
+
+// The rows and columns of tile t (of the batch) that the caller reads: the
+// window [lo, hi) of padded indices along x and y, from the tile's yielded
+// extent.  reach >= 0: the hyb keep band, [ov - reach, extent - ov + reach);
+// reach < 0: the stitched centre, [ov, extent - ov).
+__device__ __forceinline__ void read_window(const TileGeom &g, int t, int reach, int &xlo, int &xhi, int &ylo,
+                                            int &yhi) {
+    const TileDesc d = mm_tile_desc(g, g.t0 + t);
+    const int r = reach < 0 ? 0 : reach;
+    xlo = max(0, g.ov - r);
+    ylo = max(0, g.ov - r);
+    xhi = min(d.xend, d.xend - g.ov + r);
+    yhi = min(d.yend, d.yend - g.ov + r);
+    if (xhi < xlo) xhi = xlo;
+    if (yhi < ylo) yhi = ylo;
+}
+
+// The inverse y pass over the read windows only: per tile, the rows x in
+// [xlo, xhi) of every plane, in groups of 2 nl rows (a plane's last group is
+// cut at xhi), stores limited to the columns [ylo, yhi).  Rows and columns
+// outside are not written.  The CTAs first tabulate the groups per tile
+// (tiles <= kMaxWinTiles), then walk the groups as k_rows_inv does.
+constexpr int kMaxWinTiles = 256;
+template <int LMAX, int NF = 0, int NLF = 0>
+__global__ void __launch_bounds__(kRowsInvCfg.threads, kRowsInvCfg.ctas)
+k_rows_inv_win(const float2 *__restrict__ S, TileGeom g, int reach, float *__restrict__ out, FftPlan P, int nl,
+               int cum_off) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    int *cum = reinterpret_cast<int *>(smem_raw + cum_off);  // groups before tile t (nt + 1 entries)
+    const FftSmem L = fft_smem_layout(smem_raw, P, nl);
+    fft_load_tables(P, L.tw, L.tab);
+    if constexpr (NF > 0) nl = NLF;
+    const int gr = 2 * nl;
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int t = 0; t < g.nt; ++t) {
+            cum[t] = acc;
+            int xlo, xhi, ylo, yhi;
+            read_window(g, t, reach, xlo, xhi, ylo, yhi);
+            acc += g.Z * ((xhi - xlo + 1 + gr - 1) / gr);
+        }
+        cum[g.nt] = acc;
+    }
+    __syncthreads();
+    const int ngroups = cum[g.nt];
+    const long long plane = (long long)g.P;
+    for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+        int t = 0;
+        while (cum[t + 1] <= grp) ++t;
+        int xlo, xhi, ylo, yhi;
+        read_window(g, t, reach, xlo, xhi, ylo, yhi);
+        const int per_plane = (xhi - xlo + 1 + gr - 1) / gr;
+        const int k = grp - cum[t];
+        const int z = k / per_plane, c = k - z * per_plane;
+        const long long base = ((long long)t * g.Z + z) * plane;
+        // pairs of rows share a transform line, and a row's rounding depends
+        // on its partner: start on an even row of the batch, so that the pairs
+        // are those of the whole-tile pass (rows 2l and 2l + 1); the row
+        // before the window that this may add is computed exactly as there
+        const long long row0 = ((base + xlo) & ~1LL) + (long long)c * gr;
+        rows_inv_group<LMAX, NF, NLF>(S, base + xhi, g.H, out, nullptr, -1, P, nl, L, row0, ylo, yhi);
         __syncthreads();
     }
 }
@@ -510,6 +595,27 @@ int mm_launch_rows_inv(const float2 *S, int nrows, int Pn, int H, float *out, fl
     void *args[] = {&S, &nr, &H, &out, &blur, &delta, &P, &nl, &ngroups};
     return launch_fft_kernel(MM_FFT_KERNEL(P, nl, 8, k_rows_inv, ), dim3(fft_grid(ngroups, kRowsInvCfg)), sm, st, args,
                              kRowsInvCfg.threads);
+}
+
+int mm_launch_rows_inv_win(const float2 *S, const TileGeom &g, int reach, float *out, cudaStream_t st) {
+    FftPlan P;
+    int rc = mm_fft_plan_get(g.P, &P);
+    if (rc) return rc;
+    MM_REQUIRE(g.nt <= kMaxWinTiles, "windowed inverse pass takes at most %d tiles per batch", kMaxWinTiles);
+    const size_t lim = (size_t)fft_smem_limit(kRowsInvCfg);
+    const size_t cumb = sizeof(int) * ((size_t)g.nt + 1);
+    auto bytes = [&](int l) { return ((fft_smem(P, l, kRowsInvCfg) + 15) & ~(size_t)15) + cumb; };
+    int nl = 16;
+    while (nl > 1 && bytes(nl) > lim) nl >>= 1;
+    MM_REQUIRE(bytes(nl) <= lim, "windowed inverse pass does not fit shared memory");
+    const size_t sm = bytes(nl);
+    int cum_off = (int)(sm - cumb);
+    // an upper bound of the groups (the kernel counts the exact number)
+    const long long ngroups = (long long)g.nt * g.Z * mm_cdiv(g.P, 2 * nl);
+    TileGeom ga = g;
+    void *args[] = {&S, &ga, &reach, &out, &P, &nl, &cum_off};
+    return launch_fft_kernel(MM_FFT_KERNEL(P, nl, 8, k_rows_inv_win, ), dim3(fft_grid(ngroups, kRowsInvCfg)), sm, st,
+                             args, kRowsInvCfg.threads);
 }
 
 int mm_launch_blur_x_sub(const TileGeom &g, const float *res, const float *tmp, int delta, float *res_out,

@@ -147,6 +147,10 @@ int mm_blur_response_get(int P, int delta, const float **out);
 int mm_launch_zfwd(float2 *S, int Zp, int plane, cudaStream_t st);
 int mm_launch_rows_inv(const float2 *S, int nrows, int P, int H, float *out, float *blur, int delta,
                        cudaStream_t st);
+// the inverse y pass (no blur) over the rows and columns of each tile that the
+// caller reads: reach >= 0, the band [ov - reach, extent - ov + reach) of the
+// hyb keep filter; reach < 0, the stitched centre [ov, extent - ov)
+int mm_launch_rows_inv_win(const float2 *S, const TileGeom &g, int reach, float *out, cudaStream_t st);
 int mm_launch_blur_x_sub(const TileGeom &g, const float *res, const float *tmp, int delta,
                          float *res_out, float *stitch, long long osz, long long osx, cudaStream_t st);
 int mm_launch_make_raw(const TileGeom &g, const void *img, int dtype, const float *flat, float *raw,

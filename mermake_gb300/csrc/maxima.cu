@@ -96,7 +96,29 @@ struct Vols {
     long long rsz, rsx, rvol;
     const void *chan;
     const float *flat;
+    int band;                  // >= 0 (keep mode): only maxima within `band` of the kept region are sought
 };
+
+// The voxels of volume (tile) vi whose maxima are sought: the whole view, or
+// in keep mode (mermake/__main__.py:254-256: ov <= xc, yc < extent - ov on the
+// fitted centroid) the band the kept rows can come from.  A centroid is a
+// weighted mean of the maximum's position plus offsets |d| <= delta_fit with
+// non-negative weights (v - min v), or the position itself, so a maximum
+// farther than delta_fit outside the kept region cannot be kept; `band`
+// (delta_fit + 1) leaves a pixel for the rounding of the centroid.  The
+// maxima tests and fits still read the whole view.
+__device__ __forceinline__ void scan_range(const Vols &V, int X, int Y, int &xlo, int &xhi, int &ylo, int &yhi) {
+    xlo = 0; xhi = X; ylo = 0; yhi = Y;
+    if (V.band >= 0) {
+        const int ov = V.g.ov;
+        xlo = max(0, ov - V.band);
+        ylo = max(0, ov - V.band);
+        xhi = min(X, X - ov + V.band);
+        yhi = min(Y, Y - ov + V.band);
+        if (xhi < xlo) xhi = xlo;
+        if (yhi < ylo) yhi = ylo;
+    }
+}
 
 __device__ __forceinline__ void vol_dims(const Vols &V, int vi, int &X, int &Y, TileDesc &d) {
     if (V.tiles) {
@@ -227,7 +249,10 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
     TileDesc d;
     vol_dims(V, vi, X, Y, d);
     const int Z = V.Z;
-    const int rows = Z * X;
+    int xlo, xhi, ylo, yhi;
+    scan_range(V, X, Y, xlo, xhi, ylo, yhi);
+    const int nx = xhi - xlo;
+    const int rows = Z * nx;
     const float *img = V.img + vi * V.ivol;
     const int nn = g_sphere_n[delta];
     const char4 *sph = g_sphere[delta];
@@ -239,15 +264,15 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
 
     int qn = 0;
     for (int row = blockIdx.x * wpb + warp; row < rows; row += gridDim.x * wpb) {
-        const int z = row / X, x = row - z * X;
+        const int z = row / nx, x = xlo + (row - z * nx);
         const unsigned key = (unsigned)z | ((unsigned)x << 16);
         const float *rp = img + z * V.isz + x * V.isx;
-        for (int y0 = 0; y0 < Y; y0 += 32 * kMaxY) {
+        for (int y0 = ylo; y0 < yhi; y0 += 32 * kMaxY) {
             float vals[kMaxY];
 #pragma unroll
             for (int k = 0; k < kMaxY; ++k) {
                 const int y = y0 + 32 * k + (int)lane;
-                vals[k] = y < Y ? rp[y] : 0.f;
+                vals[k] = y < yhi ? rp[y] : 0.f;
             }
             // queue the voxels above the threshold (maxima.cu:19; a NaN
             // threshold admits every voxel)
@@ -257,7 +282,7 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
                 const float v = xf(vals[k], t);
                 for (int sgn = 0; sgn < (both ? 2 : 1); ++sgn) {
                     const float sv = sgn ? -v : v;
-                    const bool up = y < Y && !(sv <= th);
+                    const bool up = y < yhi && !(sv <= th);
                     const unsigned m = __ballot_sync(0xffffffffu, up);
                     if (up) {
                         const int at = qn + __popc(m & ((1u << lane) - 1));
@@ -529,6 +554,7 @@ static Vols make_vols(const MaximaArgs &a) {
     if (a.tiles) V.g = *a.tiles;
     V.raw_kind = a.raw_kind; V.raw = a.raw; V.rsz = a.rsz; V.rsx = a.rsx; V.rvol = a.rvol;
     V.chan = a.chan; V.flat = a.flat;
+    V.band = (a.tiles && a.keep_filter) ? a.delta_fit + 1 : -1;
     return V;
 }
 
