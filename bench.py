@@ -31,6 +31,10 @@ A step is one FOV of the workload, inputs resident in HBM:
   i mod 20, round = i div 20, later rounds drift-aligned against round 0)
   through ``serve.FovServer`` (continuous batching under a 120 GB budget);
   reports stream voxels/s and p50/p99 request latency.
+* ``loader``: one 3-colour + DAPI FOV written in the acquisition's layout (bz2
+  zarr of uint8 square-root frames, the xml's channel count) and read
+  ``--steps`` times by ``io.FovPrefetcher`` (chunks decoded by a pool of host
+  threads into pinned memory); reports FOV/s and decode GB/s on the host cores.
 * ``drift16``: 16 DAPI rounds of one 50 x 2048 x 2048 field drifted by known
   shifts (+-3 z, +-20 x/y, sub-pixel), each deconvolved, spot-called and
   aligned against round 0's resident maxima; reports rounds/s and the error
@@ -112,8 +116,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="mermake_gb300", choices=["mermake_gb300", "reference"])
-    ap.add_argument("--workload", default="fov3c", choices=sorted(WORKLOADS) + ["served", "drift16"])
-    ap.add_argument("--fovs", type=int, default=40,
+    ap.add_argument("--workload", default="fov3c", choices=sorted(WORKLOADS) + ["served", "drift16", "loader"])
+    ap.add_argument("--fovs", type=int, default=200,
                     help="served: requests in the stream (FOV id = i mod 20, round = i div 20)")
     ap.add_argument("--interval", type=float, default=1.5, help="served: mean Poisson arrival interval (s)")
     ap.add_argument("--workers", type=int, default=2, help="served: concurrent requests on the device")
@@ -433,15 +437,19 @@ def gpu_arm(args, rank, world, local):
         "clocks": clk.summary(),
     }
     if dom == "zpass" and args.form == "batched":
-        # the z pass is FP32-FMA bound: its arithmetic against the nominal FP32
-        # peak (SMs x 128 lanes x 2 flops x the sampled maximum SM clock)
+        # the z pass is bound by FP32 FMA issue, not by bytes: the line's bound
+        # is its arithmetic against the nominal FP32 peak (SMs x 128 lanes x 2
+        # flops x the sampled maximum SM clock; the measured peaks file has no
+        # FP32 figure), with the HBM figures beside it
         props = torch.cuda.get_device_properties(dev)
-        mhz = line["clocks"].get("sm_max_mhz") or peaks.get("sm_max_mhz") or 2070.0
+        mhz = (line["clocks"] or {}).get("sm_max_mhz") or peaks.get("sm_max_mhz") or 2070.0
         fpeak = props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
         fl = zpass_flops(w, s) * args.steps / dl
-        line["roofline"]["fp32"] = {"achieved": fl / ((dms / dl) / 1e3) / 1e12, "peak_nominal": fpeak,
-                                    "unit": "TFLOP/s", "frac": fl / ((dms / dl) / 1e3) / 1e12 / fpeak,
-                                    "flops_per_launch": fl}
+        fach = fl / ((dms / dl) / 1e3) / 1e12
+        rf = line["roofline"]
+        hbm = {k: rf[k] for k in ("achieved", "peak", "unit", "frac", "peak_source")}
+        rf.update(bound="fp32", achieved=fach, peak=fpeak, unit="TFLOP/s", frac=fach / fpeak,
+                  peak_source="nominal (SMs x 128 FP32 lanes x 2 x max SM clock)", flops_per_launch=fl, hbm=hbm)
 
     if not args.no_e2e:
         import torch
@@ -858,6 +866,7 @@ def served_arm(args, local):
             res = [fu.result() for fu in futs]
             t1 = max(x.done for x in res)
             peak = srv.max_in_flight
+            peak_bytes, releases = srv.peak_bytes, srv.releases
     lat = sorted(1e3 * x.latency for x in res)
     svc = sorted(1e3 * (x.done - x.admitted) for x in res)
     que = sorted(1e3 * (x.admitted - x.request.arrival) for x in res)
@@ -876,7 +885,8 @@ def served_arm(args, local):
         "data": "synthetic (seeded Poisson background + Gaussian puncta / nuclei), %d FOV shapes" % nf,
         "config": {"workload": "served", "fovs": [list(f) for f in fovs], "requests": len(reqs),
                    "mean_interval_s": args.interval, "workers": args.workers, "hbm_budget_gb": 120,
-                   "peak_in_flight": peak, "tile_size": hyb["tile_size"], "overlap": hyb["overlap"]},
+                   "peak_in_flight": peak, "peak_device_gb_held": peak_bytes / 1e9,
+                   "idle_worker_releases": releases, "tile_size": hyb["tile_size"], "overlap": hyb["overlap"]},
         "latency_ms": {"p50": pct(lat, 50), "p99": pct(lat, 99), "max": lat[-1]},
         "service_ms": {"p50": pct(svc, 50), "p99": pct(svc, 99)},
         "queue_ms": {"p50": pct(que, 50), "p99": pct(que, 99)},
@@ -945,6 +955,95 @@ def drift_arm(args, local):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+# loader: the FOV reader with prefetch on the host cores
+# ---------------------------------------------------------------------------
+def write_fov_zarr(root, chans, fov="Conv_zscan__000", workers=None):
+    """One FOV in the layout mermake/io.py:read_im reads: frames of uint8
+    (the square root of the uint16 intensities, as the acquisition stores
+    them), frame 0 a dummy, then the channels interleaved plane by plane,
+    one bz2 (level 9) chunk per frame, and the xml's z_offsets naming the
+    channel count."""
+    import bz2
+    import concurrent.futures as cf
+
+    import numpy as np
+    nch, (Z, X, Y) = len(chans), chans[0].shape
+    d = os.path.join(root, fov.split("_")[-1], "data")
+    os.makedirs(d, exist_ok=True)
+    n = 1 + nch * Z
+    json.dump({"chunks": [1, X, Y], "compressor": {"id": "bz2", "level": 9}, "dtype": "|u1", "fill_value": 0,
+               "filters": None, "order": "C", "shape": [n, X, Y], "zarr_format": 2},
+              open(os.path.join(d, ".zarray"), "w"))
+
+    def frame(i):
+        if i == 0:
+            u8 = np.zeros((X, Y), np.uint8)
+        else:
+            c, z = (i - 1) % nch, (i - 1) // nch
+            u8 = np.minimum(np.rint(np.sqrt(chans[c][z].astype(np.float32))), 255).astype(np.uint8)
+        with open(os.path.join(d, "%d.0.0" % i), "wb") as f:
+            f.write(bz2.compress(u8.tobytes(), 9))
+
+    with cf.ThreadPoolExecutor(max_workers=workers or os.cpu_count()) as ex:
+        list(ex.map(frame, range(n)))
+    with open(os.path.join(root, fov + ".xml"), "w") as f:
+        f.write('<settings><z_offsets type="string">-10:0.3:5:%d</z_offsets></settings>' % nch)
+    os.makedirs(os.path.join(root, fov + ".zarr"), exist_ok=True)
+    return os.path.join(root, fov + ".zarr")
+
+
+def loader_arm(args):
+    """Decode throughput of io.FovPrefetcher (bz2 zarr chunks decoded by a pool
+    of host threads into pinned memory) on one FOV of the fov3c shape read
+    args.steps times."""
+    import shutil
+    import tempfile
+
+    import torch
+
+    from mermake_gb300 import io, synth
+    w = WORKLOADS["fov3c"]
+    Z, X, Y = w["Z"], w["X"], w["Y"]
+    gain = synth.flat_gain(X, Y)
+    chans = [synth.hyb_stack(Z, X, Y, w["puncta"], 1000 + 17 * c, device="cuda", gain=gain).cpu().numpy()
+             for c in range(w["colours"])] + [synth.dapi_stack(Z, X, Y, 1099, device="cuda").cpu().numpy()]
+    root = tempfile.mkdtemp(prefix="mm_loader_")
+    t0 = time.perf_counter()
+    path = write_fov_zarr(root, chans)
+    t_write = time.perf_counter() - t0
+    comp = sum(os.path.getsize(os.path.join(dp, f)) for dp, _, fs in os.walk(root) for f in fs)
+    with io.FovPrefetcher([path] * args.warmup, prefetch=2) as pf:
+        for _ in pf:
+            pass
+    pf = io.FovPrefetcher([path] * args.steps, prefetch=2)
+    t0 = time.perf_counter()
+    n = 0
+    for _, im in pf:
+        if isinstance(im, Exception):
+            raise im
+        n += 1
+    wall = time.perf_counter() - t0
+    pf.close()
+    fov_bytes = sum(c.nbytes for c in chans)
+    line = {
+        "metric": "FOV decode throughput (bz2 zarr -> pinned uint16, host threads)",
+        "value": n / wall,
+        "unit": "FOV/s",
+        "n_gpus": 1, "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * wall / n,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic fov3c channels written as the acquisition's uint8 square-root frames",
+        "config": {"workload": "loader", "Z": Z, "X": X, "Y": Y, "channels": len(chans),
+                   "threads": os.cpu_count(), "pinned": torch.cuda.is_available()},
+        "decoded_GBps": pf.decoded_bytes / pf.decode_seconds / 1e9,
+        "uint16_GBps": n * fov_bytes / wall / 1e9,
+        "compressed_MB_per_fov": comp / 1e6,
+        "write_s": t_write,
+    }
+    print(json.dumps(line), flush=True)
+    shutil.rmtree(root, ignore_errors=True)
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -958,6 +1057,12 @@ def main():
     if args.workload == "drift16":
         if rank == 0:
             drift_arm(args, local)
+        return
+    if args.workload == "loader":
+        if rank == 0:
+            import torch
+            torch.cuda.set_device(local)
+            loader_arm(args)
         return
     gpu_arm(args, rank, world, local)
 

@@ -53,6 +53,11 @@ const char *mm_last_error(void);
  * CuPy's memory pool and the per-call free_all_blocks, mermake/maxima.py:96). */
 int mm_ctx_create(mm_ctx **out);
 int mm_ctx_destroy(mm_ctx *ctx);
+/* Device bytes of scratch the context holds (no reference counterpart; for
+ * callers that budget device memory, e.g. a serving loop).  The scratch grows
+ * on demand, in stream order on the calling stream, and is freed by
+ * mm_ctx_destroy.  Safe to call while another thread uses the context. */
+int mm_ctx_scratch_bytes(const mm_ctx *ctx, uint64_t *bytes);
 
 /* Context options (no reference counterpart).  MM_OPT_BLUR_MODE selects how
  * the blur subtraction of tile_wise (mermake/deconvolver.py:160-163: the
@@ -72,8 +77,23 @@ int mm_ctx_destroy(mm_ctx *ctx);
  *   MM_BLUR_SPECTRAL: as AUTO, and mm_deconv_tiles folds as well (overlap >=
  *     d + 1), so that it returns the volumes the drivers compute (its voxels
  *     within d of a tile edge then differ from the truncated blur's). */
-enum { MM_OPT_BLUR_MODE = 1 };
+enum { MM_OPT_BLUR_MODE = 1, MM_OPT_ZFORM = 2 };
 enum { MM_BLUR_AUTO = 0, MM_BLUR_EXACT = 1, MM_BLUR_SPECTRAL = 2 };
+/* MM_OPT_ZFORM selects how the z step of tile_wise (padding by reflection,
+ * transforms over Zp, times W, crop; mermake/deconvolver.py:139-157) runs:
+ *   MM_ZFORM_AUTO (default): the first form below that the batch qualifies for
+ *     (the two matrix forms from batches of 10 tiles);
+ *   MM_ZFORM_REGISTERS: one Z x Z matrix per frequency, formed in registers
+ *     from the z kernel (one spectrum, Z a multiple of 5, 1 <= zpad <= Z - 1,
+ *     up to 30 tiles), operands staged by TMA;
+ *   MM_ZFORM_SHARED: the same matrix summed into shared memory (one spectrum,
+ *     Z <= 64, at most four copies of a plane);
+ *   MM_ZFORM_DIRECT: the direct sum over the padded planes per tile;
+ *   MM_ZFORM_TRANSFORMS: the reference's transforms over the padded depth.
+ * A form the batch does not qualify for falls back to AUTO's choice.  All
+ * forms give the same voxels within float32 rounding; the choice is a
+ * performance setting (tune.autotune picks it per geometry). */
+enum { MM_ZFORM_AUTO = 0, MM_ZFORM_REGISTERS = 1, MM_ZFORM_SHARED = 2, MM_ZFORM_DIRECT = 3, MM_ZFORM_TRANSFORMS = 4 };
 int mm_ctx_set_option(mm_ctx *ctx, int option, int value);
 
 /* fill.reflect (mermake/fill.py:54-111, kernel `mirror` fill.py:6-52), in place.

@@ -15,8 +15,9 @@ import torch
 from . import _build
 
 MM_OK, MM_EINVAL, MM_ENOMEM, MM_EOVERFLOW, MM_ETIMEOUT, MM_EDEVICE = range(6)
-MM_OPT_BLUR_MODE = 1
+MM_OPT_BLUR_MODE, MM_OPT_ZFORM = 1, 2
 MM_BLUR_AUTO, MM_BLUR_EXACT, MM_BLUR_SPECTRAL = range(3)
+MM_ZFORM_AUTO, MM_ZFORM_REGISTERS, MM_ZFORM_SHARED, MM_ZFORM_DIRECT, MM_ZFORM_TRANSFORMS = range(5)
 
 _lock = threading.Lock()
 _lib = None
@@ -47,6 +48,7 @@ _SIGS = {
     "mm_last_error": ([], C.c_char_p),
     "mm_ctx_create": ([C.POINTER(_vp)], _i32),
     "mm_ctx_destroy": ([_vp], _i32),
+    "mm_ctx_scratch_bytes": ([_vp, C.POINTER(C.c_uint64)], _i32),
     "mm_ctx_set_option": ([_vp, _i32, _i32], _i32),
     "mm_reflect_f32": ([_vp, _i32, _pi64, _pi64, _i32, _i32, _i32, _vp], _i32),
     "mm_box_1d_f32": ([_vp, _pi64, _vp, _pi64, _i32, _i32, _i32, _i32, _i32, _vp], _i32),
@@ -139,6 +141,13 @@ def release_thread_ctx():
     per.clear()
 
 
+def scratch_bytes(device=None):
+    """Device bytes of library scratch the calling thread's context holds."""
+    v = C.c_uint64(0)
+    check(lib().mm_ctx_scratch_bytes(ctx(device), C.byref(v)))
+    return int(v.value)
+
+
 def last_error():
     return (_lib.mm_last_error() or b"").decode(errors="replace") if _lib else ""
 
@@ -205,3 +214,19 @@ class blur_mode:
 
     def __exit__(self, *exc):
         check(lib().mm_ctx_set_option(ctx(self.device), MM_OPT_BLUR_MODE, MM_BLUR_AUTO))
+
+
+class zform:
+    """Context manager: the calling thread's library context runs the z step
+    in the given form (MM_ZFORM_*, see mm_ctx_set_option) inside the block and
+    with MM_ZFORM_AUTO after it."""
+
+    def __init__(self, form, device=None):
+        self.form, self.device = int(form), device
+
+    def __enter__(self):
+        check(lib().mm_ctx_set_option(ctx(self.device), MM_OPT_ZFORM, self.form))
+        return self
+
+    def __exit__(self, *exc):
+        check(lib().mm_ctx_set_option(ctx(self.device), MM_OPT_ZFORM, MM_ZFORM_AUTO))

@@ -70,6 +70,10 @@ struct mm_ctx {
     unsigned *h_counters = nullptr;  // pinned: [0] candidates, [1] rows, [2] rows (2nd set)
     int device = 0;
     int blur_mode = MM_BLUR_AUTO;    // mm_ctx_set_option(MM_OPT_BLUR_MODE)
+    int zform = MM_ZFORM_AUTO;       // mm_ctx_set_option(MM_OPT_ZFORM)
+    bool used = false;               // a call has used the scratch ...
+    cudaStream_t last_stream = nullptr;  // ... on this stream
+    std::atomic<unsigned long long> scratch_total{0};  // device bytes of scratch held
     Prof prof;
 };
 
@@ -108,31 +112,41 @@ struct StageTimer {
     }
 };
 
-int ws_get(mm_ctx *c, Slot s, size_t bytes, void **out) {
+// Scratch slot s of at least `bytes`, grown (never shrunk) in stream order on
+// the calling stream st: the old buffer is freed and the new one allocated on
+// st (cudaFreeAsync / cudaMallocAsync), so growing does not wait for the rest
+// of the device.  Earlier work of this context on st is ordered before the
+// free; when the context's previous call ran on another stream, the device is
+// synchronised first, as that work may still read the old buffer.
+int ws_get(mm_ctx *c, Slot s, size_t bytes, void **out, cudaStream_t st) {
     if (bytes == 0) bytes = 16;
     if (c->ws_bytes[s] < bytes) {
         if (c->ws[s]) {
-            MM_CUDA_TRY(cudaDeviceSynchronize());
-            cudaFree(c->ws[s]);
+            if (c->used && c->last_stream != st) MM_CUDA_TRY(cudaDeviceSynchronize());
+            MM_CUDA_TRY(cudaFreeAsync(c->ws[s], st));
+            c->scratch_total.fetch_sub(c->ws_bytes[s]);
             c->ws[s] = nullptr;
             c->ws_bytes[s] = 0;
         }
         // grow with headroom so that slowly growing requests do not thrash
         size_t want = bytes + bytes / 8;
-        cudaError_t e = cudaMalloc(&c->ws[s], want);
+        cudaError_t e = cudaMallocAsync(&c->ws[s], want, st);
         if (e != cudaSuccess) {
             cudaGetLastError();
-            e = cudaMalloc(&c->ws[s], bytes);
+            e = cudaMallocAsync(&c->ws[s], bytes, st);
             want = bytes;
         }
         if (e != cudaSuccess) {
             cudaGetLastError();
             c->ws[s] = nullptr;
-            mm_set_error("cudaMalloc of %zu bytes of scratch failed: %s", bytes, cudaGetErrorString(e));
+            mm_set_error("allocation of %zu bytes of scratch failed: %s", bytes, cudaGetErrorString(e));
             return MM_ENOMEM;
         }
         c->ws_bytes[s] = want;
+        c->scratch_total.fetch_add(want);
     }
+    c->used = true;
+    c->last_stream = st;
     *out = c->ws[s];
     return MM_OK;
 }
@@ -143,17 +157,31 @@ struct Small {
     unsigned rows;       // kept rows (set 1)
     unsigned rows2;      // kept rows (set 2)
     unsigned overflow;   // largest candidate count that did not fit
+    unsigned err;        // a kernel gave up a bounded wait (MM_ETIMEOUT)
+    unsigned pad0_;
     double sumsq;
     float div;
     float pad_;
     double parts[MM_SUM_PARTS];  // per-block partial sums (fixed-order reductions)
 };
 
-int small_get(mm_ctx *c, Small **out) {
+int small_get(mm_ctx *c, Small **out, cudaStream_t st) {
     void *p;
-    int rc = ws_get(c, WS_SMALL, sizeof(Small), &p);
+    const bool fresh = c->ws[WS_SMALL] == nullptr;
+    int rc = ws_get(c, WS_SMALL, sizeof(Small), &p, st);
+    if (rc) return rc;
+    if (fresh) MM_CUDA_TRY(cudaMemsetAsync(p, 0, sizeof(Small), st));  // counters and the error flag start at zero
     *out = (Small *)p;
-    return rc;
+    return MM_OK;
+}
+
+// A kernel's bounded wait gave up (Small::err, read back with the counters):
+// clears the flag and reports MM_ETIMEOUT.
+int timeout_seen(Small *sm, unsigned err, cudaStream_t st) {
+    if (!err) return MM_OK;
+    MM_CUDA_TRY(cudaMemsetAsync(&sm->err, 0, sizeof(unsigned), st));
+    mm_set_error("a kernel gave up waiting for its shared-memory copies");
+    return MM_ETIMEOUT;
 }
 
 int ntiles_of(const TileGeom &g) {
@@ -198,12 +226,35 @@ int fill_geom(TileGeom &g, int Z, int X, int Y, long long isz, long long isx, lo
 // kept spots of a hyb tile have centroids inside it and read their maxima and
 // fit neighbourhoods, at most delta_fit + max(delta, delta_fit) closer to the
 // edge.
+// The z step of a batch: MM_ZFORM_REGISTERS (k_zth_apply), _SHARED
+// (k_zop_apply), _DIRECT (k_zconv) or _TRANSFORMS (k_zpass).  The context's
+// MM_OPT_ZFORM choice when the batch qualifies for it (a z kernel, one
+// spectrum for the two matrix forms, the forms' shape limits), else the first
+// of those four that qualifies, the matrix forms only for batches of at least
+// MM_ZOP_MIN_TILES tiles.
+int zform_of(const mm_ctx *c, const TileGeom &g, const float2 *zop) {
+    const long long plane = (long long)g.P * g.H;
+    auto ok = [&](int f, int min_tiles) {
+        switch (f) {
+            case MM_ZFORM_REGISTERS:
+                return zop && g.npsf == 1 && g.nt >= min_tiles && mm_zth_supported(g.Z, g.zpad, g.nt, plane) != 0;
+            case MM_ZFORM_SHARED:
+                return zop && g.npsf == 1 && g.nt >= min_tiles && mm_zop_supported(g.Z, g.zpad) != 0;
+            case MM_ZFORM_DIRECT: return zop && mm_zconv_supported(g.Z, g.zpad) != 0;
+            default: return true;
+        }
+    };
+    if (c->zform != MM_ZFORM_AUTO && ok(c->zform, 1)) return c->zform;
+    for (int f : {MM_ZFORM_REGISTERS, MM_ZFORM_SHARED, MM_ZFORM_DIRECT})
+        if (ok(f, MM_ZOP_MIN_TILES)) return f;
+    return MM_ZFORM_TRANSFORMS;
+}
+
 bool fold_allowed(const mm_ctx *c, const TileGeom &g, int blur_radius, const float2 *zop, bool driver, int reach) {
     if (blur_radius < 0 || !zop || c->blur_mode == MM_BLUR_EXACT) return false;
     if (!driver && c->blur_mode != MM_BLUR_SPECTRAL) return false;
-    const bool zk = (g.npsf == 1 && g.nt >= MM_ZOP_MIN_TILES && mm_zop_supported(g.Z, g.zpad)) ||
-                    mm_zconv_supported(g.Z, g.zpad);
-    return zk && g.ov - reach >= blur_radius / 2 + 1 && 2 * (blur_radius / 2) + 1 <= g.P;
+    return zform_of(c, g, zop) != MM_ZFORM_TRANSFORMS && g.ov - reach >= blur_radius / 2 + 1 &&
+           2 * (blur_radius / 2) + 1 <= g.P;
 }
 
 // tile_wise core for tiles [g.t0, g.t0 + g.nt); fold: the blur subtraction
@@ -227,10 +278,10 @@ int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *
     if (fold && delta >= 0 && (rc = mm_blur_response_get(g.P, delta, &fresp))) return rc;
     // the box means still to take on the result
     const int rdelta = fresp ? -1 : delta;
-    if ((rc = ws_get(c, WS_SPEC, sizeof(float2) * tile_c * g.nt, &spec))) return rc;
+    if ((rc = ws_get(c, WS_SPEC, sizeof(float2) * tile_c * g.nt, &spec, st))) return rc;
     res = res_out;
-    if (!res && (rc = ws_get(c, WS_RES, sizeof(float) * tile_r * g.nt, &res))) return rc;
-    if (rdelta >= 0 && (rc = ws_get(c, WS_TMP, sizeof(float) * tile_r * g.nt, &tmp))) return rc;
+    if (!res && (rc = ws_get(c, WS_RES, sizeof(float) * tile_r * g.nt, &res, st))) return rc;
+    if (rdelta >= 0 && (rc = ws_get(c, WS_TMP, sizeof(float) * tile_r * g.nt, &tmp, st))) return rc;
     float2 *S = (float2 *)spec;
     const long long wstride = (long long)g.Zp * plane_c;
     // algorithmic bytes of each stage for this batch (its inputs read once, outputs written once)
@@ -248,11 +299,19 @@ int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *
         StageTimer t(c, ST_COLS_FWD, 2 * spec_b, st);
         if ((rc = mm_launch_cols(S, g.P, g.H, g.H, plane_c, g.nt * g.Z, false, st))) return rc;
     }
-    if (zop && g.npsf == 1 && g.nt >= MM_ZOP_MIN_TILES && mm_zop_supported(g.Z, g.zpad)) {
+    const int zform = zform_of(c, g, zop);
+    if (zform == MM_ZFORM_REGISTERS) {
+        // the matrix formed in registers, operands staged by TMA; the z kernel
+        // is read once per batch
+        Small *sm;
+        if ((rc = small_get(c, &sm, st))) return rc;
+        StageTimer t(c, ST_ZPASS, 2 * spec_b + 8.0 * wstride, st);
+        if ((rc = mm_launch_zth_apply(S, zop, g.Z, g.zpad, g.Zp, plane_c, g.nt, fresp, &sm->err, st))) return rc;
+    } else if (zform == MM_ZFORM_SHARED) {
         // the z kernel (Zp per frequency, the size of W) is read once per batch
         StageTimer t(c, ST_ZPASS, 2 * spec_b + 8.0 * wstride, st);
         if ((rc = mm_launch_zop_apply(S, zop, g.Z, g.zpad, g.Zp, plane_c, g.nt, fresp, st))) return rc;
-    } else if (zop && mm_zconv_supported(g.Z, g.zpad)) {
+    } else if (zform == MM_ZFORM_DIRECT) {
         // each tile's z kernel read once (once per batch when shared)
         StageTimer t(c, ST_ZPASS, 2 * spec_b + (g.npsf == 1 ? 8.0 * wstride : w_b), st);
         if ((rc = mm_launch_zconv(S, zop, wstride, g.Z, g.zpad, g.Zp, plane_c, g.t0, g.nt, g.npsf, fresp, st)))
@@ -266,15 +325,19 @@ int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *
         StageTimer t(c, ST_COLS_INV, 2 * spec_b, st);
         if ((rc = mm_launch_cols(S, g.P, g.H, g.H, plane_c, g.nt * g.Z, true, st))) return rc;
     }
+    // with the blur folded and only the centre read, the stitched buffer is
+    // written straight from the inverse pass
+    const bool direct_stitch = fresp && win == -1 && !res_out && stitch;
     if (fresp && win >= -1 && !res_out) {
         StageTimer t(c, ST_ROWS_INV, spec_b + real_b, st);
-        if ((rc = mm_launch_rows_inv_win(S, g, win, (float *)res, st))) return rc;
+        if ((rc = mm_launch_rows_inv_win(S, g, win, (float *)res, direct_stitch ? stitch : nullptr, osz, osx, st)))
+            return rc;
     } else {
         StageTimer t(c, ST_ROWS_INV, spec_b + real_b * (rdelta >= 0 ? 2 : 1), st);
         if ((rc = mm_launch_rows_inv(S, g.nt * g.Z * g.P, g.P, g.H, (float *)res, (float *)tmp, rdelta, st)))
             return rc;
     }
-    if (rdelta >= 0 || stitch) {
+    if (rdelta >= 0 || (stitch && !direct_stitch)) {
         // with no box mean left to take, only the stitch: the result is final
         // in res already and is not written back
         StageTimer t(c, ST_BLUR_X, (rdelta >= 0 ? 3 : 2) * real_b, st);
@@ -326,9 +389,16 @@ int mm_ctx_destroy(mm_ctx *c) {
             cudaEventDestroy(c->prof.ev1[i]);
         }
     for (int s = 0; s < WS_N; ++s)
-        if (c->ws[s]) cudaFree(c->ws[s]);
+        if (c->ws[s]) cudaFreeAsync(c->ws[s], 0);
+    cudaStreamSynchronize(0);
     if (c->h_counters) cudaFreeHost(c->h_counters);
     delete c;
+    return MM_OK;
+}
+
+int mm_ctx_scratch_bytes(const mm_ctx *c, uint64_t *bytes) {
+    MM_REQUIRE(c && bytes, "null argument");
+    *bytes = c->scratch_total.load();
     return MM_OK;
 }
 
@@ -345,9 +415,9 @@ int mm_wiener_spectrum(mm_ctx *c, const float *psf, int pz, int px, int py, int 
     void *vol, *spec;
     Small *sm;
     int rc;
-    if ((rc = ws_get(c, WS_VOL, sizeof(float) * (size_t)nz * nx * nx, &vol))) return rc;
-    if ((rc = ws_get(c, WS_SPEC, sizeof(float2) * (size_t)nz * nx * H, &spec))) return rc;
-    if ((rc = small_get(c, &sm))) return rc;
+    if ((rc = ws_get(c, WS_VOL, sizeof(float) * (size_t)nz * nx * nx, &vol, st))) return rc;
+    if ((rc = ws_get(c, WS_SPEC, sizeof(float2) * (size_t)nz * nx * H, &spec, st))) return rc;
+    if ((rc = small_get(c, &sm, st))) return rc;
     StageTimer tm(c, ST_WIENER, 4.0 * nz * nx * nx + 8.0 * nz * nx * H, st);
     return mm_wiener_build_impl(psf, pz, px, py, tile_height, tile_size, zpad, overlap, beta, (float2 *)W,
                                 (float *)vol, (float2 *)spec, &sm->sumsq, sm->parts, st);
@@ -406,12 +476,12 @@ int mm_find_local_maxima(mm_ctx *c, const float *image, int Z, int X, int Y, int
     cudaStream_t st = (cudaStream_t)stream;
     Small *sm;
     int rc;
-    if ((rc = small_get(c, &sm))) return rc;
+    if ((rc = small_get(c, &sm, st))) return rc;
     for (int attempt = 0; attempt < 2; ++attempt) {
         size_t cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
         if (cap < 65536) cap = 65536;
         void *cand;
-        if ((rc = ws_get(c, WS_CAND, cap * sizeof(uint2), &cand))) return rc;
+        if ((rc = ws_get(c, WS_CAND, cap * sizeof(uint2), &cand, st))) return rc;
         cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
         MaximaArgs a = {};
         a.img = image; a.isz = isz; a.isx = isx; a.ivol = 0;
@@ -430,7 +500,7 @@ int mm_find_local_maxima(mm_ctx *c, const float *image, int Z, int X, int Y, int
             *count = n;
             return n > out_cap ? MM_EOVERFLOW : MM_OK;
         }
-        if ((rc = ws_get(c, WS_CAND, (size_t)n * sizeof(uint2), &cand))) return rc;
+        if ((rc = ws_get(c, WS_CAND, (size_t)n * sizeof(uint2), &cand, st))) return rc;
     }
     mm_set_error("candidate list did not converge");
     return MM_EDEVICE;
@@ -486,10 +556,10 @@ static int hyb_pass(mm_ctx *c, const TileGeom &g, int batch, const uint16_t *ima
 }
 
 // the candidate list: at least 1 M entries, as large as any earlier call made it
-static int cand_list(mm_ctx *c, void **cand, size_t *cap) {
+static int cand_list(mm_ctx *c, void **cand, size_t *cap, cudaStream_t st) {
     size_t n = c->ws_bytes[WS_CAND] / sizeof(uint2);
     if (n < (1u << 20)) n = 1u << 20;
-    int rc = ws_get(c, WS_CAND, n * sizeof(uint2), cand);
+    int rc = ws_get(c, WS_CAND, n * sizeof(uint2), cand, st);
     if (rc) return rc;
     *cap = c->ws_bytes[WS_CAND] / sizeof(uint2);
     return MM_OK;
@@ -512,24 +582,25 @@ int mm_hyb_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t 
     std::lock_guard<std::mutex> lock(c->mu);
     cudaStream_t st = (cudaStream_t)stream;
     Small *sm;
-    if ((rc = small_get(c, &sm))) return rc;
+    if ((rc = small_get(c, &sm, st))) return rc;
     *count = 0;
     for (int attempt = 0; attempt < 2; ++attempt) {
         void *cand;
         size_t cap;
-        if ((rc = cand_list(c, &cand, &cap))) return rc;
+        if ((rc = cand_list(c, &cand, &cap, st))) return rc;
         if ((rc = hyb_pass(c, g, batch, image, flat, W, zop, blur_radius, threshold, delta, delta_fit, sigmaZ,
                            sigmaXY, out, out_cap, cand, cap, sm, st)))
             return rc;
-        MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters, &sm->rows, 2 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
-        MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters + 2, &sm->overflow, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        // rows, rows2, overflow and err are consecutive in Small
+        MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters, &sm->rows, 4 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
         MM_CUDA_TRY(cudaStreamSynchronize(st));
+        if ((rc = timeout_seen(sm, c->h_counters[3], st))) return rc;
         unsigned over = c->h_counters[2];
         if (over == 0) {
             *count = c->h_counters[0];
             return *count > out_cap ? MM_EOVERFLOW : MM_OK;
         }
-        if ((rc = ws_get(c, WS_CAND, (size_t)over * sizeof(uint2), &cand))) return rc;
+        if ((rc = ws_get(c, WS_CAND, (size_t)over * sizeof(uint2), &cand, st))) return rc;
     }
     mm_set_error("candidate list did not converge");
     return MM_EDEVICE;
@@ -551,13 +622,15 @@ int mm_hyb_spots_async(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, in
     std::lock_guard<std::mutex> lock(c->mu);
     cudaStream_t st = (cudaStream_t)stream;
     Small *sm;
-    if ((rc = small_get(c, &sm))) return rc;
+    if ((rc = small_get(c, &sm, st))) return rc;
     void *cand;
     size_t cap;
-    if ((rc = cand_list(c, &cand, &cap))) return rc;
+    if ((rc = cand_list(c, &cand, &cap, st))) return rc;
     if ((rc = hyb_pass(c, g, batch, image, flat, W, zop, blur_radius, threshold, delta, delta_fit, sigmaZ, sigmaXY,
                        out, out_cap, cand, cap, sm, st)))
         return rc;
+    // a timed-out wait makes the result incomplete, like a candidate overflow
+    if ((rc = mm_launch_note_overflow(&sm->err, 0, &sm->overflow, st))) return rc;
     MM_CUDA_TRY(cudaMemcpyAsync(count_dev, &sm->rows, sizeof(unsigned), cudaMemcpyDeviceToDevice, st));
     MM_CUDA_TRY(cudaMemcpyAsync(overflow_dev, &sm->overflow, sizeof(unsigned), cudaMemcpyDeviceToDevice, st));
     return MM_OK;
@@ -634,18 +707,19 @@ int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t
     std::lock_guard<std::mutex> lock(c->mu);
     cudaStream_t st = (cudaStream_t)stream;
     Small *sm;
-    if ((rc = small_get(c, &sm))) return rc;
+    if ((rc = small_get(c, &sm, st))) return rc;
     for (int attempt = 0; attempt < 2; ++attempt) {
         void *cand;
         size_t cap;
-        if ((rc = cand_list(c, &cand, &cap))) return rc;
+        if ((rc = cand_list(c, &cand, &cap, st))) return rc;
         if ((rc = dapi_pass(c, g, batch, image, isz, isx, flat, W, zop, blur_radius, threshold, delta, delta_fit,
                             sigmaZ, sigmaXY, buffer, out_plus, cap_plus, out_minus, cap_minus, cand, cap, sm, st)))
             return rc;
-        MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters, &sm->rows, 3 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+        MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters, &sm->rows, 4 * sizeof(unsigned), cudaMemcpyDeviceToHost, st));
         float hdiv = 0.f;
         MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters + 4, &sm->div, sizeof(float), cudaMemcpyDeviceToHost, st));
         MM_CUDA_TRY(cudaStreamSynchronize(st));
+        if ((rc = timeout_seen(sm, c->h_counters[3], st))) return rc;
         memcpy(&hdiv, c->h_counters + 4, sizeof(float));
         if (rms) *rms = hdiv;
         if (c->h_counters[2] == 0) {
@@ -653,7 +727,7 @@ int mm_dapi_spots(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, int64_t
             *count_minus = c->h_counters[1];
             return (*count_plus > cap_plus || *count_minus > cap_minus) ? MM_EOVERFLOW : MM_OK;
         }
-        if ((rc = ws_get(c, WS_CAND, 2 * (size_t)c->h_counters[2] * sizeof(uint2), &cand))) return rc;
+        if ((rc = ws_get(c, WS_CAND, 2 * (size_t)c->h_counters[2] * sizeof(uint2), &cand, st))) return rc;
     }
     mm_set_error("candidate list did not converge");
     return MM_EDEVICE;
@@ -676,13 +750,14 @@ int mm_dapi_spots_async(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, i
     std::lock_guard<std::mutex> lock(c->mu);
     cudaStream_t st = (cudaStream_t)stream;
     Small *sm;
-    if ((rc = small_get(c, &sm))) return rc;
+    if ((rc = small_get(c, &sm, st))) return rc;
     void *cand;
     size_t cap;
-    if ((rc = cand_list(c, &cand, &cap))) return rc;
+    if ((rc = cand_list(c, &cand, &cap, st))) return rc;
     if ((rc = dapi_pass(c, g, batch, image, isz, isx, flat, W, zop, blur_radius, threshold, delta, delta_fit, sigmaZ,
                         sigmaXY, buffer, out_plus, cap_plus, out_minus, cap_minus, cand, cap, sm, st)))
         return rc;
+    if ((rc = mm_launch_note_overflow(&sm->err, 0, &sm->overflow, st))) return rc;
     // rows, rows2 and overflow are consecutive in Small
     MM_CUDA_TRY(cudaMemcpyAsync(counts_dev, &sm->rows, 3 * sizeof(unsigned), cudaMemcpyDeviceToDevice, st));
     if (rms_dev) MM_CUDA_TRY(cudaMemcpyAsync(rms_dev, &sm->div, sizeof(float), cudaMemcpyDeviceToDevice, st));
@@ -693,11 +768,16 @@ int mm_dapi_spots_async(mm_ctx *c, const uint16_t *image, int Z, int X, int Y, i
 
 extern "C" int mm_ctx_set_option(mm_ctx *c, int option, int value) {
     MM_REQUIRE(c, "null context");
-    MM_REQUIRE(option == MM_OPT_BLUR_MODE, "unknown option %d", option);
-    MM_REQUIRE(value == MM_BLUR_AUTO || value == MM_BLUR_EXACT || value == MM_BLUR_SPECTRAL,
-               "unknown blur mode %d", value);
+    MM_REQUIRE(option == MM_OPT_BLUR_MODE || option == MM_OPT_ZFORM, "unknown option %d", option);
     std::lock_guard<std::mutex> lock(c->mu);
-    c->blur_mode = value;
+    if (option == MM_OPT_BLUR_MODE) {
+        MM_REQUIRE(value == MM_BLUR_AUTO || value == MM_BLUR_EXACT || value == MM_BLUR_SPECTRAL,
+                   "unknown blur mode %d", value);
+        c->blur_mode = value;
+    } else {
+        MM_REQUIRE(value >= MM_ZFORM_AUTO && value <= MM_ZFORM_TRANSFORMS, "unknown z form %d", value);
+        c->zform = value;
+    }
     return MM_OK;
 }
 
@@ -779,7 +859,7 @@ extern "C" int mm_median_f32(mm_ctx *c, const float *x, int64_t n, float *median
     cudaStream_t st = (cudaStream_t)stream;
     void *scr;
     int rc;
-    if ((rc = ws_get(c, WS_SELECT, sizeof(unsigned) * 272, &scr))) return rc;
+    if ((rc = ws_get(c, WS_SELECT, sizeof(unsigned) * 272, &scr, st))) return rc;
     float *med_dev = reinterpret_cast<float *>(static_cast<unsigned *>(scr) + 264);
     if ((rc = mm_median_impl(x, n, static_cast<unsigned *>(scr), med_dev, out, st))) return rc;
     MM_CUDA_TRY(cudaMemcpyAsync(c->h_counters + 8, med_dev, sizeof(float), cudaMemcpyDeviceToHost, st));

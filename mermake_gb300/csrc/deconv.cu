@@ -253,13 +253,28 @@ k_rows_fwd_f32(const float *__restrict__ vol, long long nrows, float2 *__restric
 // in-range count) is written to `blur` as well: each lane slides a window
 // over a contiguous segment of the row held in shared memory.
 // ---------------------------------------------------------------------------
+// The stitched destination of a group's rows (Deconvolver.apply,
+// deconvolver.py:179-183): rows of plane z of tile ti starting at batch row
+// `base`; a voxel (x, y) of the window [ov, xend - ov) x [ov, yend - ov) goes to
+// the FOV voxel (d.x + x - ov, d.y + y - ov) when this tile is that voxel's
+// last writer in the reference's order (mm_stitch_owner).
+struct StitchMap {
+    float *out;
+    long long osz, osx;
+    long long base;
+    int z, ti, xlo;
+    TileDesc d;
+    const TileGeom *g;
+};
+
 template <int LMAX, int NF, int NLF>
 __device__ __forceinline__ void rows_inv_group(const float2 *__restrict__ S, long long nrows, int H,
                                                float *__restrict__ out, float *__restrict__ blur, int delta,
                                                const FftPlan &P, int nl, const FftSmem &L, long long row0,
-                                               int ylo = 0, int yhi = 1 << 30) {
+                                               int ylo = 0, int yhi = 1 << 30, const StitchMap *smap = nullptr) {
     // rows [row0, nrows) of the group exist (nrows: the end of the group's
-    // window, or of the batch); only columns [ylo, yhi) are stored
+    // window, or of the batch); only columns [ylo, yhi) are stored, into `out`
+    // (row-major, n per row) or the stitched FOV buffer (smap)
     if constexpr (NF > 0) {
         nl = NLF;
         H = NF / 2 + 1;
@@ -300,7 +315,20 @@ __device__ __forceinline__ void rows_inv_group(const float2 *__restrict__ S, lon
     for (int it = threadIdx.x; it < 2 * nl * n; it += blockDim.x) {
         const int q = fdiv_i(it, n, invn), e = it - q * n;
         const long long row = row0 + q;
-        if (row < nrows && e >= ylo && e < yhi) out[row * n + e] = Rf[2 * sidx(e, q >> 1, nl) + (q & 1)];
+        if (row >= nrows || e < ylo || e >= yhi) continue;
+        const float v = Rf[2 * sidx(e, q >> 1, nl) + (q & 1)];
+        if (!smap) {
+            out[row * n + e] = v;
+            continue;
+        }
+        const long long xr = row - smap->base;
+        if (xr < smap->xlo) continue;  // the row paired in from before the window
+        const TileGeom &g = *smap->g;
+        const int ox = smap->d.x + (int)xr - g.ov, oy = smap->d.y + e - g.ov;
+        // inside its own span a tile is the final writer; past it, ask who is
+        const bool own = ox < smap->d.x + g.ts && oy < smap->d.y + g.ts;
+        if (ox < g.X && oy < g.Y && (own || mm_stitch_owner(g, ox, oy) == smap->ti))
+            smap->out[smap->z * smap->osz + (long long)ox * smap->osx + oy] = v;
     }
     if (delta < 0) return;
     // y blur: the free ping-pong buffer holds 2 nl rows of n floats
@@ -380,7 +408,7 @@ constexpr int kMaxWinTiles = 256;
 template <int LMAX, int NF = 0, int NLF = 0>
 __global__ void __launch_bounds__(kRowsInvCfg.threads, kRowsInvCfg.ctas)
 k_rows_inv_win(const float2 *__restrict__ S, TileGeom g, int reach, float *__restrict__ out, FftPlan P, int nl,
-               int cum_off) {
+               int cum_off, float *__restrict__ stitch, long long osz, long long osx) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     int *cum = reinterpret_cast<int *>(smem_raw + cum_off);  // groups before tile t (nt + 1 entries)
     const FftSmem L = fft_smem_layout(smem_raw, P, nl);
@@ -414,7 +442,16 @@ k_rows_inv_win(const float2 *__restrict__ S, TileGeom g, int reach, float *__res
         // are those of the whole-tile pass (rows 2l and 2l + 1); the row
         // before the window that this may add is computed exactly as there
         const long long row0 = ((base + xlo) & ~1LL) + (long long)c * gr;
-        rows_inv_group<LMAX, NF, NLF>(S, base + xhi, g.H, out, nullptr, -1, P, nl, L, row0, ylo, yhi);
+        if (stitch) {
+            StitchMap sm;
+            sm.out = stitch; sm.osz = osz; sm.osx = osx;
+            sm.base = base; sm.z = z; sm.ti = g.t0 + t; sm.xlo = xlo;
+            sm.d = mm_tile_desc(g, g.t0 + t);
+            sm.g = &g;
+            rows_inv_group<LMAX, NF, NLF>(S, base + xhi, g.H, out, nullptr, -1, P, nl, L, row0, ylo, yhi, &sm);
+        } else {
+            rows_inv_group<LMAX, NF, NLF>(S, base + xhi, g.H, out, nullptr, -1, P, nl, L, row0, ylo, yhi);
+        }
         __syncthreads();
     }
 }
@@ -597,7 +634,9 @@ int mm_launch_rows_inv(const float2 *S, int nrows, int Pn, int H, float *out, fl
                              kRowsInvCfg.threads);
 }
 
-int mm_launch_rows_inv_win(const float2 *S, const TileGeom &g, int reach, float *out, cudaStream_t st) {
+int mm_launch_rows_inv_win(const float2 *S, const TileGeom &g, int reach, float *out, float *stitch, long long osz,
+                           long long osx, cudaStream_t st) {
+    MM_REQUIRE(!stitch || reach < 0, "stitching stores the centre window only");
     FftPlan P;
     int rc = mm_fft_plan_get(g.P, &P);
     if (rc) return rc;
@@ -613,7 +652,7 @@ int mm_launch_rows_inv_win(const float2 *S, const TileGeom &g, int reach, float 
     // an upper bound of the groups (the kernel counts the exact number)
     const long long ngroups = (long long)g.nt * g.Z * mm_cdiv(g.P, 2 * nl);
     TileGeom ga = g;
-    void *args[] = {&S, &ga, &reach, &out, &P, &nl, &cum_off};
+    void *args[] = {&S, &ga, &reach, &out, &P, &nl, &cum_off, &stitch, &osz, &osx};
     return launch_fft_kernel(MM_FFT_KERNEL(P, nl, 8, k_rows_inv_win, ), dim3(fft_grid(ngroups, kRowsInvCfg)), sm, st,
                              args, kRowsInvCfg.threads);
 }

@@ -141,6 +141,13 @@ int mm_launch_zop_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, lon
 int mm_zconv_supported(int Z, int zpad);
 int mm_launch_zconv(float2 *S, const float2 *w, long long wstride, int Z, int zpad, int Zp, long long plane, int t0,
                     int nt, int npsf, const float *fresp, cudaStream_t st);
+// The z operator with the matrix of each frequency formed in registers from
+// the z kernel (Toeplitz plus two masked Hankel parts, 1 <= zpad <= Z - 1,
+// Z a multiple of 5) and its operands staged by TMA (zop_tma.cu).  A CTA that
+// gives up waiting for its copies sets *err.
+int mm_zth_supported(int Z, int zpad, int nt, long long plane);
+int mm_launch_zth_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, long long plane, int nt,
+                        const float *fresp, unsigned *err, cudaStream_t st);
 // 1 - D(kx) D(ky) per half-spectrum frequency of a P x P plane, D the
 // frequency response of the box mean of width 2 delta + 1 (zop.cu)
 int mm_blur_response_get(int P, int delta, const float **out);
@@ -150,7 +157,10 @@ int mm_launch_rows_inv(const float2 *S, int nrows, int P, int H, float *out, flo
 // the inverse y pass (no blur) over the rows and columns of each tile that the
 // caller reads: reach >= 0, the band [ov - reach, extent - ov + reach) of the
 // hyb keep filter; reach < 0, the stitched centre [ov, extent - ov)
-int mm_launch_rows_inv_win(const float2 *S, const TileGeom &g, int reach, float *out, cudaStream_t st);
+// (reach < 0 with `stitch` given: the centre goes straight into the stitched
+// FOV buffer, strides osz, osx, in Deconvolver.apply's overwrite order)
+int mm_launch_rows_inv_win(const float2 *S, const TileGeom &g, int reach, float *out, float *stitch, long long osz,
+                           long long osx, cudaStream_t st);
 int mm_launch_blur_x_sub(const TileGeom &g, const float *res, const float *tmp, int delta,
                          float *res_out, float *stitch, long long osz, long long osx, cudaStream_t st);
 int mm_launch_make_raw(const TileGeom &g, const void *img, int dtype, const float *flat, float *raw,

@@ -1,0 +1,337 @@
+// z operator of one Wiener spectrum over a tile batch, with the matrix of each
+// frequency formed in registers and the operands staged by TMA.
+//
+// Y[t][i][p] = sum_j M_p[i][j] X[t][j][p] (zop.cu has the derivation).  When
+// 1 <= zpad <= Z - 1 every real plane j has at most three padded copies
+// (mermake/deconvolver.py:145-148: itself, its reflection about zpad for
+// 1 <= j <= zpad, and its reflection about zpad + Z - 1 for
+// Z - 1 - zpad <= j <= Z - 2), so with w the z kernel (indices mod Zp)
+//
+//   M[i][j] = w[i - j] + [1 <= j <= zpad] w[i + j] + [Z-1-zpad <= j <= Z-2] w[i + j - 2Z + 2]:
+//
+// a Toeplitz matrix plus two masked Hankel matrices.  A thread owns rows
+// i0 .. i0 + 4 of kTT tiles; along j each family's five values slide by one
+// place, so the thread keeps them in three register rings of five and loads
+// one new value of each per column (the slots are compile-time constants with
+// j unrolled by five).  No matrix is stored: shared memory holds only the
+// operands, X (nt x Z x kPB) and the kernel rows w[-kA .. 2Z-2] (two TMA boxes
+// of the (Zp, plane) kernel, the negative rows from its top; kA is 2Z - 2
+// rounded up to a multiple of four, so that both boxes land on 128-byte
+// boundaries as tiled TMA requires), double buffered, each group's loads
+// completing on an mbarrier while the CTA works on the previous group.  The
+// persistent CTAs take groups of kPB consecutive frequencies.  Every wait is
+// bounded: a CTA that gives up records the failure in *err and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
+#include "deconv.cuh"
+
+namespace {
+
+constexpr int kPB = 4;      // frequencies per group (32 bytes of a plane row)
+constexpr int kTI = 5;      // rows of a thread, and the unroll of the column loop
+constexpr int kTT = 5;      // tiles of a thread
+constexpr int kThreadsMax = 256;
+constexpr unsigned kWaitPolls = 1u << 24;
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+// true once the barrier's phase with this parity has completed; false after
+// kWaitPolls polls
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+    const unsigned a = smem_u32(bar);
+    for (unsigned it = 0; it < kWaitPolls; ++it) {
+        unsigned done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                            uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int c0, int c1, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"(map), "r"(c0), "r"(c1), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {
+    c.x = fmaf(a.x, b.x, fmaf(-a.y, b.y, c.x));
+    c.y = fmaf(a.x, b.y, fmaf(a.y, b.x, c.y));
+    return c;
+}
+
+struct ZthArgs {
+    int Z, Zp, nt, ntg;
+    long long plane;
+    int ngroups;       // ceil(plane / kPB)
+    int jin_hi;        // the reflection about zpad copies planes 1 .. jin_hi (= zpad)
+    int jout_lo;       // the reflection about zpad + Z - 1 copies planes jout_lo .. Z - 2
+    int kA;            // staged row of w[0]: 2Z - 2 rounded up to a multiple of 4
+    unsigned xbytes;   // X box bytes (kPB x Z x nt float2)
+    unsigned wbytesA;  // kernel rows -kA .. -1 (kA x 32 bytes, a multiple of 128)
+    unsigned wbytesB;  // kernel rows 0 .. 2Z-2
+    unsigned bufstride, woff;  // bytes per buffer, offset of the kernel rows in it
+    const float *fresp;
+    unsigned *err;
+};
+
+// ZC > 0: Z known at compile time (50, the depth of every channel of the
+// benchmark FOV); otherwise any multiple of kTI.
+template <int ZC>
+__global__ void __launch_bounds__(kThreadsMax, 2)
+k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap xmap,
+            const __grid_constant__ CUtensorMap wmapA, const __grid_constant__ CUtensorMap wmapB, const ZthArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ __align__(8) uint64_t bars[2];
+    const int Z = ZC > 0 ? ZC : a.Z;
+    const int nig = Z / kTI;
+    const int tid = threadIdx.x;
+    const int p = tid % kPB;
+    const int r = tid / kPB;
+    const int ig = r % nig, tg = r / nig;
+    const int i0 = ig * kTI, t0 = tg * kTT;
+    const int kb = a.kA;              // row of w[0] in the staged kernel rows
+    const int ko = kb - (2 * Z - 2);  // row of w[-(2Z-2)], the lowest index the rings read
+
+    // every TMA destination (buffer starts, kernel rows, their second box) is
+    // 128-byte aligned given an aligned base: check the base, and give up
+    // (recording the failure) rather than issue a misaligned copy
+    if ((smem_u32(smem) & 127u) != 0u) {
+        if (tid == 0) atomicOr(a.err, 2u);
+        return;
+    }
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+
+    auto issue = [&](int grp, int buf) {
+        unsigned char *b = smem + (size_t)buf * a.bufstride;
+        const int p0 = grp * kPB;
+        mbar_expect_tx(&bars[buf], a.xbytes + a.wbytesA + a.wbytesB);
+        tma_load_3d(b, &xmap, p0, 0, 0, &bars[buf]);
+        tma_load_2d(b + a.woff, &wmapA, p0, a.Zp - kb, &bars[buf]);
+        tma_load_2d(b + a.woff + a.wbytesA, &wmapB, p0, 0, &bars[buf]);
+    };
+
+    if (tid == 0 && blockIdx.x < a.ngroups) issue(blockIdx.x, 0);
+    int it = 0;
+    for (int grp = blockIdx.x; grp < a.ngroups; grp += gridDim.x, ++it) {
+        const int buf = it & 1;
+        const int nxt = grp + gridDim.x;
+        if (tid == 0 && nxt < a.ngroups) {
+            // the other buffer was last read by the previous group (all threads
+            // passed the barrier at its end); order those reads before the TMA
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(nxt, buf ^ 1);
+        }
+        const bool ok = __syncthreads_and(mbar_wait(&bars[buf], (it >> 1) & 1));
+        if (!ok) {
+            if (tid == 0) {
+                atomicOr(a.err, 1u);
+                // let the other buffer's copies land before the CTA exits
+                if (nxt < a.ngroups) mbar_wait(&bars[buf ^ 1], ((it + 1) >> 1) & 1);
+            }
+            return;
+        }
+        const float2 *X = reinterpret_cast<const float2 *>(smem + (size_t)buf * a.bufstride);
+        const float2 *W = reinterpret_cast<const float2 *>(smem + (size_t)buf * a.bufstride + a.woff);
+        if (tg < a.ntg) {
+            float2 acc[kTI][kTT];
+#pragma unroll
+            for (int u = 0; u < kTI; ++u)
+#pragma unroll
+                for (int b = 0; b < kTT; ++b) acc[u][b] = make_float2(0.f, 0.f);
+            // rings: direct family value of position q (= row - column) in slot
+            // q mod 5; the two reflected families of position q (= row + column)
+            // in slot q mod 5 (i0 and the column blocks are multiples of 5)
+            float2 rT[kTI], rI[kTI], rO[kTI];
+#pragma unroll
+            for (int q = 1; q < kTI; ++q) rT[q] = W[(i0 + q + kb) * kPB + p];
+#pragma unroll
+            for (int q = 0; q < kTI - 1; ++q) {
+                rI[q] = W[(i0 + q + kb) * kPB + p];
+                rO[q] = W[(i0 + q + ko) * kPB + p];
+            }
+            rT[0] = rI[kTI - 1] = rO[kTI - 1] = make_float2(0.f, 0.f);
+            const float2 *xr = X + ((size_t)t0 * Z) * kPB + p;
+            for (int j0 = 0; j0 < Z; j0 += kTI) {
+#pragma unroll
+                for (int u = 0; u < kTI; ++u) {
+                    const int j = j0 + u;
+                    rT[(kTI - u) % kTI] = W[(i0 - j + kb) * kPB + p];
+                    rI[(u + kTI - 1) % kTI] = W[(i0 + j + kTI - 1 + kb) * kPB + p];
+                    rO[(u + kTI - 1) % kTI] = W[(i0 + j + kTI - 1 + ko) * kPB + p];
+                    const bool vin = j >= 1 && j <= a.jin_hi;
+                    const bool vout = j >= a.jout_lo && j <= Z - 2;
+                    float2 m[kTI];
+#pragma unroll
+                    for (int q = 0; q < kTI; ++q) {
+                        m[q] = rT[(q - u + kTI) % kTI];
+                        if (vin) m[q] = cadd(m[q], rI[(q + u) % kTI]);
+                        if (vout) m[q] = cadd(m[q], rO[(q + u) % kTI]);
+                    }
+                    float2 x[kTT];
+#pragma unroll
+                    for (int b = 0; b < kTT; ++b) x[b] = xr[((size_t)b * Z + j) * kPB];
+#pragma unroll
+                    for (int q = 0; q < kTI; ++q)
+#pragma unroll
+                        for (int b = 0; b < kTT; ++b) acc[q][b] = cfma(m[q], x[b], acc[q][b]);
+                }
+            }
+            const long long pg = (long long)grp * kPB + p;
+            if (pg < a.plane) {
+                const float f = a.fresp ? a.fresp[pg] : 1.f;
+#pragma unroll
+                for (int b = 0; b < kTT; ++b) {
+                    const int t = t0 + b;
+                    if (t < a.nt) {
+#pragma unroll
+                        for (int q = 0; q < kTI; ++q)
+                            S[((long long)t * Z + i0 + q) * a.plane + pg] = cscale(acc[q][b], f);
+                    }
+                }
+            }
+        }
+        __syncthreads();  // every read of this buffer precedes the TMA that refills it
+    }
+    // the last group's prefetch is never issued past ngroups, so nothing is in flight
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// rows of float2 (8-byte elements), innermost dimension first
+int make_map(CUtensorMap *m, const void *base, int rank, const cuuint64_t *dims, const cuuint64_t *strides_bytes,
+             const cuuint32_t *box) {
+    auto fn = encode_fn();
+    MM_REQUIRE(fn != nullptr, "cuTensorMapEncodeTiled is not available");
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, (cuuint32_t)rank, const_cast<void *>(base), dims,
+                    strides_bytes, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        mm_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return MM_EDEVICE;
+    }
+    return MM_OK;
+}
+
+// staged row of w[0]: the rows -(2Z-2) .. -1 rounded up to a multiple of four,
+// so that the second kernel box starts on a 128-byte boundary
+int zth_ka(int Z) { return (2 * Z - 2 + 3) & ~3; }
+
+// bytes per buffer: X sized for whole tile groups (the last group's threads
+// read their tiles past nt, whose results are discarded), then the kernel rows
+// -kA .. 2Z - 2; both parts start on 128-byte boundaries
+size_t zth_bufstride(int Z, int nt, unsigned *woff) {
+    const int ntg = (nt + kTT - 1) / kTT;
+    const size_t xb = (size_t)kPB * Z * ntg * kTT * sizeof(float2);
+    const size_t wb = (size_t)kPB * (zth_ka(Z) + 2 * Z - 1) * sizeof(float2);
+    const size_t xo = (xb + 127) & ~(size_t)127;
+    if (woff) *woff = (unsigned)xo;
+    return (xo + wb + 127) & ~(size_t)127;
+}
+
+}  // namespace
+
+int mm_zth_supported(int Z, int zpad, int nt, long long plane) {
+    if (Z < kTI || Z % kTI != 0 || zpad < 1 || zpad > Z - 1 || nt < 1 || plane % 2 != 0) return 0;
+    if (2 * Z - 1 > 256 || zth_ka(Z) > 256) return 0;  // TMA box height
+    const int ntg = (nt + kTT - 1) / kTT;
+    if (kPB * (Z / kTI) * ntg > kThreadsMax) return 0;
+    return 2 * zth_bufstride(Z, nt, nullptr) <= 110 * 1024 && encode_fn() != nullptr;
+}
+
+int mm_launch_zth_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, long long plane, int nt,
+                        const float *fresp, unsigned *err, cudaStream_t st) {
+    MM_REQUIRE(Zp == Z + 2 * zpad && mm_zth_supported(Z, zpad, nt, plane),
+               "z operator (TMA form) does not take Z %d, zpad %d, %d tiles", Z, zpad, nt);
+    MM_REQUIRE(((uintptr_t)S & 15) == 0 && ((uintptr_t)w & 15) == 0, "spectra must be 16-byte aligned");
+    CUtensorMap xmap, wA, wB;
+    const cuuint32_t kb = (cuuint32_t)(2 * Z - 2), kA = (cuuint32_t)zth_ka(Z);
+    {
+        cuuint64_t dims[3] = {(cuuint64_t)plane, (cuuint64_t)Z, (cuuint64_t)nt};
+        cuuint64_t strides[2] = {(cuuint64_t)plane * 8, (cuuint64_t)plane * 8 * Z};
+        cuuint32_t box[3] = {kPB, (cuuint32_t)Z, (cuuint32_t)nt};
+        if (int rc = make_map(&xmap, S, 3, dims, strides, box)) return rc;
+    }
+    {
+        cuuint64_t dims[2] = {(cuuint64_t)plane, (cuuint64_t)Zp};
+        cuuint64_t strides[1] = {(cuuint64_t)plane * 8};
+        cuuint32_t boxA[2] = {kPB, kA}, boxB[2] = {kPB, kb + 1};
+        if (int rc = make_map(&wA, w, 2, dims, strides, boxA)) return rc;
+        if (int rc = make_map(&wB, w, 2, dims, strides, boxB)) return rc;
+    }
+    ZthArgs a = {};
+    a.Z = Z;
+    a.Zp = Zp;
+    a.nt = nt;
+    a.ntg = (nt + kTT - 1) / kTT;
+    a.plane = plane;
+    a.ngroups = (int)((plane + kPB - 1) / kPB);
+    a.jin_hi = zpad;
+    a.jout_lo = Z - 1 - zpad;
+    a.kA = (int)kA;
+    a.xbytes = (unsigned)(kPB * Z * nt * sizeof(float2));
+    a.wbytesA = (unsigned)(kPB * kA * sizeof(float2));
+    a.wbytesB = (unsigned)(kPB * (kb + 1) * sizeof(float2));
+    a.bufstride = (unsigned)zth_bufstride(Z, nt, &a.woff);
+    MM_REQUIRE(a.bufstride % 128 == 0 && a.woff % 128 == 0 && a.wbytesA % 128 == 0,
+               "TMA destinations of the z operator must be 128-byte aligned");
+    a.fresp = fresp;
+    a.err = err;
+    const size_t sm = 2 * (size_t)a.bufstride;
+    const int threads = kPB * (Z / kTI) * a.ntg;
+    const void *fn = Z == 50 ? (const void *)k_zth_apply<50> : (const void *)k_zth_apply<0>;
+    if (int rc = mm_set_smem(fn, sm)) return rc;
+    int per_sm = 0;
+    MM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, sm));
+    if (per_sm < 1) per_sm = 1;
+    const long long cap = (long long)mm_sm_count() * per_sm;
+    const unsigned grid = (unsigned)(a.ngroups < cap ? a.ngroups : cap);
+    void *args[] = {&S, &xmap, &wA, &wB, &a};
+    MM_CUDA_TRY(cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, sm, st));
+    mm_launch_counter_add();
+    return MM_OK;
+}

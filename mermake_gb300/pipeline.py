@@ -60,17 +60,25 @@ def _seen(dec, key, n):
 
 
 def hyb_spots(dec, image, flat_field=None, *, threshold=None, delta=1, delta_fit=0, sigmaZ=1, sigmaXY=1.5,
-              blur_radius=None, batch=0, capacity=None, stream=None, **kwargs):
+              blur_radius=None, batch=0, capacity=None, stream=None, ctx=None, tuned=True, **kwargs):
     """Rows ``[zc, xc, yc, bg, a, habs, hn, h]`` of one colour, in FOV coordinates
     (mermake/__main__.py:253-265).  ``dec`` is a ``Deconvolver``.  ``batch``:
     tiles per batch; 0 picks it (``tune.batch_for``), negative means all.
     ``capacity``: rows allocated for the output; None sizes it from the
     largest count this Deconvolver has returned for the shape (a call that
-    overflows is run again with the exact count)."""
+    overflows is run again with the exact count).  ``ctx``: a library context
+    to run on (default: the calling thread's).  ``tuned``: run the z form
+    ``tune.autotune`` chose for the geometry, if any."""
     _check_delta(delta)
     img = _u16_channel(image)
     if batch == 0:
         batch = tune.batch_for(dec, img.shape)
+    form = tune.zform_for(dec, img.shape) if tuned else _lib.MM_ZFORM_AUTO
+    if form != _lib.MM_ZFORM_AUTO and ctx is None:
+        with _lib.zform(form, img.device.index):
+            return hyb_spots(dec, img, flat_field, threshold=threshold, delta=delta, delta_fit=delta_fit,
+                             sigmaZ=sigmaZ, sigmaXY=sigmaXY, blur_radius=blur_radius, batch=batch,
+                             capacity=capacity, stream=stream, tuned=False)
     fl = _flat(flat_field, img.shape)
     Z, X, Y = img.shape
     L = _lib.lib()
@@ -81,7 +89,7 @@ def hyb_spots(dec, image, flat_field=None, *, threshold=None, delta=1, delta_fit
     for _ in range(2):
         out = torch.empty((cap, 8), dtype=torch.float32, device=img.device)
         n = C.c_uint32(0)
-        rc = L.mm_hyb_spots(_lib.ctx(img.device.index), _lib.ptr(img), Z, X, Y, img.stride(0), img.stride(1),
+        rc = L.mm_hyb_spots(ctx or _lib.ctx(img.device.index), _lib.ptr(img), Z, X, Y, img.stride(0), img.stride(1),
                             _lib.ptr(fl), fl.stride(0) if fl is not None else 0, _lib.ptr(dec.psf_fft),
                             dec.psf_fft.shape[0], _lib.ptr(dec.z_operator), dec.tile_size, dec.zpad, dec.overlap,
                             br, th, int(delta), int(delta_fit), float(sigmaZ), float(sigmaXY), max(int(batch), 0),
@@ -96,14 +104,20 @@ def hyb_spots(dec, image, flat_field=None, *, threshold=None, delta=1, delta_fit
 
 
 def dapi_spots(dec, image, flat_field=None, *, threshold=None, delta=1, delta_fit=0, sigmaZ=1, sigmaXY=1.5,
-               blur_radius=None, batch=0, buffer=None, capacity=None, stream=None, **kwargs):
+               blur_radius=None, batch=0, buffer=None, capacity=None, stream=None, ctx=None, tuned=True, **kwargs):
     """``(Xh_plus, Xh_minus, buffer, rms)`` of the DAPI block
     (mermake/__main__.py:215-225); ``buffer`` holds the stitched deconvolution
-    before normalisation.  ``batch`` as in ``hyb_spots``."""
+    before normalisation.  ``batch``, ``ctx`` and ``tuned`` as in ``hyb_spots``."""
     _check_delta(delta)
     img = _u16_channel(image)
     if batch == 0:
         batch = tune.batch_for(dec, img.shape, dapi=True)
+    form = tune.zform_for(dec, img.shape, dapi=True) if tuned else _lib.MM_ZFORM_AUTO
+    if form != _lib.MM_ZFORM_AUTO and ctx is None:
+        with _lib.zform(form, img.device.index):
+            return dapi_spots(dec, img, flat_field, threshold=threshold, delta=delta, delta_fit=delta_fit,
+                              sigmaZ=sigmaZ, sigmaXY=sigmaXY, blur_radius=blur_radius, batch=batch,
+                              buffer=buffer, capacity=capacity, stream=stream, tuned=False)
     fl = _flat(flat_field, img.shape)
     Z, X, Y = img.shape
     if buffer is None:
@@ -120,7 +134,7 @@ def dapi_spots(dec, image, flat_field=None, *, threshold=None, delta=1, delta_fi
         op = torch.empty((cp, 8), dtype=torch.float32, device=img.device)
         om = torch.empty((cm, 8), dtype=torch.float32, device=img.device)
         n_p, n_m, rms = C.c_uint32(0), C.c_uint32(0), C.c_float(0)
-        rc = L.mm_dapi_spots(_lib.ctx(img.device.index), _lib.ptr(img), Z, X, Y, img.stride(0), img.stride(1),
+        rc = L.mm_dapi_spots(ctx or _lib.ctx(img.device.index), _lib.ptr(img), Z, X, Y, img.stride(0), img.stride(1),
                              _lib.ptr(fl), fl.stride(0) if fl is not None else 0, _lib.ptr(dec.psf_fft),
                              dec.psf_fft.shape[0], _lib.ptr(dec.z_operator), dec.tile_size, dec.zpad,
                              dec.overlap, br, th, int(delta), int(delta_fit), float(sigmaZ), float(sigmaXY),
@@ -234,8 +248,9 @@ class FovGraph:
     Deconvolvers have seen (``hyb_spots``' rule).  One eager pass sizes the
     context's scratch before capture.  ``run`` replays and reads every count
     in one transfer; a FOV whose rows or candidates did not fit falls back to
-    the synchronous drivers (``fallbacks`` counts them).  Flat fields are fixed
-    at construction.
+    the synchronous drivers (``fallbacks`` counts them), after which the row
+    buffers and candidate lists are grown to that FOV's counts and the graph is
+    captured again (``recaptures``).  Flat fields are fixed at construction.
     """
 
     def __init__(self, dec_hyb, dec_dapi, shape, n_colours, hyb_args=None, dapi_args=None, flats=None,
@@ -262,21 +277,46 @@ class FovGraph:
         self.flats = [_flat(f, self.shape) for f in (flats if flats is not None else [None] * self.n)]
         self.dapi_flat = _flat(dapi_flat, self.shape)
         self.batch_h = max(int(tune.batch_for(dec_hyb, self.shape) if batch == 0 else batch), 0)
-        self.cap = _capacity(dec_hyb, ("hyb", Z, X, Y), 1 << 18)
-        self.rows = [torch.empty((self.cap, 8), dtype=torch.float32, device=dev) for _ in range(self.n)]
         # counts: [rows (+), rows (-), DAPI candidate overflow] + [rows, overflow] per colour
         self.counts = torch.zeros(3 + 2 * self.n, dtype=torch.int32, device=dev)
         self.rms = torch.zeros(1, dtype=torch.float32, device=dev)
         if dec_dapi is not None:
             self.batch_d = max(int(tune.batch_for(dec_dapi, self.shape, dapi=True) if batch == 0 else batch), 0)
-            self.cap_p = _capacity(dec_dapi, ("dapi+", Z, X, Y), 1 << 16)
-            self.cap_m = _capacity(dec_dapi, ("dapi-", Z, X, Y), 1 << 16)
-            self.plus = torch.empty((self.cap_p, 8), dtype=torch.float32, device=dev)
-            self.minus = torch.empty((self.cap_m, 8), dtype=torch.float32, device=dev)
             self.buffer = torch.empty(self.shape, dtype=torch.float32, device=dev)
         self._stream = torch.cuda.Stream(device=dev)
+        self.graph = None
+        self.recaptures = 0
+        self._capture()
+
+    def _alloc_rows(self):
+        """Row buffers from the largest counts the Deconvolvers have seen
+        (hyb_spots' rule)."""
+        Z, X, Y = self.shape
+        dev = torch.device("cuda", self.dev)
+        self.cap = _capacity(self.dec_hyb, ("hyb", Z, X, Y), 1 << 18)
+        self.rows = [torch.empty((self.cap, 8), dtype=torch.float32, device=dev) for _ in range(self.n)]
+        if self.dec_dapi is not None:
+            self.cap_p = _capacity(self.dec_dapi, ("dapi+", Z, X, Y), 1 << 16)
+            self.cap_m = _capacity(self.dec_dapi, ("dapi-", Z, X, Y), 1 << 16)
+            self.plus = torch.empty((self.cap_p, 8), dtype=torch.float32, device=dev)
+            self.minus = torch.empty((self.cap_m, 8), dtype=torch.float32, device=dev)
+
+    def _capture(self, grow=False):
+        """Row buffers, one eager pass (sizes the context's scratch and the
+        transform plans), then the capture.  grow: first run the synchronous
+        drivers on the graph's own context, which grow its candidate lists and
+        record the counts the row buffers are sized from."""
+        self.graph = None
         with torch.cuda.stream(self._stream):
-            self._issue()  # eager: sizes the context's scratch and the transform plans
+            if grow:
+                if self.dec_dapi is not None:
+                    dapi_spots(self.dec_dapi, self.dapi, self.dapi_flat, buffer=self.buffer, batch=self.batch_d,
+                               ctx=self._ctx, **self.dapi_args)
+                for c in range(self.n):
+                    hyb_spots(self.dec_hyb, self.colours[c], self.flats[c], batch=self.batch_h, ctx=self._ctx,
+                              **self.hyb_args)
+            self._alloc_rows()
+            self._issue()
         self._stream.synchronize()
         self.graph = torch.cuda.CUDAGraph()
         n0 = _lib.launch_count()
@@ -335,12 +375,18 @@ class FovGraph:
         self.replay()
         got = self.results()
         if got is None:
+            # a result did not fit: this FOV through the synchronous drivers,
+            # then the row buffers and candidate lists grown to its counts and
+            # the graph captured again, so that later FOVs like it replay
             self.fallbacks += 1
             plus = minus = None
             if self.dec_dapi is not None:
                 plus, minus, _, _ = dapi_spots(self.dec_dapi, self.dapi, self.dapi_flat, **self.dapi_args)
             got = (plus, minus, [hyb_spots(self.dec_hyb, self.colours[c], self.flats[c], **self.hyb_args)
                                  for c in range(self.n)])
+            torch.cuda.current_stream().synchronize()
+            self._capture(grow=True)
+            self.recaptures += 1
         plus, minus, xh = got
         return (plus.cpu().numpy() if plus is not None else None, minus.cpu().numpy() if minus is not None else None,
                 [r.cpu().numpy() for r in xh])

@@ -1,21 +1,25 @@
-"""Batch-size tuning for the per-FOV drivers (``pipeline.hyb_spots`` /
-``dapi_spots``, ``batch=0``).
+"""Tuning of the per-FOV drivers (``pipeline.hyb_spots`` / ``dapi_spots``):
+the tile batch size and the form of the z step, per geometry.
 
 A tile batch's working set is its spectrum (Z x P x (P/2+1) complex64) plus
-the float32 result and blur copies (2 x Z x P x P).  One batch of all tiles
+the float32 result and blur copy (2 x Z x P x P).  One batch of all tiles
 amortises the launches and, with one PSF, lets the z step run as a matrix
 product over the batch.  Measured on GB300, that beats batches small enough
 to stay in the L2 cache even where a tile is only 110 MB (Z 40, tiles of 300,
 100 PSFs: 170.5 ms per FOV for one batch against 183.7 ms for one tile at a
 time).  ``default_batch`` therefore takes all tiles, up to a scratch budget
-(``SCRATCH_BYTES``); ``autotune`` times candidate sizes on a real channel once
-per geometry and keeps the fastest on the Deconvolver, where the drivers find
-it.
+(``SCRATCH_BYTES``), and the library picks the z form (``MM_ZFORM_AUTO``).
 
-With several PSFs every batch size gives the same rows.  With one PSF, batches
-of fewer than 10 tiles use the padded-depth transforms instead of the z
-operator; the voxels then differ in the float32 rounding (about 1e-7
-relative), which can move a spot that sits on the threshold.
+``autotune`` times, on a real channel, every candidate batch size with every
+z form the geometry qualifies for (the matrix in registers, the matrix in
+shared memory, the direct sum per tile, the transforms over the padded depth;
+``mm_ctx_set_option(MM_OPT_ZFORM)``) and keeps the fastest pair on the
+Deconvolver, where the drivers find it (``settings_for``).
+
+With several PSFs every batch size gives the same rows.  The z forms, and
+with one PSF batches on either side of the matrix forms' 10 tiles, give the
+same voxels within float32 rounding (about 1e-7 relative), which can move a
+spot that sits on the threshold.
 """
 from __future__ import annotations
 
@@ -45,42 +49,66 @@ def default_batch(dec, shape):
 
 def batch_for(dec, shape, dapi=False):
     """The tuned batch of this geometry, else ``default_batch``."""
-    tuned = getattr(dec, "_tuned_batch", {}).get(_key(dec, shape, dapi))
-    return default_batch(dec, shape) if tuned is None else tuned
+    tuned = getattr(dec, "_tuned", {}).get(_key(dec, shape, dapi))
+    return default_batch(dec, shape) if tuned is None else tuned[0]
 
 
-def autotune(dec, image, flat_field=None, settings=None, dapi=False, candidates=None, reps=2):
+def zform_for(dec, shape, dapi=False):
+    """The tuned z form of this geometry (``_lib.MM_ZFORM_*``), else AUTO."""
+    from . import _lib
+    tuned = getattr(dec, "_tuned", {}).get(_key(dec, shape, dapi))
+    return _lib.MM_ZFORM_AUTO if tuned is None else tuned[1]
+
+
+def zforms(dec):
+    """The z forms worth timing for a Deconvolver: those of its z kernels when
+    it has them, and the transforms over the padded depth."""
+    from . import _lib
+    forms = [_lib.MM_ZFORM_TRANSFORMS]
+    if dec.z_operator is not None:
+        forms = [_lib.MM_ZFORM_DIRECT] + forms
+        if dec.psf_fft.shape[0] == 1:
+            forms = [_lib.MM_ZFORM_REGISTERS, _lib.MM_ZFORM_SHARED] + forms
+    return forms
+
+
+def autotune(dec, image, flat_field=None, settings=None, dapi=False, candidates=None, forms=None, reps=2):
     """Times ``hyb_spots`` (or ``dapi_spots`` with ``dapi=True``) on ``image``
-    for each candidate batch size (-1: all tiles) and keeps the fastest for
-    this geometry on ``dec``.  Returns ``{batch: ms}``; the chosen one is
-    ``batch_for(dec, image.shape, dapi)``."""
-    from . import pipeline
+    for every candidate batch size (-1: all tiles) with every z form, and keeps
+    the fastest pair for this geometry on ``dec``.  Returns
+    ``{(batch, form): ms}``; the choice is ``settings_for(dec, shape, dapi)``."""
+    from . import _lib, pipeline
     settings = dict(settings or {})
     settings.pop("batch", None)
     shape = tuple(int(v) for v in image.shape)
     nt = dec.n_tiles(shape)
     if candidates is None:
         candidates = sorted({c for c in (1, 4, 10, default_batch(dec, shape)) if 0 < c < nt} | {-1})
+    forms = zforms(dec) if forms is None else list(forms)
     times = {}
     buf = None
     for b in candidates:
-        def run():
-            nonlocal buf
-            if dapi:
-                out = pipeline.dapi_spots(dec, image, flat_field, batch=b, buffer=buf, **settings)
-                buf = out[2]
-            else:
-                pipeline.hyb_spots(dec, image, flat_field, batch=b, **settings)
-        run()  # warm-up (scratch sized for this batch)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            run()
-        torch.cuda.synchronize()
-        times[b] = 1e3 * (time.perf_counter() - t0) / reps
+        for f in forms:
+            def run():
+                nonlocal buf
+                with _lib.zform(f):
+                    if dapi:
+                        out = pipeline.dapi_spots(dec, image, flat_field, batch=b, buffer=buf, tuned=False, **settings)
+                        buf = out[2]
+                    else:
+                        pipeline.hyb_spots(dec, image, flat_field, batch=b, tuned=False, **settings)
+            run()  # warm-up (scratch sized for this batch)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                run()
+            torch.cuda.synchronize()
+            times[(b, f)] = 1e3 * (time.perf_counter() - t0) / reps
     best = min(times, key=times.get)
-    if not hasattr(dec, "_tuned_batch"):
-        dec._tuned_batch = {}
-    dec._tuned_batch[_key(dec, shape, dapi)] = best
+    dec.__dict__.setdefault("_tuned", {})[_key(dec, shape, dapi)] = best
     return times
 
+
+def settings_for(dec, shape, dapi=False):
+    """(batch, z form) the drivers use for this geometry."""
+    return batch_for(dec, shape, dapi), zform_for(dec, shape, dapi)

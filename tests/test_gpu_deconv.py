@@ -189,13 +189,16 @@ def test_apply_stitch_order_matches_reference(dc, npsf):
 
 
 @pytest.mark.parametrize("Z,zpad,ts,ov", [(13, 12, 10, 3), (64, 63, 10, 3), (50, 24, 30, 9), (7, 2, 15, 3),
-                                          (5, 9, 10, 3)])
+                                          (5, 9, 10, 3), (50, 49, 10, 3), (30, 14, 12, 4)])
 def test_z_operator_matches_padded_transforms(dc, Z, zpad, ts, ov):
-    """The z operator (one Z x Z matrix per frequency, summed from the z
-    kernel) against the FFT z pass over the padded depth, on whole batches: Z
-    not a multiple of the 10-plane chunks, a batch of 25 tiles split into two
-    tile chunks at Z = 64, an odd frequency plane (P = 21), and zpad > Z
-    (four padded planes copy one real plane)."""
+    """The z operator (one Z x Z matrix per frequency, from the z kernel)
+    against the FFT z pass over the padded depth, on whole batches: Z not a
+    multiple of the 10-plane chunks, a batch of 25 tiles split into two tile
+    chunks at Z = 64, an odd frequency plane (P = 21), and zpad > Z (four
+    padded planes copy one real plane) take the form with the matrix in shared
+    memory; Z a multiple of 5 with 1 <= zpad <= Z - 1 (the depths of both
+    benchmark blocks, zpad = Z - 1 and (Z - 1) / 2) the form with the matrix
+    in registers and TMA-staged operands (csrc/zop_tma.cu)."""
     rng = np.random.default_rng(Z)
     X = Y = 5 * ts
     img = rng.integers(100, 5000, (Z, X, Y)).astype(np.uint16)

@@ -198,21 +198,38 @@ def test_fov_runner_matches_direct_calls(mm):
     assert runner.h2d_bytes == 3 * Z * X * Y * 2
 
 
-def test_autotune_picks_a_batch_and_keeps_rows(mm):
-    """tune.autotune times candidate batch sizes on the channel, keeps the
-    fastest for the geometry, and hyb_spots(batch=0) then uses it with the
-    same rows (9 tiles: every candidate runs the padded-depth transforms)."""
-    from mermake_gb300 import tune
-    img, flat, psf = hyb_case(mm)
-    Z = img.shape[0]
+def test_autotune_picks_batch_and_z_form(mm):
+    """tune.autotune times every candidate batch size with every z form the
+    geometry qualifies for (25 tiles of one PSF, Z = 10: the matrix in
+    registers, the matrix in shared memory, the direct sum, the transforms over
+    the padded depth), keeps the fastest pair for the geometry, and
+    hyb_spots(batch=0) then runs it: its rows are those of the same pair set
+    explicitly, and every form's rows agree with the others' within float32
+    rounding of the voxels (the same spots but for near-ties)."""
+    from mermake_gb300 import _lib, tune
+    Z, X, Y = 10, 300, 300
+    img = mm["synth"].hyb_stack(Z, X, Y, 600, 9, gain=mm["synth"].flat_gain(X, Y))
+    flat = mm["synth"].flat_gain(X, Y)
+    psf = mm["synth"].gaussian_psf((9, 9, 9), 2.0, 1.3)
     dec = mm["dc"].Deconvolver(psf, img.shape, zpad=Z - 1, **HYB)
     dimg, dflat = img.cuda(), torch.from_numpy(flat).cuda()
-    times = tune.autotune(dec, dimg, dflat, HYB, candidates=(1, 4, -1), reps=1)
-    assert set(times) == {1, 4, -1} and all(t > 0 for t in times.values())
-    assert tune.batch_for(dec, img.shape) == min(times, key=times.get)
-    want = ck.sort_rows(mm["pl"].hyb_spots(dec, dimg, dflat, batch=-1, **HYB).cpu().numpy())
+    assert dec.n_tiles(img.shape) == 25
+    forms = tune.zforms(dec)
+    assert forms == [_lib.MM_ZFORM_REGISTERS, _lib.MM_ZFORM_SHARED, _lib.MM_ZFORM_DIRECT, _lib.MM_ZFORM_TRANSFORMS]
+    times = tune.autotune(dec, dimg, dflat, HYB, candidates=(4, -1), reps=1)
+    assert set(times) == {(b, f) for b in (4, -1) for f in forms} and all(t > 0 for t in times.values())
+    best = min(times, key=times.get)
+    assert tune.settings_for(dec, img.shape) == best
     got = ck.sort_rows(mm["pl"].hyb_spots(dec, dimg, dflat, **HYB).cpu().numpy())
+    with _lib.zform(best[1]):
+        want = ck.sort_rows(mm["pl"].hyb_spots(dec, dimg, dflat, batch=best[0], tuned=False, **HYB).cpu().numpy())
     np.testing.assert_array_equal(got, want)
+    ref = {tuple(np.round(r[:3], 2)) for r in want}
+    for f in forms:
+        with _lib.zform(f):
+            rows = mm["pl"].hyb_spots(dec, dimg, dflat, batch=-1, tuned=False, **HYB).cpu().numpy()
+        keys = {tuple(np.round(r[:3], 2)) for r in rows}
+        assert len(ref) > 50 and len(keys & ref) >= 0.99 * max(len(keys), len(ref)), f
 
 
 def test_fov_graph_replays_match_direct_calls(mm):
@@ -242,3 +259,33 @@ def test_fov_graph_replays_match_direct_calls(mm):
             for got, w in zip(rows, want):
                 np.testing.assert_array_equal(ck.sort_rows(got), ck.sort_rows(w.cpu().numpy()))
         assert g.fallbacks == 0
+
+
+def test_fov_graph_grows_and_recaptures_after_an_overflow(mm):
+    """A graph captured with row buffers too small for the FOV (8 rows) falls
+    back to the synchronous drivers once, grows its buffers to that FOV's
+    counts, captures again, and replays the next FOV without falling back; the
+    rows equal the direct calls' both times."""
+    Z, X, Y = 12, 170, 150
+    dapi = mm["synth"].dapi_stack(Z, X, Y, 5, n_nuclei=12, radii=(3.0, 12.0, 12.0))
+    img, flat, psf = hyb_case(mm, seed=1, Z=Z, X=X, Y=Y)
+    flats = [torch.from_numpy(flat).cuda()]
+    dh = mm["dc"].Deconvolver(psf, (Z, X, Y), zpad=Z - 1, **HYB)
+    dd = mm["dc"].Deconvolver(psf, (Z, X, Y), zpad=(Z - 1) // 2, **DAPI)
+    want_p, want_m, _, _ = mm["pl"].dapi_spots(dd, dapi.cuda(), None, **DAPI)
+    want = mm["pl"].hyb_spots(dh, img.cuda(), flats[0], **HYB).cpu().numpy()
+    real = mm["pl"]._capacity
+    mm["pl"]._capacity = lambda dec, key, default: 8
+    try:
+        g = mm["pl"].FovGraph(dh, dd, (Z, X, Y), 1, HYB, DAPI, flats=flats)
+    finally:
+        mm["pl"]._capacity = real
+    with g:
+        assert g.cap == 8
+        for k in range(2):
+            p, m, rows = g.run(dapi, [img])
+            np.testing.assert_array_equal(ck.sort_rows(p), ck.sort_rows(want_p.cpu().numpy()))
+            np.testing.assert_array_equal(ck.sort_rows(m), ck.sort_rows(want_m.cpu().numpy()))
+            np.testing.assert_array_equal(ck.sort_rows(rows[0]), ck.sort_rows(want))
+            assert (g.fallbacks, g.recaptures) == (1, 1)
+        assert g.cap >= len(want)

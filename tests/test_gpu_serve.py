@@ -99,3 +99,34 @@ def test_admission_respects_budget(mm):
         for f in futs:
             f.result(timeout=600)
         assert srv.max_in_flight == 1  # nothing fits beside a running request
+
+
+def test_device_memory_stays_within_budget(mm):
+    """Admission is checked against the memory actually held -- torch's
+    reserved memory (spectra, worker buffers, cached outputs) plus every
+    worker's library scratch -- plus the growth reserved for requests in
+    flight.  With room for the resident spectra and about one request, three
+    workers run the requests one or two at a time, idle workers give their
+    memory back when it is needed, the held total never exceeds the budget,
+    and the results equal those of an unconstrained server."""
+    reqs = requests(mm, n=6)
+    serve = mm["serve"]
+    psf = mm["synth"].gaussian_psf((9, 9, 9), 2.0, 1.3)
+    free, _ = run(mm, reqs, workers=1, budget=1e12, together=False)
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    torch.cuda.reset_peak_memory_stats()
+    base = torch.cuda.memory_reserved()
+    with serve.FovServer(psf, HYB, DAPI, hbm_budget=1e12, workers=3) as srv:
+        one = max(sum(srv._est(serve.FovRequest(**r))) for r in reqs)
+        spectra = sum(srv._spectra_bytes(s) for s in SHAPES.values())
+        srv.budget = base + spectra + 1.3 * one
+        futs = [srv.submit(serve.FovRequest(**r)) for r in reqs]
+        res = [f.result(timeout=600) for f in futs]
+        budget, peak = srv.budget, srv.peak_bytes
+    print("budget %.1f MB over the base, peak held %.1f MB, torch peak %.1f MB"
+          % ((budget - base) / 1e6, (peak - base) / 1e6, (torch.cuda.max_memory_reserved() - base) / 1e6))
+    assert peak <= budget
+    assert torch.cuda.max_memory_reserved() <= budget
+    for a, b in zip(free, res):
+        same(a, b)

@@ -121,9 +121,12 @@ def test_default_batch_takes_all_tiles_within_the_scratch_budget(monkeypatch):
     assert tune.default_batch(dec(40, 300, 89, 100), (40, 3000, 3000)) == 9     # 110 MB per tile
     assert tune.default_batch(dec(50, 500, 89, 25), (50, 2048, 2048)) == 3
     d = dec(40, 300, 89, 100)
-    d._tuned_batch = {((40, 3000, 3000), False): 4}
+    d._tuned = {((40, 3000, 3000), False): (4, 3)}
     assert tune.batch_for(d, (40, 3000, 3000)) == 4
+    assert tune.zform_for(d, (40, 3000, 3000)) == 3
+    assert tune.settings_for(d, (40, 3000, 3000)) == (4, 3)
     assert tune.batch_for(d, (40, 3000, 3000), dapi=True) == 9
+    assert tune.zform_for(d, (40, 3000, 3000), dapi=True) == 0  # MM_ZFORM_AUTO
 
 
 def test_spot_capacity_grows_from_counts_seen():
@@ -262,3 +265,58 @@ def test_zpass_flop_model_follows_the_z_pass_form():
     w = dict(Z=40, X=3000, Y=3000, colours=1)
     s = dict(dec_h=dec(40, 39, 478, 100, 100), dec_d=None)
     assert bench.zpass_flops(w, s) == 100 * 478 * 240 * 40 * 120 * 8.0
+
+
+def test_z_operator_register_rings_restate_the_matrix():
+    """The TMA z operator (csrc/zop_tma.cu) forms M[i][j] in registers from
+    three rings of five z-kernel values (the direct copy of plane j and its
+    reflections about zpad and zpad + Z - 1) and loads one value of each ring
+    per column.  Restated here with the kernel's slot arithmetic and staged
+    rows (k + kA for w[k mod Zp], kA = 2Z - 2 rounded up to a multiple of 4,
+    the rows past the padded depth zero as the TMA fills them), against M
+    built from the padding map; every read stays inside the staged rows."""
+    rng = np.random.default_rng(5)
+    for Z, zpad in [(50, 49), (50, 24), (30, 29), (40, 20), (10, 3), (15, 14), (20, 9)]:
+        Zp = Z + 2 * zpad
+        w = rng.standard_normal(Zp) + 1j * rng.standard_normal(Zp)
+        M = np.zeros((Z, Z), complex)
+        for z in range(Zp):
+            j = int(_map_z(z, Z, zpad, Zp))
+            if j >= 0:
+                for i in range(Z):
+                    M[i, j] += w[(zpad + i - z) % Zp]
+        kA = (2 * Z - 2 + 3) & ~3  # rows of box A: 2Z - 2 rounded up to a multiple of 4 (128-byte boxes)
+        kb, ko = kA, kA - (2 * Z - 2)
+        assert (kA * 4 * 8) % 128 == 0
+        staged = np.zeros(kA + 2 * Z - 1, complex)
+        for row in range(kA):  # box A: kernel rows Zp - kA .. Zp - 1 (negative rows read as zero)
+            src = Zp - kA + row
+            staged[row] = w[src] if 0 <= src < Zp else 0
+        for row in range(2 * Z - 1):  # box B: kernel rows 0 .. 2Z - 2 (rows >= Zp read as zero)
+            staged[kA + row] = w[row] if row < Zp else 0
+        n_staged = len(staged)
+
+        def at(i):
+            assert 0 <= i < n_staged, i  # every read stays inside the staged rows
+            return staged[i]
+
+        got = np.zeros((Z, Z), complex)
+        for i0 in range(0, Z, 5):
+            rT, rI, rO = [0j] * 5, [0j] * 5, [0j] * 5
+            for q in range(1, 5):
+                rT[q] = at(i0 + q + kb)
+            for q in range(4):
+                rI[q] = at(i0 + q + kb)
+                rO[q] = at(i0 + q + ko)
+            for j0 in range(0, Z, 5):
+                for u in range(5):
+                    j = j0 + u
+                    rT[(5 - u) % 5] = at(i0 - j + kb)
+                    rI[(u + 4) % 5] = at(i0 + j + 4 + kb)
+                    rO[(u + 4) % 5] = at(i0 + j + 4 + ko)
+                    vin = 1 <= j <= zpad
+                    vout = Z - 1 - zpad <= j <= Z - 2
+                    for q in range(5):
+                        m = rT[(q - u + 5) % 5] + (rI[(q + u) % 5] if vin else 0) + (rO[(q + u) % 5] if vout else 0)
+                        got[i0 + q, j] = m
+        np.testing.assert_allclose(got, M, rtol=0, atol=1e-12)
