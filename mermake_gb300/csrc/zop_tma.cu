@@ -17,10 +17,13 @@
 // operands, X (nt x Z x kPB) and the kernel rows w[-kA .. 2Z-2] (two TMA boxes
 // of the (Zp, plane) kernel, the negative rows from its top; kA is 2Z - 2
 // rounded up to a multiple of four, so that both boxes land on 128-byte
-// boundaries as tiled TMA requires), double buffered, each group's loads
-// completing on an mbarrier while the CTA works on the previous group.  The
-// persistent CTAs take groups of kPB consecutive frequencies.  Every wait is
-// bounded: a CTA that gives up records the failure in *err and returns.
+// boundaries as tiled TMA requires), double buffered.  The persistent CTAs
+// take groups of kPB consecutive frequencies.  A producer warp issues each
+// group's copies once the buffer is free; the compute warps wait only for
+// their buffer to fill (its "full" mbarrier completes with the copies' bytes)
+// and release it with one arrive per warp on its "empty" mbarrier, so no CTA
+// barrier separates the groups.  Every wait is bounded: a thread that gives up
+// records the failure in *err and returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -40,6 +43,9 @@ __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)_
 
 __device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
@@ -106,7 +112,7 @@ __global__ void __launch_bounds__(kThreadsMax, 2)
 k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap xmap,
             const __grid_constant__ CUtensorMap wmapA, const __grid_constant__ CUtensorMap wmapB, const ZthArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ __align__(8) uint64_t full[2], empty[2];
     const int Z = ZC > 0 ? ZC : a.Z;
     const int nig = Z / kTI;
     const int tid = threadIdx.x;
@@ -124,40 +130,45 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap xmap,
         if (tid == 0) atomicOr(a.err, 2u);
         return;
     }
+    const int lane = tid & 31, warp = tid >> 5;
+    const int ncw = (kPB * nig * a.ntg + 31) / 32;  // compute warps; warp ncw produces
     if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&full[b], 1);
+            mbar_init(&empty[b], ncw);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
 
-    auto issue = [&](int grp, int buf) {
-        unsigned char *b = smem + (size_t)buf * a.bufstride;
-        const int p0 = grp * kPB;
-        mbar_expect_tx(&bars[buf], a.xbytes + a.wbytesA + a.wbytesB);
-        tma_load_3d(b, &xmap, p0, 0, 0, &bars[buf]);
-        tma_load_2d(b + a.woff, &wmapA, p0, a.Zp - kb, &bars[buf]);
-        tma_load_2d(b + a.woff + a.wbytesA, &wmapB, p0, 0, &bars[buf]);
-    };
+    if (warp == ncw) {
+        // producer: the copies of group `it` go to buffer it & 1 once the
+        // compute warps have released its previous use (group it - 2)
+        if (lane != 0) return;
+        int it = 0;
+        for (int grp = blockIdx.x; grp < a.ngroups; grp += gridDim.x, ++it) {
+            const int buf = it & 1;
+            if (it >= 2 && !mbar_wait(&empty[buf], ((it - 2) >> 1) & 1)) {
+                atomicOr(a.err, 4u);
+                return;
+            }
+            // order the compute warps' reads of the buffer before the TMA writes
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            unsigned char *b = smem + (size_t)buf * a.bufstride;
+            const int p0 = grp * kPB;
+            mbar_expect_tx(&full[buf], a.xbytes + a.wbytesA + a.wbytesB);
+            tma_load_3d(b, &xmap, p0, 0, 0, &full[buf]);
+            tma_load_2d(b + a.woff, &wmapA, p0, a.Zp - kb, &full[buf]);
+            tma_load_2d(b + a.woff + a.wbytesA, &wmapB, p0, 0, &full[buf]);
+        }
+        return;
+    }
 
-    if (tid == 0 && blockIdx.x < a.ngroups) issue(blockIdx.x, 0);
     int it = 0;
     for (int grp = blockIdx.x; grp < a.ngroups; grp += gridDim.x, ++it) {
         const int buf = it & 1;
-        const int nxt = grp + gridDim.x;
-        if (tid == 0 && nxt < a.ngroups) {
-            // the other buffer was last read by the previous group (all threads
-            // passed the barrier at its end); order those reads before the TMA
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(nxt, buf ^ 1);
-        }
-        const bool ok = __syncthreads_and(mbar_wait(&bars[buf], (it >> 1) & 1));
-        if (!ok) {
-            if (tid == 0) {
-                atomicOr(a.err, 1u);
-                // let the other buffer's copies land before the CTA exits
-                if (nxt < a.ngroups) mbar_wait(&bars[buf ^ 1], ((it + 1) >> 1) & 1);
-            }
+        if (!mbar_wait(&full[buf], (it >> 1) & 1)) {
+            atomicOr(a.err, 1u);
             return;
         }
         const float2 *X = reinterpret_cast<const float2 *>(smem + (size_t)buf * a.bufstride);
@@ -206,6 +217,9 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap xmap,
                         for (int b = 0; b < kTT; ++b) acc[q][b] = cfma(m[q], x[b], acc[q][b]);
                 }
             }
+            // the operands are in registers: release the buffer before the stores
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[buf]);
             const long long pg = (long long)grp * kPB + p;
             if (pg < a.plane) {
                 const float f = a.fresp ? a.fresp[pg] : 1.f;
@@ -219,10 +233,11 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap xmap,
                     }
                 }
             }
+        } else {
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&empty[buf]);
         }
-        __syncthreads();  // every read of this buffer precedes the TMA that refills it
     }
-    // the last group's prefetch is never issued past ngroups, so nothing is in flight
 }
 
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
@@ -257,6 +272,10 @@ int make_map(CUtensorMap *m, const void *base, int rank, const cuuint64_t *dims,
     return MM_OK;
 }
 
+// the compute warps (threads kPB x Z/kTI x ntg, rounded up to whole warps)
+// and the producer warp
+int zth_threads(int Z, int ntg) { return ((kPB * (Z / kTI) * ntg + 31) / 32 + 1) * 32; }
+
 // staged row of w[0]: the rows -(2Z-2) .. -1 rounded up to a multiple of four,
 // so that the second kernel box starts on a 128-byte boundary
 int zth_ka(int Z) { return (2 * Z - 2 + 3) & ~3; }
@@ -279,7 +298,7 @@ int mm_zth_supported(int Z, int zpad, int nt, long long plane) {
     if (Z < kTI || Z % kTI != 0 || zpad < 1 || zpad > Z - 1 || nt < 1 || plane % 2 != 0) return 0;
     if (2 * Z - 1 > 256 || zth_ka(Z) > 256) return 0;  // TMA box height
     const int ntg = (nt + kTT - 1) / kTT;
-    if (kPB * (Z / kTI) * ntg > kThreadsMax) return 0;
+    if (zth_threads(Z, ntg) > kThreadsMax) return 0;
     return 2 * zth_bufstride(Z, nt, nullptr) <= 110 * 1024 && encode_fn() != nullptr;
 }
 
@@ -322,7 +341,7 @@ int mm_launch_zth_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, lon
     a.fresp = fresp;
     a.err = err;
     const size_t sm = 2 * (size_t)a.bufstride;
-    const int threads = kPB * (Z / kTI) * a.ntg;
+    const int threads = zth_threads(Z, a.ntg);
     const void *fn = Z == 50 ? (const void *)k_zth_apply<50> : (const void *)k_zth_apply<0>;
     if (int rc = mm_set_smem(fn, sm)) return rc;
     int per_sm = 0;
