@@ -73,6 +73,11 @@ WORKLOADS = {
                            delta_fit=3, sigmaZ=1, sigmaXY=1.5),
                   dapi_args=dict(tile_size=500, overlap=89, beta=0.01, threshold=3.0, blur_radius=50, delta=5,
                                  delta_fit=5, sigmaZ=1, sigmaXY=1.5)),
+    "fov80": dict(Z=80, X=2048, Y=2048, colours=3, puncta=40000, flat=True, dapi=True, nuclei=300,
+                  hyb=dict(tile_size=500, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
+                           delta_fit=3, sigmaZ=1, sigmaXY=1.5),
+                  dapi_args=dict(tile_size=500, overlap=89, beta=0.01, threshold=3.0, blur_radius=50, delta=5,
+                                 delta_fit=5, sigmaZ=1, sigmaXY=1.5)),
     "quad": dict(Z=50, X=1000, Y=1000, colours=1, puncta=10000, flat=True, dapi=False, nuclei=0,
                  hyb=dict(tile_size=500, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
                           delta_fit=3, sigmaZ=1, sigmaXY=1.5)),
@@ -107,7 +112,7 @@ def config_of(w, args, world):
             "channels": w["colours"] + (1 if w["dapi"] else 0), "tile_size": w["hyb"]["tile_size"],
             "overlap": w["hyb"]["overlap"], "fov_voxels": fov_voxels(w), "batch": args.batch,
             "l2": "inputs larger than L2 (%.2f GB per FOV vs 129 MB)" % (fov_voxels(w) * 2 / 1e9),
-            "parallelism": "replicas" if world > 1 else "single"}
+            "parallelism": "replicas" if world > 1 else "single", "zform": args.zform}
 
 
 def parse():
@@ -124,6 +129,9 @@ def parse():
     ap.add_argument("--form", default="batched", choices=["batched", "plain", "graph"])
     ap.add_argument("--batch", type=int, default=0,
                     help="batched form: tiles per batch (0: the tuned / L2-rule size, -1: all tiles)")
+    ap.add_argument("--zform", default="auto",
+                    choices=["auto", "registers", "shared", "direct", "transforms", "tensor"],
+                    help="z step form of every batch that qualifies for it (the library's MM_OPT_ZFORM)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-extra", action="store_true",
@@ -341,6 +349,9 @@ def gpu_arm(args, rank, world, local):
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     w = WORKLOADS[args.workload]
+    if args.zform != "auto":
+        _lib.zform(["auto", "registers", "shared", "direct", "transforms", "tensor"].index(args.zform),
+                   local).__enter__()
     pg = None
     if world > 1:
         import torch.distributed as dist

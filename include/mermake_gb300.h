@@ -89,11 +89,22 @@ enum { MM_BLUR_AUTO = 0, MM_BLUR_EXACT = 1, MM_BLUR_SPECTRAL = 2 };
  *   MM_ZFORM_SHARED: the same matrix summed into shared memory (one spectrum,
  *     Z <= 64, at most four copies of a plane);
  *   MM_ZFORM_DIRECT: the direct sum over the padded planes per tile;
- *   MM_ZFORM_TRANSFORMS: the reference's transforms over the padded depth.
+ *   MM_ZFORM_TRANSFORMS: the reference's transforms over the padded depth;
+ *   MM_ZFORM_TENSOR: the matrix of each frequency applied on the tensor
+ *     cores (tcgen05, TF32 operands split in two so that the products keep
+ *     float32 accuracy; one spectrum, Z <= 56, 1 <= zpad <= Z - 1, up to 32
+ *     tiles).
  * A form the batch does not qualify for falls back to AUTO's choice.  All
  * forms give the same voxels within float32 rounding; the choice is a
  * performance setting (tune.autotune picks it per geometry). */
-enum { MM_ZFORM_AUTO = 0, MM_ZFORM_REGISTERS = 1, MM_ZFORM_SHARED = 2, MM_ZFORM_DIRECT = 3, MM_ZFORM_TRANSFORMS = 4 };
+enum {
+    MM_ZFORM_AUTO = 0,
+    MM_ZFORM_REGISTERS = 1,
+    MM_ZFORM_SHARED = 2,
+    MM_ZFORM_DIRECT = 3,
+    MM_ZFORM_TRANSFORMS = 4,
+    MM_ZFORM_TENSOR = 5
+};
 int mm_ctx_set_option(mm_ctx *ctx, int option, int value);
 
 /* fill.reflect (mermake/fill.py:54-111, kernel `mirror` fill.py:6-52), in place.

@@ -17,7 +17,7 @@ from . import _build
 MM_OK, MM_EINVAL, MM_ENOMEM, MM_EOVERFLOW, MM_ETIMEOUT, MM_EDEVICE = range(6)
 MM_OPT_BLUR_MODE, MM_OPT_ZFORM = 1, 2
 MM_BLUR_AUTO, MM_BLUR_EXACT, MM_BLUR_SPECTRAL = range(3)
-MM_ZFORM_AUTO, MM_ZFORM_REGISTERS, MM_ZFORM_SHARED, MM_ZFORM_DIRECT, MM_ZFORM_TRANSFORMS = range(5)
+MM_ZFORM_AUTO, MM_ZFORM_REGISTERS, MM_ZFORM_SHARED, MM_ZFORM_DIRECT, MM_ZFORM_TRANSFORMS, MM_ZFORM_TENSOR = range(6)
 
 _lock = threading.Lock()
 _lib = None

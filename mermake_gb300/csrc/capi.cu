@@ -231,22 +231,32 @@ int fill_geom(TileGeom &g, int Z, int X, int Y, long long isz, long long isx, lo
 // MM_OPT_ZFORM choice when the batch qualifies for it (a z kernel, one
 // spectrum for the two matrix forms, the forms' shape limits), else the first
 // of those four that qualifies, the matrix forms only for batches of at least
-// MM_ZOP_MIN_TILES tiles.
+// MM_ZOP_MIN_TILES tiles.  A register-form batch split into tile chunks
+// (deeper tiles: each chunk reloads the z kernel and rounds its tiles up to
+// whole thread groups) gives way to the shared-memory form where that form
+// takes the depth.
 int zform_of(const mm_ctx *c, const TileGeom &g, const float2 *zop) {
     const long long plane = (long long)g.P * g.H;
-    auto ok = [&](int f, int min_tiles) {
+    // forced: the context's own choice, which takes any batch the form takes
+    auto ok = [&](int f, bool forced) {
+        const int min_tiles = forced ? 1 : MM_ZOP_MIN_TILES;
         switch (f) {
-            case MM_ZFORM_REGISTERS:
-                return zop && g.npsf == 1 && g.nt >= min_tiles && mm_zth_supported(g.Z, g.zpad, g.nt, plane) != 0;
+            case MM_ZFORM_REGISTERS: {
+                if (!zop || g.npsf != 1 || g.nt < min_tiles) return false;
+                const int chunks = mm_zth_supported(g.Z, g.zpad, g.nt, plane);
+                return chunks == 1 || (chunks > 1 && (forced || mm_zop_supported(g.Z, g.zpad) == 0));
+            }
             case MM_ZFORM_SHARED:
                 return zop && g.npsf == 1 && g.nt >= min_tiles && mm_zop_supported(g.Z, g.zpad) != 0;
+            case MM_ZFORM_TENSOR:
+                return zop && g.npsf == 1 && g.nt >= min_tiles && mm_zmma_supported(g.Z, g.zpad, g.nt, plane) != 0;
             case MM_ZFORM_DIRECT: return zop && mm_zconv_supported(g.Z, g.zpad) != 0;
             default: return true;
         }
     };
-    if (c->zform != MM_ZFORM_AUTO && ok(c->zform, 1)) return c->zform;
+    if (c->zform != MM_ZFORM_AUTO && ok(c->zform, true)) return c->zform;
     for (int f : {MM_ZFORM_REGISTERS, MM_ZFORM_SHARED, MM_ZFORM_DIRECT})
-        if (ok(f, MM_ZOP_MIN_TILES)) return f;
+        if (ok(f, false)) return f;
     return MM_ZFORM_TRANSFORMS;
 }
 
@@ -300,7 +310,13 @@ int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *
         if ((rc = mm_launch_cols(S, g.P, g.H, g.H, plane_c, g.nt * g.Z, false, st))) return rc;
     }
     const int zform = zform_of(c, g, zop);
-    if (zform == MM_ZFORM_REGISTERS) {
+    if (zform == MM_ZFORM_TENSOR) {
+        // the matrix applied on the tensor cores; the z kernel is read once per batch
+        Small *sm;
+        if ((rc = small_get(c, &sm, st))) return rc;
+        StageTimer t(c, ST_ZPASS, 2 * spec_b + 8.0 * wstride, st);
+        if ((rc = mm_launch_zmma_apply(S, zop, g.Z, g.zpad, g.Zp, plane_c, g.nt, fresp, &sm->err, st))) return rc;
+    } else if (zform == MM_ZFORM_REGISTERS) {
         // the matrix formed in registers, operands staged by TMA; the z kernel
         // is read once per batch
         Small *sm;
@@ -775,7 +791,7 @@ extern "C" int mm_ctx_set_option(mm_ctx *c, int option, int value) {
                    "unknown blur mode %d", value);
         c->blur_mode = value;
     } else {
-        MM_REQUIRE(value >= MM_ZFORM_AUTO && value <= MM_ZFORM_TRANSFORMS, "unknown z form %d", value);
+        MM_REQUIRE(value >= MM_ZFORM_AUTO && value <= MM_ZFORM_TENSOR, "unknown z form %d", value);
         c->zform = value;
     }
     return MM_OK;

@@ -144,8 +144,16 @@ int mm_launch_zconv(float2 *S, const float2 *w, long long wstride, int Z, int zp
 // The z operator with the matrix of each frequency formed in registers from
 // the z kernel (Toeplitz plus two masked Hankel parts, 1 <= zpad <= Z - 1,
 // Z a multiple of 5) and its operands staged by TMA (zop_tma.cu).  A CTA that
-// gives up waiting for its copies sets *err.
+// gives up waiting for its copies sets *err.  mm_zth_supported returns the
+// number of tile chunks a batch of nt tiles is split into (0: not supported).
 int mm_zth_supported(int Z, int zpad, int nt, long long plane);
+// The same z step on the tensor cores (zop_mma.cu): tcgen05 MMAs with the
+// matrix in tensor memory, TF32 operands split into two parts; Z <= 56,
+// 1 <= zpad <= Z - 1, nt <= 32, plane a multiple of 4.  A CTA that gives up
+// waiting sets *err.
+int mm_zmma_supported(int Z, int zpad, int nt, long long plane);
+int mm_launch_zmma_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, long long plane, int nt,
+                         const float *fresp, unsigned *err, cudaStream_t st);
 int mm_launch_zth_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, long long plane, int nt,
                         const float *fresp, unsigned *err, cudaStream_t st);
 // 1 - D(kx) D(ky) per half-spectrum frequency of a P x P plane, D the

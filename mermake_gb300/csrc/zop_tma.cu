@@ -91,13 +91,16 @@ __device__ __forceinline__ float2 cfma(float2 a, float2 b, float2 c) {
 }
 
 struct ZthArgs {
-    int Z, Zp, nt, ntg;
+    int Z, Zp, nt;
+    int ntc;           // tiles of a chunk (the X box's height)
+    int ntg;           // tile groups of kTT a CTA computes (ceil(ntc / kTT))
+    int nchunks;       // chunks the batch's tiles are split into
     long long plane;
-    int ngroups;       // ceil(plane / kPB)
+    int nitems;        // frequency groups (ceil(plane / kPB)) x chunks
     int jin_hi;        // the reflection about zpad copies planes 1 .. jin_hi (= zpad)
     int jout_lo;       // the reflection about zpad + Z - 1 copies planes jout_lo .. Z - 2
     int kA;            // staged row of w[0]: 2Z - 2 rounded up to a multiple of 4
-    unsigned xbytes;   // X box bytes (kPB x Z x nt float2)
+    unsigned xbytes;   // X box bytes (kPB x Z x ntc float2)
     unsigned wbytesA;  // kernel rows -kA .. -1 (kA x 32 bytes, a multiple of 128)
     unsigned wbytesB;  // kernel rows 0 .. 2Z-2
     unsigned bufstride, woff;  // bytes per buffer, offset of the kernel rows in it
@@ -105,21 +108,36 @@ struct ZthArgs {
     unsigned *err;
 };
 
+// Work item -> frequency group and the first tile of its chunk.  Chunk c
+// owns tiles [c * ntc, min((c + 1) * ntc, nt)); its box starts at
+// min(c * ntc, nt - ntc) so that every box lies inside the batch (the last
+// chunk's box may reach back into the previous chunk, whose tiles it computes
+// again but does not store).
+__device__ __forceinline__ void zth_item(const ZthArgs &a, int item, int &grp, int &own0, int &box0) {
+    grp = item / a.nchunks;
+    const int c = item - grp * a.nchunks;
+    own0 = c * a.ntc;
+    box0 = min(own0, a.nt - a.ntc);
+}
+
 // ZC > 0: Z known at compile time (50, the depth of every channel of the
-// benchmark FOV); otherwise any multiple of kTI.
-template <int ZC>
+// benchmark FOV); otherwise any multiple of kTI.  CH: the batch is split
+// into several tile chunks (otherwise item == frequency group, one box of
+// all nt tiles).
+template <int ZC, bool CH>
 __global__ void __launch_bounds__(kThreadsMax, 2)
 k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap xmap,
             const __grid_constant__ CUtensorMap wmapA, const __grid_constant__ CUtensorMap wmapB, const ZthArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t full[2], empty[2];
+    __shared__ int3 item_of[2];  // (group, first owned tile, box start) of each buffer's item
     const int Z = ZC > 0 ? ZC : a.Z;
     const int nig = Z / kTI;
     const int tid = threadIdx.x;
     const int p = tid % kPB;
     const int r = tid / kPB;
     const int ig = r % nig, tg = r / nig;
-    const int i0 = ig * kTI, t0 = tg * kTT;
+    const int i0 = ig * kTI, tl0 = tg * kTT;  // first row, first tile of the chunk's box
     const int kb = a.kA;              // row of w[0] in the staged kernel rows
     const int ko = kb - (2 * Z - 2);  // row of w[-(2Z-2)], the lowest index the rings read
 
@@ -142,11 +160,11 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap xmap,
     __syncthreads();
 
     if (warp == ncw) {
-        // producer: the copies of group `it` go to buffer it & 1 once the
-        // compute warps have released its previous use (group it - 2)
+        // producer: the copies of item `it` go to buffer it & 1 once the
+        // compute warps have released its previous use (item it - 2)
         if (lane != 0) return;
-        int it = 0;
-        for (int grp = blockIdx.x; grp < a.ngroups; grp += gridDim.x, ++it) {
+        int grp, own0, box0;
+        for (int item = blockIdx.x, it = 0; item < a.nitems; item += gridDim.x, ++it) {
             const int buf = it & 1;
             if (it >= 2 && !mbar_wait(&empty[buf], ((it - 2) >> 1) & 1)) {
                 atomicOr(a.err, 4u);
@@ -155,17 +173,18 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap xmap,
             // order the compute warps' reads of the buffer before the TMA writes
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             unsigned char *b = smem + (size_t)buf * a.bufstride;
+            zth_item(a, item, grp, own0, box0);
+            item_of[buf] = make_int3(grp, own0, box0);  // published by the arrive below
             const int p0 = grp * kPB;
             mbar_expect_tx(&full[buf], a.xbytes + a.wbytesA + a.wbytesB);
-            tma_load_3d(b, &xmap, p0, 0, 0, &full[buf]);
+            tma_load_3d(b, &xmap, p0, 0, box0, &full[buf]);
             tma_load_2d(b + a.woff, &wmapA, p0, a.Zp - kb, &full[buf]);
             tma_load_2d(b + a.woff + a.wbytesA, &wmapB, p0, 0, &full[buf]);
         }
         return;
     }
 
-    int it = 0;
-    for (int grp = blockIdx.x; grp < a.ngroups; grp += gridDim.x, ++it) {
+    for (int item = blockIdx.x, it = 0; item < a.nitems; item += gridDim.x, ++it) {
         const int buf = it & 1;
         if (!mbar_wait(&full[buf], (it >> 1) & 1)) {
             atomicOr(a.err, 1u);
@@ -191,7 +210,9 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap xmap,
                 rO[q] = W[(i0 + q + ko) * kPB + p];
             }
             rT[0] = rI[kTI - 1] = rO[kTI - 1] = make_float2(0.f, 0.f);
-            const float2 *xr = X + ((size_t)t0 * Z) * kPB + p;
+            // the box's tiles past ntc read stale buffer contents; their
+            // results are not stored
+            const float2 *xr = X + ((size_t)tl0 * Z) * kPB + p;
             for (int j0 = 0; j0 < Z; j0 += kTI) {
 #pragma unroll
                 for (int u = 0; u < kTI; ++u) {
@@ -218,15 +239,19 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap xmap,
                 }
             }
             // the operands are in registers: release the buffer before the stores
+            const int3 ii = CH ? item_of[buf] : make_int3(item, 0, 0);
+            const int own0 = ii.y, box0 = ii.z;
             __syncwarp();
             if (lane == 0) mbar_arrive(&empty[buf]);
-            const long long pg = (long long)grp * kPB + p;
+            const long long pg = (long long)ii.x * kPB + p;
             if (pg < a.plane) {
                 const float f = a.fresp ? a.fresp[pg] : 1.f;
+                // box0 + ntc >= t_end: the condition keeps t inside the box
+                const int t_end = CH ? min(own0 + a.ntc, a.nt) : a.nt;
 #pragma unroll
                 for (int b = 0; b < kTT; ++b) {
-                    const int t = t0 + b;
-                    if (t < a.nt) {
+                    const int t = CH ? box0 + tl0 + b : tl0 + b;
+                    if ((!CH || t >= own0) && t < t_end) {
 #pragma unroll
                         for (int q = 0; q < kTI; ++q)
                             S[((long long)t * Z + i0 + q) * a.plane + pg] = cscale(acc[q][b], f);
@@ -280,11 +305,10 @@ int zth_threads(int Z, int ntg) { return ((kPB * (Z / kTI) * ntg + 31) / 32 + 1)
 // so that the second kernel box starts on a 128-byte boundary
 int zth_ka(int Z) { return (2 * Z - 2 + 3) & ~3; }
 
-// bytes per buffer: X sized for whole tile groups (the last group's threads
-// read their tiles past nt, whose results are discarded), then the kernel rows
-// -kA .. 2Z - 2; both parts start on 128-byte boundaries
-size_t zth_bufstride(int Z, int nt, unsigned *woff) {
-    const int ntg = (nt + kTT - 1) / kTT;
+// bytes per buffer: X for ntg whole tile groups (the last group's threads
+// read tiles past the box, whose results are not stored), then the kernel
+// rows -kA .. 2Z - 2; both parts start on 128-byte boundaries
+size_t zth_bufstride(int Z, int ntg, unsigned *woff) {
     const size_t xb = (size_t)kPB * Z * ntg * kTT * sizeof(float2);
     const size_t wb = (size_t)kPB * (zth_ka(Z) + 2 * Z - 1) * sizeof(float2);
     const size_t xo = (xb + 127) & ~(size_t)127;
@@ -292,14 +316,33 @@ size_t zth_bufstride(int Z, int nt, unsigned *woff) {
     return (xo + wb + 127) & ~(size_t)127;
 }
 
+// shared memory of one CTA, two CTAs per SM
+constexpr size_t kSmemMax = 110 * 1024;
+
+// How a batch of nt tiles is split: the fewest chunks whose tile groups fit
+// one CTA (threads and shared memory), then the tiles spread evenly over them.
+struct ZthPlan {
+    int nchunks, ntc, ntg;
+};
+bool zth_plan(int Z, int nt, ZthPlan *pl) {
+    const int ntg_all = (nt + kTT - 1) / kTT;
+    int ntg_max = ntg_all;
+    while (ntg_max > 0 && (zth_threads(Z, ntg_max) > kThreadsMax || 2 * zth_bufstride(Z, ntg_max, nullptr) > kSmemMax))
+        --ntg_max;
+    if (ntg_max == 0) return false;
+    pl->nchunks = (ntg_all + ntg_max - 1) / ntg_max;
+    pl->ntc = (nt + pl->nchunks - 1) / pl->nchunks;
+    pl->ntg = (pl->ntc + kTT - 1) / kTT;
+    return true;
+}
+
 }  // namespace
 
 int mm_zth_supported(int Z, int zpad, int nt, long long plane) {
     if (Z < kTI || Z % kTI != 0 || zpad < 1 || zpad > Z - 1 || nt < 1 || plane % 2 != 0) return 0;
     if (2 * Z - 1 > 256 || zth_ka(Z) > 256) return 0;  // TMA box height
-    const int ntg = (nt + kTT - 1) / kTT;
-    if (zth_threads(Z, ntg) > kThreadsMax) return 0;
-    return 2 * zth_bufstride(Z, nt, nullptr) <= 110 * 1024 && encode_fn() != nullptr;
+    ZthPlan pl;
+    return zth_plan(Z, nt, &pl) && encode_fn() != nullptr ? pl.nchunks : 0;
 }
 
 int mm_launch_zth_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, long long plane, int nt,
@@ -307,12 +350,14 @@ int mm_launch_zth_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, lon
     MM_REQUIRE(Zp == Z + 2 * zpad && mm_zth_supported(Z, zpad, nt, plane),
                "z operator (TMA form) does not take Z %d, zpad %d, %d tiles", Z, zpad, nt);
     MM_REQUIRE(((uintptr_t)S & 15) == 0 && ((uintptr_t)w & 15) == 0, "spectra must be 16-byte aligned");
+    ZthPlan pl;
+    zth_plan(Z, nt, &pl);
     CUtensorMap xmap, wA, wB;
     const cuuint32_t kb = (cuuint32_t)(2 * Z - 2), kA = (cuuint32_t)zth_ka(Z);
     {
         cuuint64_t dims[3] = {(cuuint64_t)plane, (cuuint64_t)Z, (cuuint64_t)nt};
         cuuint64_t strides[2] = {(cuuint64_t)plane * 8, (cuuint64_t)plane * 8 * Z};
-        cuuint32_t box[3] = {kPB, (cuuint32_t)Z, (cuuint32_t)nt};
+        cuuint32_t box[3] = {kPB, (cuuint32_t)Z, (cuuint32_t)pl.ntc};
         if (int rc = make_map(&xmap, S, 3, dims, strides, box)) return rc;
     }
     {
@@ -326,29 +371,36 @@ int mm_launch_zth_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, lon
     a.Z = Z;
     a.Zp = Zp;
     a.nt = nt;
-    a.ntg = (nt + kTT - 1) / kTT;
+    a.ntc = pl.ntc;
+    a.ntg = pl.ntg;
+    a.nchunks = pl.nchunks;
     a.plane = plane;
-    a.ngroups = (int)((plane + kPB - 1) / kPB);
+    const long long nitems = ((plane + kPB - 1) / kPB) * pl.nchunks;
+    MM_REQUIRE(nitems < (1LL << 31), "z operator: too many frequency groups");
+    a.nitems = (int)nitems;
     a.jin_hi = zpad;
     a.jout_lo = Z - 1 - zpad;
     a.kA = (int)kA;
-    a.xbytes = (unsigned)(kPB * Z * nt * sizeof(float2));
+    a.xbytes = (unsigned)(kPB * Z * pl.ntc * sizeof(float2));
     a.wbytesA = (unsigned)(kPB * kA * sizeof(float2));
     a.wbytesB = (unsigned)(kPB * (kb + 1) * sizeof(float2));
-    a.bufstride = (unsigned)zth_bufstride(Z, nt, &a.woff);
+    a.bufstride = (unsigned)zth_bufstride(Z, pl.ntg, &a.woff);
     MM_REQUIRE(a.bufstride % 128 == 0 && a.woff % 128 == 0 && a.wbytesA % 128 == 0,
                "TMA destinations of the z operator must be 128-byte aligned");
+    MM_REQUIRE(a.xbytes <= a.woff, "z operator: the X box overruns its buffer");
     a.fresp = fresp;
     a.err = err;
     const size_t sm = 2 * (size_t)a.bufstride;
     const int threads = zth_threads(Z, a.ntg);
-    const void *fn = Z == 50 ? (const void *)k_zth_apply<50> : (const void *)k_zth_apply<0>;
+    const void *fn = pl.nchunks > 1 ? (const void *)k_zth_apply<0, true>
+                     : Z == 50     ? (const void *)k_zth_apply<50, false>
+                                   : (const void *)k_zth_apply<0, false>;
     if (int rc = mm_set_smem(fn, sm)) return rc;
     int per_sm = 0;
     MM_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, sm));
     if (per_sm < 1) per_sm = 1;
     const long long cap = (long long)mm_sm_count() * per_sm;
-    const unsigned grid = (unsigned)(a.ngroups < cap ? a.ngroups : cap);
+    const unsigned grid = (unsigned)(a.nitems < cap ? a.nitems : cap);
     void *args[] = {&S, &xmap, &wA, &wB, &a};
     MM_CUDA_TRY(cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, sm, st));
     mm_launch_counter_add();

@@ -189,7 +189,8 @@ def test_apply_stitch_order_matches_reference(dc, npsf):
 
 
 @pytest.mark.parametrize("Z,zpad,ts,ov", [(13, 12, 10, 3), (64, 63, 10, 3), (50, 24, 30, 9), (7, 2, 15, 3),
-                                          (5, 9, 10, 3), (50, 49, 10, 3), (30, 14, 12, 4)])
+                                          (5, 9, 10, 3), (50, 49, 10, 3), (30, 14, 12, 4), (80, 79, 10, 3),
+                                          (60, 29, 10, 3), (100, 99, 8, 2)])
 def test_z_operator_matches_padded_transforms(dc, Z, zpad, ts, ov):
     """The z operator (one Z x Z matrix per frequency, from the z kernel)
     against the FFT z pass over the padded depth, on whole batches: Z not a
@@ -198,7 +199,10 @@ def test_z_operator_matches_padded_transforms(dc, Z, zpad, ts, ov):
     padded planes copy one real plane) take the form with the matrix in shared
     memory; Z a multiple of 5 with 1 <= zpad <= Z - 1 (the depths of both
     benchmark blocks, zpad = Z - 1 and (Z - 1) / 2) the form with the matrix
-    in registers and TMA-staged operands (csrc/zop_tma.cu)."""
+    in registers and TMA-staged operands (csrc/zop_tma.cu), whose 25 tiles
+    are split into two chunks of 13 at Z = 80 and 100 (the second chunk's box
+    reaching back one tile into the first; at Z = 60 the shared-memory form
+    takes the batch instead)."""
     rng = np.random.default_rng(Z)
     X = Y = 5 * ts
     img = rng.integers(100, 5000, (Z, X, Y)).astype(np.uint16)
@@ -246,5 +250,39 @@ def test_z_convolution_matches_padded_transforms(dc, Z, zpad, ts, ov, npsf, nx):
     rb = torch.empty_like(ra)
     a._call(u16(img), dc.MM_DTYPE_U16, None, 0, nt, 6, res_out=ra)
     b._call(u16(img), dc.MM_DTYPE_U16, None, 0, nt, 6, res_out=rb)
+    err = float((ra - rb).abs().max() / rb.abs().max())
+    assert err < 2e-5, err
+
+
+@pytest.mark.parametrize("Z,zpad,ts,ov,nx", [(13, 12, 10, 3, 2), (50, 49, 10, 3, 5), (50, 24, 30, 9, 5),
+                                             (30, 29, 12, 4, 5), (56, 55, 8, 2, 4), (2, 1, 10, 3, 3),
+                                             (40, 7, 12, 4, 3)])
+def test_tensor_z_operator_matches_padded_transforms(dc, Z, zpad, ts, ov, nx):
+    """The z operator on the tensor cores (csrc/zop_mma.cu: tcgen05 MMAs of
+    the real form of each frequency's matrix, TF32 operands split into two
+    parts) against the FFT z pass over the padded depth: the benchmark
+    depths (Z = 50 with zpad 49 and 24, 25 tiles in one 32-wide MMA), the
+    largest depth the form takes (Z = 56, 16 tiles in a 16-wide MMA), a
+    single plane pair (Z = 2) and reflections that do not overlap (zpad 7 of
+    40)."""
+    from mermake_gb300 import _lib
+    rng = np.random.default_rng(100 + Z)
+    X = Y = nx * ts
+    img = rng.integers(100, 5000, (Z, X, Y)).astype(np.uint16)
+    psf = np.zeros((5, 5, 5), np.float32)
+    psf[2, 2, 2] = 1.0
+    psf[1:4, 1:4, 1:4] += 0.1 * rng.random((3, 3, 3)).astype(np.float32)
+    args = dict(tile_size=ts, zpad=zpad, overlap=ov, beta=0.01)
+    a = dc.Deconvolver(psf, img.shape, z_operator=True, **args)
+    b = dc.Deconvolver(psf, img.shape, z_operator=False, **args)
+    nt = a.n_tiles(img.shape)
+    assert nt == nx * nx
+    ra = torch.full((nt, Z, a.P, a.P), float("nan"), device="cuda")
+    rb = torch.empty_like(ra)
+    with _lib.zform(_lib.MM_ZFORM_TENSOR):
+        a._call(u16(img), dc.MM_DTYPE_U16, None, 0, nt, 6, res_out=ra)
+    b._call(u16(img), dc.MM_DTYPE_U16, None, 0, nt, 6, res_out=rb)
+    torch.cuda.synchronize()
+    assert bool(torch.isfinite(ra).all())
     err = float((ra - rb).abs().max() / rb.abs().max())
     assert err < 2e-5, err
