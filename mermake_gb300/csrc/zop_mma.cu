@@ -18,24 +18,36 @@
 //
 // Layout of a CTA (one per SM, persistent over groups of kPB = 4 consecutive
 // frequencies, whose values are 32 contiguous bytes of every spectrum row):
-//  - warps 0-7 form the operands and read the results.  Warp w owns TMEM
-//    lanes 32 (w % 4) .. + 31 and half w / 4 of the columns.  Row pair i (the
-//    rows (i, 0) and (i, 1)) sits in lanes 2s, 2s + 1 of quarter i / Pq,
-//    s = i % Pq, Pq = ceil(Z / 4); the two lanes of a pair compute half of the
-//    pair's M entries each and swap them with one shuffle per value.
-//    A (M, split) goes to TMEM with tcgen05.st; B (X, split) to shared memory
-//    in the K-major no-swizzle layout (8-row x 16-byte core matrices).  X of
-//    the next group is loaded into registers while the current group is
-//    formed.
-//  - warp 8 (one lane) stages the z kernel rows of each group by TMA.
-//  - warp 9 allocates the tensor memory; one lane issues the MMAs of each
-//    frequency and commits them to an mbarrier.
+//  - warps 0-11 form the operands and read the results, three per TMEM lane
+//    quarter (warp w owns lanes 32 (w % 4) .. + 31).  Row pair i (the rows
+//    (i, 0) and (i, 1)) sits in lanes 2s, 2s + 1 of quarter i / Pq, s = i % Pq,
+//    Pq = ceil(Z / 4).  A (M, split) goes to TMEM with tcgen05.st, its
+//    16-column chunks shared round robin by the quarter's warps; each entry
+//    is the sum of two reads of a per-frequency table of the z kernel, kept
+//    once as conj(w) for the (i, 0) rows and once as (Im w, Re w) for the
+//    (i, 1) rows, so that the sum is already the lane's pair of A values.  B
+//    (X, split) goes to shared memory in the K-major no-swizzle layout (8-row
+//    x 16-byte core matrices).  Results leave TMEM in pairs of frequencies
+//    (16 bytes per tile and row) into a [t][i][p] stage that one TMA store
+//    per group writes back in place.
+//  - warp 12 (one lane) stages the z kernel rows of each group and X of each
+//    pair of its frequencies by TMA.
+//  - warp 13 allocates the tensor memory; one lane issues the 3 x K/8 MMAs of
+//    each frequency and commits them to an mbarrier.
 // A and B are double buffered per frequency, so the MMAs of frequency f run
-// while the compute warps read the results of f - 1 and form f + 1.  Results
-// go through shared memory ([p][t][i], then [t][i][p] by a transpose) and
-// leave by one TMA store per group.  Every wait is bounded: a thread that
-// gives up records the failure in *err and the CTA winds down (the tensor
-// memory is freed after the MMAs it issued have completed).
+// while the compute warps read the results of f - 1 and form f + 1.  Every
+// wait is bounded: a thread that gives up records the failure in *err and
+// the CTA winds down (the tensor memory is freed after the MMAs it issued
+// have completed).
+//
+// Throughput: a tensor copy moves one box row per ~5.3 SM cycles whatever
+// its width from 16 to 64 bytes, and the batch spectrum's layout (frequency
+// innermost) makes every box row short (16 bytes of X per plane and tile for
+// a pair of frequencies, 32 bytes of output).  At 25 tiles of 678^2 and
+// Z = 50 the copies alone take ~3.85 of the 4.06 ms a launch takes, against
+// 3.3 ms for the register form (zop_tma.cu), which stays the default; this
+// form is selected by MM_ZFORM_TENSOR.
+
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -46,11 +58,12 @@
 namespace {
 
 constexpr int kPB = 4;          // frequencies per group
-constexpr int kCW = 8;          // compute warps
+constexpr int kCW = 12;         // compute warps: three per TMEM lane quarter
 constexpr int kThreads = (kCW + 2) * 32;
 constexpr int kTmemCols = 512;
 constexpr unsigned kWaitPolls = 1u << 24;
-constexpr int kXItems = 3;      // (tile, plane pair) items of X per compute thread
+constexpr int kXItems = 2;      // (tile, plane pair) items of X per compute thread
+constexpr int kZeroRows = 64;   // zero rows after each table (a row index i + offset, i < 64)
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -87,6 +100,14 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, i
         "l"(map), "r"(c0), "r"(c1), "r"(smem_u32(bar))
         : "memory");
 }
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1, int c2,
+                                            uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
+        : "memory");
+}
 __device__ __forceinline__ void tma_store_3d(const CUtensorMap *map, const void *src, int c0, int c1, int c2) {
     asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%2, %3, %4}], [%1];" ::"l"(map),
                  "r"(smem_u32(src)), "r"(c0), "r"(c1), "r"(c2)
@@ -118,19 +139,19 @@ __device__ __forceinline__ void tc_commit(uint64_t *bar) {
                  : "memory");
 }
 
-// 16 consecutive 32-bit columns of this thread's lane
+// 16 consecutive 32-bit columns of this thread's lane.  No memory clobber:
+// the stores read only registers, and tcgen05.wait::st (volatile, with a
+// clobber) orders them before anything that reads the tensor memory.
 __device__ __forceinline__ void tc_st16(unsigned taddr, const float *v) {
     asm volatile(
         "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
         "%15, %16};" ::"r"(taddr),
         "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]), "f"(v[8]),
-        "f"(v[9]), "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15])
-        : "memory");
+        "f"(v[9]), "f"(v[10]), "f"(v[11]), "f"(v[12]), "f"(v[13]), "f"(v[14]), "f"(v[15]));
 }
 __device__ __forceinline__ void tc_st8(unsigned taddr, const float *v) {
     asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
-                 "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
-                 : "memory");
+                 "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7]));
 }
 __device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void tc_ld16(unsigned taddr, float *v) {
@@ -173,27 +194,50 @@ struct ZmmaArgs {
     int K;            // 2Z rounded up to a multiple of 8 (MMA K steps of 8)
     int Pq;           // row pairs per TMEM lane quarter
     int wrows;        // staged kernel rows: kA + 2Z - 1
-    unsigned wbytesA, wbytesB;
+    unsigned wbytesA, wbytesB, xbytes;  // TMA boxes: kernel rows (two), X of two frequencies
     // shared-memory offsets (bytes)
-    unsigned o_w, o_wt, o_b, o_i, o_o;
-    unsigned wstride, wtstride, bstride, bhalf, sbo;
+    int trows;        // rows of a table: kernel rows, hB (2Z - 1), kZeroRows zeros
+    unsigned o_w, o_x, o_wt, o_z, o_b, o_o;
+    unsigned wstride, xstride, wtstride, bstride, bhalf, sbo;
     const float *fresp;
     unsigned *err;
 };
 
-// N: MMA width (16 or 32 tiles)
-template <int N>
+// Geometry of depth Z (compile-time where Z is): K (2Z rounded up to 8),
+// the staged row kb of w[0], and the table rows of the column positions j:
+// the T value w[i - j] at row i + zm_toff(j), the H value (hB[i + j],
+// w[i + j], w[i + j - 2Z + 2] or none, by the planes the reflections copy) at
+// row i + zm_hoff(j); padding positions (j >= Z) and "none" read zero rows.
+__host__ __device__ constexpr int zm_K(int Z) { return (2 * Z + 7) & ~7; }
+__host__ __device__ constexpr int zm_kb(int Z) { return (2 * Z - 2 + 3) & ~3; }
+__host__ __device__ constexpr int zm_wrows(int Z) { return zm_kb(Z) + 2 * Z - 1; }
+__host__ __device__ constexpr int zm_zb(int Z) { return zm_wrows(Z) + 2 * Z - 1; }
+__host__ __device__ constexpr int zm_toff(int Z, int j) { return j < Z ? zm_kb(Z) - j : zm_zb(Z); }
+__host__ __device__ constexpr int zm_hoff(int Z, int zpad, int j) {
+    return j >= Z ? zm_zb(Z)
+                  : (j >= 1 && j <= zpad) ? ((j >= Z - 1 - zpad && j <= Z - 2) ? zm_wrows(Z) + j : zm_kb(Z) + j)
+                  : (j >= Z - 1 - zpad && j <= Z - 2) ? zm_kb(Z) - (2 * Z - 2) + j
+                                                      : zm_zb(Z);
+}
+
+// N: MMA width (16 or 32 tiles).  ZC > 0: depth and zpad (ZPC) known at
+// compile time (the benchmark FOV's hyb and DAPI blocks), so that the table
+// offsets of every column position fold into the loads.
+template <int N, int ZC, int ZPC>
 __global__ void __launch_bounds__(kThreads, 1)
-k_zmma_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA,
-             const __grid_constant__ CUtensorMap wmapB, const __grid_constant__ CUtensorMap omap, const ZmmaArgs a) {
+k_zmma_apply(const __grid_constant__ CUtensorMap wmapA, const __grid_constant__ CUtensorMap wmapB,
+             const __grid_constant__ CUtensorMap xmap, const __grid_constant__ CUtensorMap omap, const ZmmaArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t wfull[2], wempty[2], bfull[2], mdone[2], cbar;
+    __shared__ __align__(8) uint64_t wfull[2], wempty[2], xfull[2], xempty[2], bfull[2], mdone[2], cbar;
     __shared__ unsigned tmem_base_sh;
     __shared__ int give_up;
+    __shared__ int2 colt[64];  // per column position j: table rows of its T and H values, minus the row i
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int Z = a.Z, K = a.K, Pq = a.Pq;
-    const int kb = a.kA, ko = kb - (2 * Z - 2);
-    const int hb = a.wrows;  // staged row of hB[0] (after the kernel rows)
+    constexpr bool CT = ZC > 0;
+    const int Z = CT ? ZC : a.Z, K = CT ? zm_K(ZC) : a.K, Pq = CT ? (ZC + 3) / 4 : a.Pq;
+    const int kb = CT ? zm_kb(ZC) : a.kA, ko = kb - (2 * Z - 2);
+    const int hb = CT ? zm_wrows(ZC) : a.wrows;  // table row of hB[0] (after the kernel rows)
+    const int zb = hb + 2 * Z - 1;               // first zero row of a table
 
     if (tid == 0) {
         give_up = 0;
@@ -202,6 +246,8 @@ k_zmma_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA,
             mbar_init(&wempty[b], kCW * 32);
             mbar_init(&bfull[b], kCW * 32);
             mbar_init(&mdone[b], 1);
+            mbar_init(&xfull[b], 1);
+            mbar_init(&xempty[b], kCW * 32);
         }
         mbar_init(&cbar, kCW * 32);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -209,6 +255,25 @@ k_zmma_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA,
             atomicOr(a.err, 2u);
             give_up = 1;
         }
+    }
+    if (tid < a.K / 2) {
+        // T value w[i - j], H value (by the planes the reflections copy):
+        // hB[i + j], w[i + j], w[i + j - 2Z + 2] or none; padding positions
+        // (j >= Z) and "none" read the zero rows
+        const int j = tid;
+        const bool vin = j >= 1 && j <= a.jin_hi, vout = j >= a.jout_lo && j <= Z - 2;
+        const int off = vin ? (vout ? hb : kb) : (vout ? ko : zb);
+        colt[j] = j < Z ? make_int2(kb - j, off == zb ? zb : off + j) : make_int2(zb, zb);
+    }
+    {
+        // the zero rows of every table (never rewritten), and the zero table of
+        // the lanes without a row
+        float2 *t0 = reinterpret_cast<float2 *>(smem + a.o_wt);
+        const int ntab = 2 * 2 * kPB;  // buffers x row types x frequencies
+        for (int e = tid; e < ntab * kZeroRows; e += kThreads)
+            t0[(e / kZeroRows) * (a.wtstride / 8) + zb + e % kZeroRows] = make_float2(0.f, 0.f);
+        float2 *z0 = reinterpret_cast<float2 *>(smem + a.o_z);
+        for (int e = tid; e < a.trows; e += kThreads) z0[e] = make_float2(0.f, 0.f);
     }
     if (warp == kCW + 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
@@ -226,7 +291,8 @@ k_zmma_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA,
     const int nfreq = nitems * kPB;
 
     if (warp == kCW) {
-        // ---- producer: the z kernel rows of each group ----
+        // ---- producer: the z kernel rows of each group and X of each pair
+        // of its frequencies, by TMA ----
         if (lane == 0) {
             int it = 0;
             for (; it < nitems; ++it) {
@@ -241,10 +307,30 @@ k_zmma_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA,
                 mbar_expect_tx(&wfull[buf], a.wbytesA + a.wbytesB);
                 tma_load_2d(w, &wmapA, p0, a.Zp - kb, &wfull[buf]);
                 tma_load_2d(w + a.wbytesA, &wmapB, p0, 0, &wfull[buf]);
+                // X of frequencies 2x, 2x + 1 of the group into buffer x, once
+                // the previous group's pair has been read
+                bool stop = false;
+                for (int x = 0; x < 2; ++x) {
+                    if (it >= 1 && !mbar_wait(&xempty[x], (it - 1) & 1)) {
+                        atomicOr(a.err, 4u);
+                        stop = true;
+                        break;
+                    }
+                    fence_async_smem();
+                    mbar_expect_tx(&xfull[x], a.xbytes);
+                    tma_load_3d(smem + a.o_x + x * a.xstride, &xmap, p0 + 2 * x, 0, 0, &xfull[x]);
+                }
+                if (stop) {
+                    ++it;  // this group's copies were (partly) issued
+                    break;
+                }
             }
             // no copy may still be landing when the CTA exits
             for (int j = it - 2 < 0 ? 0 : it - 2; j < it; ++j)
                 if (!mbar_wait(&wfull[j & 1], (j >> 1) & 1)) atomicOr(a.err, 4u);
+            if (it >= 1)
+                for (int x = 0; x < 2; ++x)
+                    if (!mbar_wait(&xfull[x], (it - 1) & 1)) atomicOr(a.err, 4u);
         }
     } else if (warp == kCW + 1) {
         // ---- MMA issue ----
@@ -276,7 +362,7 @@ k_zmma_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA,
         }
     } else {
         // ---- compute warps ----
-        const int q = warp & 3, h = warp >> 2;
+        const int q = warp & 3, h = warp >> 2;  // h: 0..2 within the quarter
         const int s_pair = lane >> 1, c = lane & 1;
         const int i = q * Pq + s_pair;  // row pair of this lane
         const bool row_ok = s_pair < Pq && i < Z;
@@ -285,120 +371,90 @@ k_zmma_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA,
         const int nx = a.nt * (K / 4);  // X items (tile, plane pair) per frequency
 
         // X item e = tid + 256 r: tile n = e % nt, planes z = 2 (e / nt) and
-        // z + 1, all kPB frequencies (2 x 32 bytes); its B core-matrix row
-        // (n, kq = z / 2) holds (Xr[z], Xi[z], Xr[z+1], Xi[z+1])
-        int xrow[kXItems], bofs[kXItems], xn[kXItems];
+        // z + 1; its B core-matrix row (n, kq = z / 2) holds
+        // (Xr[z], Xi[z], Xr[z+1], Xi[z+1]).  The staged X of two frequencies
+        // is [t][z][2] complex.
+        int xoff[kXItems], bofs[kXItems], xn[kXItems];
 #pragma unroll
         for (int r = 0; r < kXItems; ++r) {
             const int e = tid + r * kCW * 32;
             const int n = e % a.nt, kq = e / a.nt;
-            xrow[r] = e < nx ? n * Z + 2 * kq : -1;
-            xn[r] = e < nx ? (2 * kq + 1 < Z ? 2 : (2 * kq < Z ? 1 : 0)) : 0;  // planes present
+            xoff[r] = (n * Z + 2 * kq) * 2;
+            xn[r] = e < nx ? (2 * kq + 1 < Z ? 2 : (2 * kq < Z ? 1 : 0)) : -1;  // planes present, -1: no item
             bofs[r] = (n >> 3) * (int)a.sbo + kq * 128 + (n & 7) * 16;
         }
-        // the group's X rows into L2 ahead of their use
-        auto prefetch_x = [&](int it) {
-            const long long p0 = ((long long)blockIdx.x + (long long)it * gridDim.x) * kPB;
-#pragma unroll
-            for (int r = 0; r < kXItems; ++r) {
-                if (xn[r] >= 1)
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(S + (long long)xrow[r] * a.plane + p0));
-                if (xn[r] >= 2)
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(S + ((long long)xrow[r] + 1) * a.plane + p0));
-            }
-        };
-        // X of frequency pg of this thread's items (planes z, z + 1); the
-        // first frequency of a group brings the 32-byte rows into L1
-        auto load_x = [&](float2 (&x)[kXItems][2], long long pg) {
-#pragma unroll
-            for (int r = 0; r < kXItems; ++r) {
-                x[r][0] = xn[r] >= 1 ? __ldg(S + (long long)xrow[r] * a.plane + pg) : make_float2(0.f, 0.f);
-                x[r][1] = xn[r] >= 2 ? __ldg(S + ((long long)xrow[r] + 1) * a.plane + pg) : make_float2(0.f, 0.f);
-            }
-        };
 
-        // B of one frequency, split
-        auto form_b = [&](const float2 (&x)[kXItems][2], int slot) {
+        // B of frequency fp of the group, split, from the staged X
+        // ([t][z][2] complex: the pair of frequencies of its buffer)
+        auto form_b = [&](int fp, int slot) {
+            const float2 *xs = reinterpret_cast<const float2 *>(smem + a.o_x + (fp >> 1) * a.xstride) + (fp & 1);
             unsigned char *bh = smem + a.o_b + slot * a.bstride, *bl = bh + a.bhalf;
 #pragma unroll
             for (int r = 0; r < kXItems; ++r) {
-                if (xrow[r] >= 0) {
+                if (xn[r] >= 0) {
+                    const float2 x0 = xn[r] >= 1 ? xs[xoff[r]] : make_float2(0.f, 0.f);
+                    const float2 x1 = xn[r] >= 2 ? xs[xoff[r] + 2] : make_float2(0.f, 0.f);
                     float4 hi, lo;
-                    split_tf32(x[r][0].x, hi.x, lo.x);
-                    split_tf32(x[r][0].y, hi.y, lo.y);
-                    split_tf32(x[r][1].x, hi.z, lo.z);
-                    split_tf32(x[r][1].y, hi.w, lo.w);
+                    split_tf32(x0.x, hi.x, lo.x);
+                    split_tf32(x0.y, hi.y, lo.y);
+                    split_tf32(x1.x, hi.z, lo.z);
+                    split_tf32(x1.y, hi.w, lo.w);
                     *reinterpret_cast<float4 *>(bh + bofs[r]) = hi;
                     *reinterpret_cast<float4 *>(bl + bofs[r]) = lo;
                 }
             }
         };
 
-        // A of one frequency: this lane's row, column chunks h, h + 2, ...,
-        // from the transposed kernel rows wt (kernel value w[s] at
-        // wt[s + kb], the combined reflection hB[s] = w[s] + w[s - 2Z + 2] at
-        // wt[s + hb])
-        auto form_a = [&](const float2 *wt, int slot) {
-            for (int ch = h; ch < nchunk; ch += 2) {
-                const bool full16 = K - 16 * ch >= 16;
-                // this lane computes positions jp0 + u (u < 4) of the chunk
-                const int jp0 = 8 * ch + (full16 ? 4 * c : 0);
-                float2 m[4];
+        // A of one frequency: this lane's row, column chunks h, h + 2, ...
+        // tb: the frequency's table for this lane's row type, offset by its
+        // row i (the zero table for lanes without a row).  Row (i, 0) reads
+        // conj(w), row (i, 1) reads (Im w, Re w), so that each entry of the
+        // sum is already the lane's pair of A values: (Mr, -Mi) or (Mi, Mr).
+        auto form_chunk = [&](int ch, const float2 *tb, int slot) {
+            float hi[16], lo[16];
+            const bool full16 = K - 16 * ch >= 16;
 #pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const int j = jp0 + u;
-                    float2 v = make_float2(0.f, 0.f);
-                    if (row_ok && j < Z) {
-                        const bool vin = (unsigned)(j - 1) < (unsigned)a.jin_hi;
-                        const bool vout = j >= a.jout_lo && j <= Z - 2;
-                        const int off = vin ? (vout ? hb : kb) : (vout ? ko : hb);
-                        const float sc = (vin || vout) ? 1.f : 0.f;
-                        const float2 t = wt[i - j + kb], hk = wt[i + j + off];
-                        v = make_float2(fmaf(sc, hk.x, t.x), fmaf(sc, hk.y, t.y));
+            for (int u = 0; u < 8; ++u) {
+                if (u < 4 || full16) {
+                    const int j = 8 * ch + u;
+                    int to, ho;
+                    if constexpr (CT) {
+                        to = zm_toff(ZC, j);
+                        ho = zm_hoff(ZC, ZPC, j);
+                    } else {
+                        const int2 cj = colt[j];
+                        to = cj.x;
+                        ho = cj.y;
                     }
-                    m[u] = v;
+                    const float2 t = tb[to], hk = tb[ho];
+                    split_tf32(t.x + hk.x, hi[2 * u], lo[2 * u]);
+                    split_tf32(t.y + hk.y, hi[2 * u + 1], lo[2 * u + 1]);
                 }
-                float2 mm[8];
-                if (full16) {
-                    // swap with the pair partner: lane c = 0 computed positions
-                    // 0..3 of the chunk, c = 1 positions 4..7
+            }
+            const unsigned ta = tmem + lane_base + colA + slot * 2 * K + 16 * ch;
+            if (full16) {
+                tc_st16(ta, hi);
+                tc_st16(ta + K, lo);
+            } else {
+                tc_st8(ta, hi);
+                tc_st8(ta + K, lo);
+            }
+        };
+        auto form_a = [&](const float2 *tb, int slot) {
+            if constexpr (CT) {
+                constexpr int nch = (zm_K(ZC) + 15) / 16;
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const float ox = __shfl_xor_sync(0xffffffffu, m[u].x, 1);
-                        const float oy = __shfl_xor_sync(0xffffffffu, m[u].y, 1);
-                        mm[u] = c ? make_float2(ox, oy) : m[u];
-                        mm[u + 4] = c ? m[u] : make_float2(ox, oy);
-                    }
-                } else {
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        mm[u] = m[u];
-                        mm[u + 4] = make_float2(0.f, 0.f);
-                    }
-                }
-                float hi[16], lo[16];
-#pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    // row (i, 0): (Mr, -Mi); row (i, 1): (Mi, Mr)
-                    const float e0 = c ? mm[u].y : mm[u].x;
-                    const float e1 = c ? mm[u].x : -mm[u].y;
-                    split_tf32(e0, hi[2 * u], lo[2 * u]);
-                    split_tf32(e1, hi[2 * u + 1], lo[2 * u + 1]);
-                }
-                const unsigned ta = tmem + lane_base + colA + slot * 2 * K + 16 * ch;
-                if (full16) {
-                    tc_st16(ta, hi);
-                    tc_st16(ta + K, lo);
-                } else {
-                    tc_st8(ta, hi);
-                    tc_st8(ta + K, lo);
-                }
+                for (int ch = 0; ch < nch; ++ch)
+                    if (ch % (kCW / 4) == h) form_chunk(ch, tb, slot);
+            } else {
+                for (int ch = h; ch < nchunk; ch += kCW / 4) form_chunk(ch, tb, slot);
             }
         };
 
-        // results of frequency fp of a group (slot), scaled by the blur
-        // response, into the [p][t][i] buffer
-        auto epilogue = [&](int fp, int slot, long long pg) {
+        // results of one frequency (slot), scaled by its blur response: this
+        // lane's (Yr, Yi) of tiles (N / 2) h + 2 m2 + c, m2 < N / 4 (warps
+        // h = 0, 1 of each quarter)
+        auto read_results = [&](int slot, long long pg, float2 (&y)[8]) {
             const float fr = a.fresp ? __ldg(a.fresp + pg) : 1.f;
             float v[16];
             const unsigned td = tmem + lane_base + colD + slot * N + (N / 2) * h;
@@ -407,15 +463,24 @@ k_zmma_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA,
             else
                 tc_ld8(td, v);
             tc_wait_ld();
-            float2 *ib = reinterpret_cast<float2 *>(smem + a.o_i) + (size_t)fp * a.nt * Z;
 #pragma unroll
             for (int m2 = 0; m2 < N / 4; ++m2) {
-                // tiles u = 2 m2 (lane c = 0) and 2 m2 + 1 (lane c = 1)
+                // lane c = 0 holds Yr and takes tile 2 m2, lane c = 1 holds Yi
+                // and takes tile 2 m2 + 1
                 const float give = c ? v[2 * m2] : v[2 * m2 + 1];
                 const float got = __shfl_xor_sync(0xffffffffu, give, 1);
-                const float yr = c ? got : v[2 * m2], yi = c ? v[2 * m2 + 1] : got;
+                y[m2] = make_float2((c ? got : v[2 * m2]) * fr, (c ? v[2 * m2 + 1] : got) * fr);
+            }
+        };
+        // two frequencies' results (p0, p0 + 1 of the group) into the
+        // [t][i][p] stage, 16 bytes per tile and row
+        auto write_results = [&](const float2 (&y0)[8], const float2 (&y1)[8], int p0) {
+            float4 *ob = reinterpret_cast<float4 *>(smem + a.o_o);
+#pragma unroll
+            for (int m2 = 0; m2 < N / 4; ++m2) {
                 const int t = (N / 2) * h + 2 * m2 + c;
-                if (row_ok && t < a.nt) ib[(size_t)t * Z + i] = make_float2(yr * fr, yi * fr);
+                if (row_ok && t < a.nt)
+                    ob[(((size_t)t * Z + i) * kPB + p0) >> 1] = make_float4(y0[m2].x, y0[m2].y, y1[m2].x, y1[m2].y);
             }
         };
 
@@ -432,18 +497,8 @@ k_zmma_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA,
             return __all_sync(0xffffffffu, mbar_wait(bar, parity));
         };
 
-        // [p][t][i] -> [t][i][p] of a group, then one TMA store
+        // the stage of a group, once every compute thread has written its part
         auto store_group = [&](int it) -> bool {
-            if (tid == 0) bulk_wait_read0();
-            if (!cbar_sync()) return false;
-            const float2 *ib = reinterpret_cast<const float2 *>(smem + a.o_i);
-            float4 *ob = reinterpret_cast<float4 *>(smem + a.o_o);
-            const int nti = a.nt * Z;
-            for (int e = tid; e < nti; e += kCW * 32) {
-                const float2 y0 = ib[e], y1 = ib[nti + e], y2 = ib[2 * nti + e], y3 = ib[3 * nti + e];
-                ob[2 * e] = make_float4(y0.x, y0.y, y1.x, y1.y);
-                ob[2 * e + 1] = make_float4(y2.x, y2.y, y3.x, y3.y);
-            }
             fence_async_smem();
             if (!cbar_sync()) return false;
             if (tid == 0) {
@@ -452,7 +507,14 @@ k_zmma_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA,
             }
             return true;
         };
+        // before the first write of a group: the previous group's store has
+        // read the stage
+        auto stage_free = [&]() -> bool {
+            if (tid == 0) bulk_wait_read0();
+            return cbar_sync();
+        };
 
+        float2 yhold[8];  // results of the even frequency of a pair
         // one group: its kernel rows transposed, then per frequency the
         // results of two frequencies back and the operands of this one
         auto group = [&](int it) -> bool {
@@ -462,8 +524,9 @@ k_zmma_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA,
                 return false;
             }
             {
+                // the group's kernel rows and hB, per frequency and row type
                 const float2 *w = reinterpret_cast<const float2 *>(smem + a.o_w + wbuf * a.wstride);
-                float2 *wt = reinterpret_cast<float2 *>(smem + a.o_wt + wbuf * kPB * a.wtstride);
+                float2 *tab = reinterpret_cast<float2 *>(smem + a.o_wt);
                 const int rows = a.wrows + 2 * Z - 1;
                 for (int e = tid; e < rows * kPB; e += kCW * 32) {
                     const int r = e >> 2, p = e & 3;
@@ -474,13 +537,14 @@ k_zmma_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA,
                         const int sr = r - a.wrows;
                         v = cadd(w[(sr + kb) * kPB + p], w[(sr + ko) * kPB + p]);
                     }
-                    wt[p * (a.wtstride / 8) + r] = v;
+                    float2 *t0 = tab + (size_t)((wbuf * kPB + p) * 2) * (a.wtstride / 8);
+                    t0[r] = make_float2(v.x, -v.y);
+                    t0[a.wtstride / 8 + r] = make_float2(v.y, v.x);
                 }
             }
             if (!cbar_sync()) return false;
             // the staged rows are no longer read
             mbar_arrive(&wempty[wbuf]);
-            if (it + 1 < nitems) prefetch_x(it + 1);
             const long long pbase = ((long long)blockIdx.x + (long long)it * gridDim.x) * kPB;
             const long long pprev = pbase - (long long)gridDim.x * kPB;
 #pragma unroll
@@ -488,22 +552,35 @@ k_zmma_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA,
                 const int f = it * kPB + fp, slot = f & 1;
                 if (f >= 2) {
                     // results of f - 2 (of the previous group when fp < 2),
-                    // which also frees slot `slot`
+                    // which also frees slot `slot`; written in pairs of
+                    // frequencies, the group stored after its fourth
                     if (!wait_all(&mdone[slot], ((f - 2) >> 1) & 1)) {
                         if (lane == 0) atomicOr(a.err, 16u);
                         return false;
                     }
                     tc_fence_after();
-                    const int pf = (fp + 2) & 3;
-                    epilogue(pf, slot, (fp < 2 ? pprev : pbase) + pf);
-                    if (fp == 1 && !store_group(it - 1)) return false;
+                    const int pe = (fp + 2) & 3;
+                    if (pe == 0 || pe == 2) {
+                        if (h < 2) read_results(slot, (fp < 2 ? pprev : pbase) + pe, yhold);
+                    } else {
+                        float2 y[8];
+                        if (h < 2) read_results(slot, (fp < 2 ? pprev : pbase) + pe, y);
+                        if (pe == 1 && !stage_free()) return false;
+                        if (h < 2) write_results(yhold, y, pe - 1);
+                        if (pe == 3 && !store_group(it - 1)) return false;
+                    }
                 }
-                const float2 *wt = reinterpret_cast<const float2 *>(smem + a.o_wt + wbuf * kPB * a.wtstride) +
-                                   (size_t)fp * (a.wtstride / 8);
-                float2 xv[kXItems][2];
-                load_x(xv, pbase + fp);  // in flight while A is formed
-                form_a(wt, slot);
-                form_b(xv, slot);
+                const float2 *tb =
+                    row_ok ? reinterpret_cast<const float2 *>(smem + a.o_wt) +
+                                 (size_t)((wbuf * kPB + fp) * 2 + c) * (a.wtstride / 8) + i
+                           : reinterpret_cast<const float2 *>(smem + a.o_z);
+                form_a(tb, slot);
+                if ((fp & 1) == 0 && !wait_all(&xfull[fp >> 1], it & 1)) {
+                    if (lane == 0) atomicOr(a.err, 1u);
+                    return false;
+                }
+                form_b(fp, slot);
+                if (fp & 1) mbar_arrive(&xempty[fp >> 1]);
                 tc_wait_st();
                 fence_async_smem();
                 tc_fence_before();
@@ -513,7 +590,6 @@ k_zmma_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA,
         };
 
         bool ok = true;
-        if (nitems > 0) prefetch_x(0);
         for (int it = 0; it < nitems && ok; ++it) ok = group(it);
         // the last two frequencies and the last group
         if (ok && nfreq > 0) {
@@ -525,8 +601,17 @@ k_zmma_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA,
                     break;
                 }
                 tc_fence_after();
-                const int fp = f & 3;
-                epilogue(fp, slot, ((long long)blockIdx.x + (long long)(f / kPB) * gridDim.x) * kPB + fp);
+                const int fp = f & 3;  // 2, then 3
+                const long long pg = ((long long)blockIdx.x + (long long)(f / kPB) * gridDim.x) * kPB + fp;
+                if (h < 2) {
+                    if (fp == 2) {
+                        read_results(slot, pg, yhold);
+                    } else {
+                        float2 y[8];
+                        read_results(slot, pg, y);
+                        write_results(yhold, y, 2);
+                    }
+                }
             }
             if (ok) store_group(nitems - 1);
         }
@@ -585,18 +670,23 @@ bool zmma_plan(int Z, int nt, ZmmaArgs *a, size_t *smem_bytes) {
     a->wbytesA = (unsigned)(kPB * a->kA * sizeof(float2));
     a->wbytesB = (unsigned)(kPB * (2 * Z - 1) * sizeof(float2));
     a->wstride = align128((size_t)kPB * a->wrows * sizeof(float2));
-    // per frequency: the kernel rows, then hB (2Z - 1 rows)
-    a->wtstride = (unsigned)(((a->wrows + 2 * Z - 1) * sizeof(float2) + 15) & ~(size_t)15);
+    // a table per buffer, frequency and row type: the kernel rows, hB (2Z - 1
+    // rows), then kZeroRows zero rows
+    a->trows = a->wrows + 2 * Z - 1 + kZeroRows;
+    a->wtstride = (unsigned)((a->trows * sizeof(float2) + 15) & ~(size_t)15);
     a->sbo = (unsigned)(a->K / 4) * 128;
     a->bhalf = align128((size_t)(N / 8) * a->sbo);
     a->bstride = 2 * a->bhalf;
     a->o_w = 0;
-    a->o_wt = a->o_w + 2 * a->wstride;
-    a->o_b = align128(a->o_wt + (size_t)2 * kPB * a->wtstride);
-    a->o_i = a->o_b + 2 * a->bstride;
-    a->o_o = align128(a->o_i + (size_t)kPB * nt * Z * sizeof(float2));
+    a->xbytes = (unsigned)(2 * Z * nt * sizeof(float2));
+    a->xstride = align128(a->xbytes);
+    a->o_x = a->o_w + 2 * a->wstride;
+    a->o_wt = a->o_x + 2 * a->xstride;
+    a->o_z = align128(a->o_wt + (size_t)2 * 2 * kPB * a->wtstride);
+    a->o_b = align128(a->o_z + (size_t)a->trows * sizeof(float2));
+    a->o_o = a->o_b + 2 * a->bstride;
     *smem_bytes = a->o_o + align128((size_t)kPB * nt * Z * sizeof(float2));
-    return *smem_bytes <= 200 * 1024;
+    return *smem_bytes <= 220 * 1024;
 }
 
 }  // namespace
@@ -628,10 +718,10 @@ int mm_launch_zmma_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, lo
     a.jout_lo = Z - 1 - zpad;
     a.fresp = fresp;
     a.err = err;
-    MM_REQUIRE(a.o_w % 128 == 0 && a.wstride % 128 == 0 && a.wbytesA % 128 == 0 && a.o_b % 128 == 0 &&
+    MM_REQUIRE(a.o_x % 128 == 0 && a.xstride % 128 == 0 && a.o_w % 128 == 0 && a.wstride % 128 == 0 && a.wbytesA % 128 == 0 && a.o_b % 128 == 0 &&
                    a.bhalf % 128 == 0 && a.o_o % 128 == 0 && a.wtstride % 8 == 0,
                "shared-memory layout of the tensor z operator");
-    CUtensorMap wA, wB, om;
+    CUtensorMap wA, wB, om, xm;
     const cuuint32_t kA = (cuuint32_t)a.kA, kb1 = (cuuint32_t)(2 * Z - 1);
     {
         cuuint64_t dims[2] = {(cuuint64_t)plane, (cuuint64_t)Zp};
@@ -645,11 +735,19 @@ int mm_launch_zmma_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, lo
         cuuint64_t strides[2] = {(cuuint64_t)plane * 8, (cuuint64_t)plane * 8 * Z};
         cuuint32_t box[3] = {kPB, (cuuint32_t)Z, (cuuint32_t)nt};
         if (int rc = make_map(&om, S, 3, dims, strides, box)) return rc;
+        cuuint32_t xbox[3] = {2, (cuuint32_t)Z, (cuuint32_t)nt};
+        if (int rc = make_map(&xm, S, 3, dims, strides, xbox)) return rc;
     }
-    const void *fn = nt <= 16 ? (const void *)k_zmma_apply<16> : (const void *)k_zmma_apply<32>;
+    const void *fn;
+    if (Z == 50 && zpad == 49)
+        fn = nt <= 16 ? (const void *)k_zmma_apply<16, 50, 49> : (const void *)k_zmma_apply<32, 50, 49>;
+    else if (Z == 50 && zpad == 24)
+        fn = nt <= 16 ? (const void *)k_zmma_apply<16, 50, 24> : (const void *)k_zmma_apply<32, 50, 24>;
+    else
+        fn = nt <= 16 ? (const void *)k_zmma_apply<16, 0, 0> : (const void *)k_zmma_apply<32, 0, 0>;
     if (int rc = mm_set_smem(fn, sm)) return rc;
     const int grid = a.ngroups < mm_sm_count() ? a.ngroups : mm_sm_count();
-    void *args[] = {&S, &wA, &wB, &om, &a};
+    void *args[] = {&wA, &wB, &xm, &om, &a};
     MM_CUDA_TRY(cudaLaunchKernel(fn, dim3(grid), dim3(kThreads), args, sm, st));
     mm_launch_counter_add();
     return MM_OK;

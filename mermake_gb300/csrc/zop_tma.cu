@@ -1,5 +1,6 @@
 // z operator of one Wiener spectrum over a tile batch, with the matrix of each
-// frequency formed in registers and the operands staged by TMA.
+// frequency formed in registers and the operands staged asynchronously (the
+// kernel rows by TMA, the spectra by cp.async).
 //
 // Y[t][i][p] = sum_j M_p[i][j] X[t][j][p] (zop.cu has the derivation).  When
 // 1 <= zpad <= Z - 1 every real plane j has at most three padded copies
@@ -14,14 +15,15 @@
 // place, so the thread keeps them in three register rings of five and loads
 // one new value of each per column (the slots are compile-time constants with
 // j unrolled by five).  No matrix is stored: shared memory holds only the
-// operands, X (nt x Z x kPB) and the kernel rows w[-kA .. 2Z-2] (two TMA boxes
-// of the (Zp, plane) kernel, the negative rows from its top; kA is 2Z - 2
-// rounded up to a multiple of four, so that both boxes land on 128-byte
-// boundaries as tiled TMA requires), double buffered.  The persistent CTAs
-// take groups of kPB consecutive frequencies.  A producer warp issues each
-// group's copies once the buffer is free; the compute warps wait only for
-// their buffer to fill (its "full" mbarrier completes with the copies' bytes)
-// and release it with one arrive per warp on its "empty" mbarrier, so no CTA
+// operands, X (nt x Z x kPB: 32-byte rows, copied by cp.async) and the kernel
+// rows w[-kA .. 2Z-2] (two TMA boxes of the (Zp, plane) kernel, the negative
+// rows from its top; kA is 2Z - 2 rounded up to a multiple of four, so that
+// both boxes land on 128-byte boundaries as tiled TMA requires), double
+// buffered.  The persistent CTAs take groups of kPB consecutive frequencies.
+// A producer warp issues each group's copies once the buffer is free; the
+// compute warps wait only for their buffer to fill (its "full" mbarrier
+// completes with the copies: 32 cp.async arrivals and the TMA bytes) and
+// release it with one arrive per warp on its "empty" mbarrier, so no CTA
 // barrier separates the groups.  Every wait is bounded: a thread that gives up
 // records the failure in *err and returns.
 #include <cuda.h>
@@ -68,13 +70,14 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
     }
     return false;
 }
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int c0, int c1, int c2,
-                                            uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
-        "[%5];" ::"r"(smem_u32(dst)),
-        "l"(map), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
-        : "memory");
+// 16 bytes global -> shared through L2, completion tracked per thread
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+// one arrive on *bar (counted in its initial count) once this thread's
+// earlier cp.async copies have landed
+__device__ __forceinline__ void cp_async_arrive(uint64_t *bar) {
+    asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int c0, int c1, uint64_t *bar) {
     asm volatile(
@@ -100,7 +103,7 @@ struct ZthArgs {
     int jin_hi;        // the reflection about zpad copies planes 1 .. jin_hi (= zpad)
     int jout_lo;       // the reflection about zpad + Z - 1 copies planes jout_lo .. Z - 2
     int kA;            // staged row of w[0]: 2Z - 2 rounded up to a multiple of 4
-    unsigned xbytes;   // X box bytes (kPB x Z x ntc float2)
+    unsigned xbytes;   // X bytes of an item (kPB x Z x ntc float2)
     unsigned wbytesA;  // kernel rows -kA .. -1 (kA x 32 bytes, a multiple of 128)
     unsigned wbytesB;  // kernel rows 0 .. 2Z-2
     unsigned bufstride, woff;  // bytes per buffer, offset of the kernel rows in it
@@ -126,8 +129,7 @@ __device__ __forceinline__ void zth_item(const ZthArgs &a, int item, int &grp, i
 // all nt tiles).
 template <int ZC, bool CH>
 __global__ void __launch_bounds__(kThreadsMax, 2)
-k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap xmap,
-            const __grid_constant__ CUtensorMap wmapA, const __grid_constant__ CUtensorMap wmapB, const ZthArgs a) {
+k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA, const __grid_constant__ CUtensorMap wmapB, const ZthArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t full[2], empty[2];
     __shared__ int3 item_of[2];  // (group, first owned tile, box start) of each buffer's item
@@ -152,7 +154,8 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap xmap,
     const int ncw = (kPB * nig * a.ntg + 31) / 32;  // compute warps; warp ncw produces
     if (tid == 0) {
         for (int b = 0; b < 2; ++b) {
-            mbar_init(&full[b], 1);
+            // the producer warp's 32 copy arrivals and its expect_tx arrive
+            mbar_init(&full[b], 33);
             mbar_init(&empty[b], ncw);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -160,27 +163,39 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap xmap,
     __syncthreads();
 
     if (warp == ncw) {
-        // producer: the copies of item `it` go to buffer it & 1 once the
-        // compute warps have released its previous use (item it - 2)
-        if (lane != 0) return;
+        // producer warp: the copies of item `it` go to buffer it & 1 once the
+        // compute warps have released its previous use (item it - 2).  X (the
+        // box's nt x Z rows of 32 bytes) by cp.async from all 32 lanes: a
+        // tensor copy moves a box row per ~5 SM cycles, which rows this short
+        // would make the bound; the kernel rows (2Z - 1 + kA rows) by TMA.
         int grp, own0, box0;
         for (int item = blockIdx.x, it = 0; item < a.nitems; item += gridDim.x, ++it) {
             const int buf = it & 1;
-            if (it >= 2 && !mbar_wait(&empty[buf], ((it - 2) >> 1) & 1)) {
-                atomicOr(a.err, 4u);
-                return;
+            const bool ok = it < 2 || mbar_wait(&empty[buf], ((it - 2) >> 1) & 1);
+            if (!__all_sync(0xffffffffu, ok)) {
+                if (lane == 0) atomicOr(a.err, 4u);
+                break;
             }
-            // order the compute warps' reads of the buffer before the TMA writes
+            // order the compute warps' reads of the buffer before the copies
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             unsigned char *b = smem + (size_t)buf * a.bufstride;
             zth_item(a, item, grp, own0, box0);
-            item_of[buf] = make_int3(grp, own0, box0);  // published by the arrive below
+            if (lane == 0) item_of[buf] = make_int3(grp, own0, box0);  // published by the arrives below
             const int p0 = grp * kPB;
-            mbar_expect_tx(&full[buf], a.xbytes + a.wbytesA + a.wbytesB);
-            tma_load_3d(b, &xmap, p0, 0, box0, &full[buf]);
-            tma_load_2d(b + a.woff, &wmapA, p0, a.Zp - kb, &full[buf]);
-            tma_load_2d(b + a.woff + a.wbytesA, &wmapB, p0, 0, &full[buf]);
+            const int nchunk = 2 * Z * a.ntc;  // 16-byte halves of the box's rows
+            for (int k = lane; k < nchunk; k += 32) {
+                const int row = k >> 1;  // (tile - box0) * Z + plane
+                cp_async16(b + (size_t)k * 16, S + ((long long)box0 * Z + row) * a.plane + p0 + 2 * (k & 1));
+            }
+            cp_async_arrive(&full[buf]);
+            if (lane == 0) {
+                mbar_expect_tx(&full[buf], a.wbytesA + a.wbytesB);
+                tma_load_2d(b + a.woff, &wmapA, p0, a.Zp - kb, &full[buf]);
+                tma_load_2d(b + a.woff + a.wbytesA, &wmapB, p0, 0, &full[buf]);
+            }
         }
+        // no copy may still be landing when the CTA exits
+        asm volatile("cp.async.wait_all;" ::: "memory");
         return;
     }
 
@@ -352,14 +367,8 @@ int mm_launch_zth_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, lon
     MM_REQUIRE(((uintptr_t)S & 15) == 0 && ((uintptr_t)w & 15) == 0, "spectra must be 16-byte aligned");
     ZthPlan pl;
     zth_plan(Z, nt, &pl);
-    CUtensorMap xmap, wA, wB;
+    CUtensorMap wA, wB;
     const cuuint32_t kb = (cuuint32_t)(2 * Z - 2), kA = (cuuint32_t)zth_ka(Z);
-    {
-        cuuint64_t dims[3] = {(cuuint64_t)plane, (cuuint64_t)Z, (cuuint64_t)nt};
-        cuuint64_t strides[2] = {(cuuint64_t)plane * 8, (cuuint64_t)plane * 8 * Z};
-        cuuint32_t box[3] = {kPB, (cuuint32_t)Z, (cuuint32_t)pl.ntc};
-        if (int rc = make_map(&xmap, S, 3, dims, strides, box)) return rc;
-    }
     {
         cuuint64_t dims[2] = {(cuuint64_t)plane, (cuuint64_t)Zp};
         cuuint64_t strides[1] = {(cuuint64_t)plane * 8};
@@ -401,7 +410,7 @@ int mm_launch_zth_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, lon
     if (per_sm < 1) per_sm = 1;
     const long long cap = (long long)mm_sm_count() * per_sm;
     const unsigned grid = (unsigned)(a.nitems < cap ? a.nitems : cap);
-    void *args[] = {&S, &xmap, &wA, &wB, &a};
+    void *args[] = {&S, &wA, &wB, &a};
     MM_CUDA_TRY(cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, sm, st));
     mm_launch_counter_add();
     return MM_OK;

@@ -68,7 +68,7 @@ def zforms(dec):
     if dec.z_operator is not None:
         forms = [_lib.MM_ZFORM_DIRECT] + forms
         if dec.psf_fft.shape[0] == 1:
-            forms = [_lib.MM_ZFORM_REGISTERS, _lib.MM_ZFORM_SHARED] + forms
+            forms = [_lib.MM_ZFORM_REGISTERS, _lib.MM_ZFORM_TENSOR, _lib.MM_ZFORM_SHARED] + forms
     return forms
 
 

@@ -215,7 +215,8 @@ def test_autotune_picks_batch_and_z_form(mm):
     dimg, dflat = img.cuda(), torch.from_numpy(flat).cuda()
     assert dec.n_tiles(img.shape) == 25
     forms = tune.zforms(dec)
-    assert forms == [_lib.MM_ZFORM_REGISTERS, _lib.MM_ZFORM_SHARED, _lib.MM_ZFORM_DIRECT, _lib.MM_ZFORM_TRANSFORMS]
+    assert forms == [_lib.MM_ZFORM_REGISTERS, _lib.MM_ZFORM_TENSOR, _lib.MM_ZFORM_SHARED, _lib.MM_ZFORM_DIRECT,
+                     _lib.MM_ZFORM_TRANSFORMS]
     times = tune.autotune(dec, dimg, dflat, HYB, candidates=(4, -1), reps=1)
     assert set(times) == {(b, f) for b in (4, -1) for f in forms} and all(t > 0 for t in times.values())
     best = min(times, key=times.get)
