@@ -171,25 +171,43 @@ static_assert(2 * 32 * kMaxY2 + 32 <= kQueue, "queue too small for the two-sign 
 constexpr int kNbBatch = 8;
 constexpr int kFitU = 2;  // fit sample rounds whose loads are in flight together (4 costs occupancy)
 
-// 1 when v is not below any in-range neighbour of (z, x, y) in the sphere
+// 1 when the voxel (raw value vr) is not below any in-range neighbour of
+// (z, x, y) in the sphere of radius delta, compared as transformed values.
+// The transform x -> x / div (div > 0, round to nearest) is monotone, so a
+// neighbour whose raw value is not above the voxel's (not below, for the
+// negated volume) cannot be above it after the transform either; only the
+// others are transformed and compared exactly.  An interior voxel (delta
+// from every face) reads its neighbours at fixed offsets, with no reflection.
 __device__ __forceinline__ bool max_test(const float *__restrict__ img, const Vols &V, Xform t, int Z, int X,
-                                         int Y, int z, int x, int y, float v, const char4 *sph, int nn) {
+                                         int Y, int z, int x, int y, float vr, const char4 *sph, int nn,
+                                         int delta) {
+    const float vt = xf(vr, t);
+    const bool mono = t.div >= 0.f;
+    const bool inner = z >= delta && z < Z - delta && x >= delta && x < X - delta && y >= delta && y < Y - delta;
+    const float *c = img + z * V.isz + x * V.isx + y;
     for (int q0 = 0; q0 < nn; q0 += kNbBatch) {
         float nb[kNbBatch];
 #pragma unroll
         for (int u = 0; u < kNbBatch; ++u) {
-            nb[u] = -INFINITY;  // no neighbour: never above v
+            nb[u] = NAN;  // no neighbour: never above
             const int q = q0 + u;
             if (q < nn) {
                 const char4 o = sph[q];
-                const int nz = refl(z + o.x, Z), nx = refl(x + o.y, X), ny = refl(y + o.z, Y);
-                if (nz >= 0 && nz < Z && nx >= 0 && nx < X && ny >= 0 && ny < Y)
-                    nb[u] = xf(img[nz * V.isz + nx * V.isx + ny], t);
+                if (inner) {
+                    nb[u] = c[o.x * V.isz + o.y * V.isx + o.z];
+                } else {
+                    const int nz = refl(z + o.x, Z), nx = refl(x + o.y, X), ny = refl(y + o.z, Y);
+                    if (nz >= 0 && nz < Z && nx >= 0 && nx < X && ny >= 0 && ny < Y)
+                        nb[u] = img[nz * V.isz + nx * V.isx + ny];
+                }
             }
         }
         bool below = false;
 #pragma unroll
-        for (int u = 0; u < kNbBatch; ++u) below |= v < nb[u];
+        for (int u = 0; u < kNbBatch; ++u) {
+            const bool may = t.neg ? nb[u] < vr : nb[u] > vr;
+            if (!mono || may) below |= vt < xf(nb[u], t);
+        }
         if (below) return false;
     }
     return true;
@@ -212,7 +230,7 @@ __device__ __forceinline__ void append_cand(bool hit, unsigned key, int y, int v
 // appends the maxima to cand, or to cand2 for the entries of the negated
 // volume (bit 30 of y, queued by the two-sign pass)
 __device__ __forceinline__ void test_round(const float *__restrict__ img, const Vols &V, Xform t, int Z, int X,
-                                           int Y, const char4 *sph, int nn, const unsigned *k, const int *yq,
+                                           int Y, const char4 *sph, int nn, int delta, const unsigned *k, const int *yq,
                                            const float *vq, int cnt, unsigned lane, int vi, uint2 *__restrict__ cand,
                                            unsigned cap, unsigned *__restrict__ count, uint2 *__restrict__ cand2,
                                            unsigned *__restrict__ count2, bool both) {
@@ -226,7 +244,7 @@ __device__ __forceinline__ void test_round(const float *__restrict__ img, const 
         y = e & 0x3fffffff;
         Xform ts = t;
         if (neg) ts.neg = !ts.neg;
-        is_max = max_test(img, V, ts, Z, X, Y, (int)(key & 0xffffu), (int)(key >> 16), y, vq[lane], sph, nn);
+        is_max = max_test(img, V, ts, Z, X, Y, (int)(key & 0xffffu), (int)(key >> 16), y, vq[lane], sph, nn, delta);
     }
     append_cand(is_max && !neg, key, y, vi, lane, cand, cap, count);
     if (both) append_cand(is_max && neg, key, y, vi, lane, cand2, cap, count2);
@@ -288,7 +306,7 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
                         const int at = qn + __popc(m & ((1u << lane) - 1));
                         my_k[at] = key;
                         my_y[at] = y | (sgn << 30);
-                        my_v[at] = sv;
+                        my_v[at] = vals[k];  // raw: max_test transforms it
                     }
                     qn += __popc(m);
                 }
@@ -297,7 +315,7 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
             if (qn >= 32) {
                 const int full = qn & ~31;
                 for (int q0 = 0; q0 < full; q0 += 32)
-                    test_round(img, V, t, Z, X, Y, sph, nn, my_k + q0, my_y + q0, my_v + q0, 32, lane, vi, cand, cap,
+                    test_round(img, V, t, Z, X, Y, sph, nn, delta, my_k + q0, my_y + q0, my_v + q0, 32, lane, vi, cand, cap,
                                count, cand2, count2, both);
                 const int rem = qn - full;
                 __syncwarp();
@@ -313,7 +331,7 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
         }
     }
     if (qn > 0)
-        test_round(img, V, t, Z, X, Y, sph, nn, my_k, my_y, my_v, qn, lane, vi, cand, cap, count, cand2, count2,
+        test_round(img, V, t, Z, X, Y, sph, nn, delta, my_k, my_y, my_v, qn, lane, vi, cand, cap, count, cand2, count2,
                    both);
 }
 

@@ -120,6 +120,32 @@ def test_maxima_strided_and_uint16_raw(mm):
     assert_rows_close(got, want)
 
 
+def test_maxima_normalised_ties_of_distinct_raw_values(mm):
+    """The maxima test compares normalised values: a neighbour whose raw value
+    is larger but whose quotient by the divisor rounds to the same float32
+    (3.9916298 and the next float, divided by 0.99041766) does not make the
+    centre a non-maximum, while the raw comparison alone would; the negated
+    volume mirrors it."""
+    a = np.float32(3.9916298)
+    b = np.nextafter(a, np.float32(10))
+    div = np.float32(0.99041766)
+    assert a < b and a / div == b / div
+    im = np.full((5, 9, 9), 0.25, np.float32)
+    im[2, 4, 4], im[2, 4, 5] = a, b
+    raw = np.ones((5, 9, 9), np.float32)
+    for neg in (False, True):
+        src = -im if neg else im
+        v = src / div
+        if neg:
+            v = -v
+        got = mm["maxima"].find_local_maxima(torch.from_numpy(src).cuda(), 1.0, 2, 1, torch.from_numpy(raw).cuda(),
+                                             norm_div=float(div), negate=neg).cpu().numpy()
+        want = ck.find_local_maxima(v.astype(np.float32), 1.0, 2, 1, raw)
+        # both voxels are maxima (their fits coincide, so the rows are equal)
+        assert len(want) == 2 and got.shape == want.shape
+        np.testing.assert_allclose(ck.sort_rows(got), ck.sort_rows(want), rtol=1e-5, atol=1e-4)
+
+
 def test_maxima_normalise_and_negate_on_read(mm):
     """DAPI: v / rms then -v (__main__.py:221-225), applied on read, bit-identical
     to dividing the volume first."""
