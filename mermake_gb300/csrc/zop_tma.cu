@@ -100,13 +100,17 @@ struct ZthArgs {
     int nchunks;       // chunks the batch's tiles are split into
     long long plane;
     int nitems;        // frequency groups (ceil(plane / kPB)) x chunks
-    int jin_hi;        // the reflection about zpad copies planes 1 .. jin_hi (= zpad)
-    int jout_lo;       // the reflection about zpad + Z - 1 copies planes jout_lo .. Z - 2
     int kA;            // staged row of w[0]: 2Z - 2 rounded up to a multiple of 4
     unsigned xbytes;   // X bytes of an item (kPB x Z x ntc float2)
     unsigned wbytesA;  // kernel rows -kA .. -1 (kA x 32 bytes, a multiple of 128)
     unsigned wbytesB;  // kernel rows 0 .. 2Z-2
     unsigned bufstride, woff;  // bytes per buffer, offset of the kernel rows in it
+    unsigned zoff;     // bytes: the zero rows (2Z + 3 of them) after the two buffers
+    // the columns j in segments of one reflection class: segment k covers
+    // [segj[k], segj[k + 1]) (segj[nseg] = Z) with class segc[k]: 0 only the
+    // reflection about zpad (w[i + j]), 1 only the one about zpad + Z - 1
+    // (w[i + j - 2Z + 2]), 2 both (hB[i + j]), 3 neither
+    int nseg, segj[6], segc[6];
     const float *fresp;
     unsigned *err;
 };
@@ -131,7 +135,7 @@ template <int ZC, bool CH>
 __global__ void __launch_bounds__(kThreadsMax, 2)
 k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA, const __grid_constant__ CUtensorMap wmapB, const ZthArgs a) {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t full[2], empty[2];
+    __shared__ __align__(8) uint64_t full[2], empty[2], wfull[2];
     __shared__ int3 item_of[2];  // (group, first owned tile, box start) of each buffer's item
     const int Z = ZC > 0 ? ZC : a.Z;
     const int nig = Z / kTI;
@@ -154,11 +158,17 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA, c
     const int ncw = (kPB * nig * a.ntg + 31) / 32;  // compute warps; warp ncw produces
     if (tid == 0) {
         for (int b = 0; b < 2; ++b) {
-            // the producer warp's 32 copy arrivals and its expect_tx arrive
-            mbar_init(&full[b], 33);
+            // the producer warp's 32 copy arrivals and its 32 arrivals once
+            // hB is written
+            mbar_init(&full[b], 64);
             mbar_init(&empty[b], ncw);
+            mbar_init(&wfull[b], 1);
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    {
+        float2 *zr = reinterpret_cast<float2 *>(smem + a.zoff);
+        for (int e = tid; e < (2 * Z + 3) * kPB; e += blockDim.x) zr[e] = make_float2(0.f, 0.f);
     }
     __syncthreads();
 
@@ -189,10 +199,24 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA, c
             }
             cp_async_arrive(&full[buf]);
             if (lane == 0) {
-                mbar_expect_tx(&full[buf], a.wbytesA + a.wbytesB);
-                tma_load_2d(b + a.woff, &wmapA, p0, a.Zp - kb, &full[buf]);
-                tma_load_2d(b + a.woff + a.wbytesA, &wmapB, p0, 0, &full[buf]);
+                mbar_expect_tx(&wfull[buf], a.wbytesA + a.wbytesB);
+                tma_load_2d(b + a.woff, &wmapA, p0, a.Zp - kb, &wfull[buf]);
+                tma_load_2d(b + a.woff + a.wbytesA, &wmapB, p0, 0, &wfull[buf]);
             }
+            // hB[s] = w[s] + w[s - 2Z + 2], s < 2Z - 1, after the kernel rows
+            if (!__all_sync(0xffffffffu, mbar_wait(&wfull[buf], (it >> 1) & 1))) {
+                if (lane == 0) atomicOr(a.err, 4u);
+                break;
+            }
+            {
+                const float2 *w = reinterpret_cast<const float2 *>(b + a.woff);
+                float2 *hbr = reinterpret_cast<float2 *>(b + a.woff + a.wbytesA + a.wbytesB);
+                for (int e = lane; e < (2 * Z - 1) * kPB; e += 32) {
+                    const int sr = e / kPB, pp = e - sr * kPB;
+                    hbr[e] = cadd(w[(sr + kb) * kPB + pp], w[(sr + ko) * kPB + pp]);
+                }
+            }
+            mbar_arrive(&full[buf]);
         }
         // no copy may still be landing when the CTA exits
         asm volatile("cp.async.wait_all;" ::: "memory");
@@ -213,18 +237,24 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA, c
             for (int u = 0; u < kTI; ++u)
 #pragma unroll
                 for (int b = 0; b < kTT; ++b) acc[u][b] = make_float2(0.f, 0.f);
-            // rings: direct family value of position q (= row - column) in slot
-            // q mod 5; the two reflected families of position q (= row + column)
-            // in slot q mod 5 (i0 and the column blocks are multiples of 5)
-            float2 rT[kTI], rI[kTI], rO[kTI];
+            // rings: the direct value of position q (= row - column) in slot
+            // q mod 5; the reflected value of position q (= row + column), from
+            // the source of the column's class, in slot q mod 5 (i0 and the
+            // column blocks are multiples of 5).  A column that starts a
+            // segment of another class reloads the reflected ring.
+            const int wrows = a.kA + 2 * Z - 1;
+            const int zrow = (int)((a.zoff - (unsigned)buf * a.bufstride - a.woff) / (kPB * sizeof(float2)));
+            auto seg_row = [&](int k) {
+                const int cls = a.segc[k];
+                return cls == 0 ? kb : cls == 1 ? ko : cls == 2 ? wrows : zrow;
+            };
+            int sk = 0, hrow = seg_row(0), jnext = a.nseg > 1 ? a.segj[1] : Z;
+            float2 rT[kTI], rH[kTI];
 #pragma unroll
             for (int q = 1; q < kTI; ++q) rT[q] = W[(i0 + q + kb) * kPB + p];
 #pragma unroll
-            for (int q = 0; q < kTI - 1; ++q) {
-                rI[q] = W[(i0 + q + kb) * kPB + p];
-                rO[q] = W[(i0 + q + ko) * kPB + p];
-            }
-            rT[0] = rI[kTI - 1] = rO[kTI - 1] = make_float2(0.f, 0.f);
+            for (int q = 0; q < kTI - 1; ++q) rH[q] = W[(i0 + q + hrow) * kPB + p];
+            rT[0] = rH[kTI - 1] = make_float2(0.f, 0.f);
             // the box's tiles past ntc read stale buffer contents; their
             // results are not stored
             const float2 *xr = X + ((size_t)tl0 * Z) * kPB + p;
@@ -233,17 +263,17 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA, c
                 for (int u = 0; u < kTI; ++u) {
                     const int j = j0 + u;
                     rT[(kTI - u) % kTI] = W[(i0 - j + kb) * kPB + p];
-                    rI[(u + kTI - 1) % kTI] = W[(i0 + j + kTI - 1 + kb) * kPB + p];
-                    rO[(u + kTI - 1) % kTI] = W[(i0 + j + kTI - 1 + ko) * kPB + p];
-                    const bool vin = j >= 1 && j <= a.jin_hi;
-                    const bool vout = j >= a.jout_lo && j <= Z - 2;
+                    if (j == jnext) {
+                        ++sk;
+                        hrow = seg_row(sk);
+                        jnext = sk + 1 < a.nseg ? a.segj[sk + 1] : Z;
+#pragma unroll
+                        for (int q = 0; q < kTI - 1; ++q) rH[(q + u) % kTI] = W[(i0 + j + q + hrow) * kPB + p];
+                    }
+                    rH[(u + kTI - 1) % kTI] = W[(i0 + j + kTI - 1 + hrow) * kPB + p];
                     float2 m[kTI];
 #pragma unroll
-                    for (int q = 0; q < kTI; ++q) {
-                        m[q] = rT[(q - u + kTI) % kTI];
-                        if (vin) m[q] = cadd(m[q], rI[(q + u) % kTI]);
-                        if (vout) m[q] = cadd(m[q], rO[(q + u) % kTI]);
-                    }
+                    for (int q = 0; q < kTI; ++q) m[q] = cadd(rT[(q - u + kTI) % kTI], rH[(q + u) % kTI]);
                     float2 x[kTT];
 #pragma unroll
                     for (int b = 0; b < kTT; ++b) x[b] = xr[((size_t)b * Z + j) * kPB];
@@ -322,17 +352,21 @@ int zth_ka(int Z) { return (2 * Z - 2 + 3) & ~3; }
 
 // bytes per buffer: X for ntg whole tile groups (the last group's threads
 // read tiles past the box, whose results are not stored), then the kernel
-// rows -kA .. 2Z - 2; both parts start on 128-byte boundaries
+// rows -kA .. 2Z - 2 and hB[0 .. 2Z - 2]; both parts start on 128-byte
+// boundaries
 size_t zth_bufstride(int Z, int ntg, unsigned *woff) {
     const size_t xb = (size_t)kPB * Z * ntg * kTT * sizeof(float2);
-    const size_t wb = (size_t)kPB * (zth_ka(Z) + 2 * Z - 1) * sizeof(float2);
+    const size_t wb = (size_t)kPB * (zth_ka(Z) + 2 * Z - 1 + 2 * Z - 1) * sizeof(float2);
     const size_t xo = (xb + 127) & ~(size_t)127;
     if (woff) *woff = (unsigned)xo;
     return (xo + wb + 127) & ~(size_t)127;
 }
 
 // shared memory of one CTA, two CTAs per SM
-constexpr size_t kSmemMax = 110 * 1024;
+constexpr size_t kSmemMax = 112 * 1024;
+
+// the zero rows after the two buffers
+size_t zth_zero_bytes(int Z) { return ((size_t)(2 * Z + 3) * kPB * sizeof(float2) + 127) & ~(size_t)127; }
 
 // How a batch of nt tiles is split: the fewest chunks whose tile groups fit
 // one CTA (threads and shared memory), then the tiles spread evenly over them.
@@ -342,7 +376,8 @@ struct ZthPlan {
 bool zth_plan(int Z, int nt, ZthPlan *pl) {
     const int ntg_all = (nt + kTT - 1) / kTT;
     int ntg_max = ntg_all;
-    while (ntg_max > 0 && (zth_threads(Z, ntg_max) > kThreadsMax || 2 * zth_bufstride(Z, ntg_max, nullptr) > kSmemMax))
+    while (ntg_max > 0 && (zth_threads(Z, ntg_max) > kThreadsMax ||
+                           2 * zth_bufstride(Z, ntg_max, nullptr) + zth_zero_bytes(Z) > kSmemMax))
         --ntg_max;
     if (ntg_max == 0) return false;
     pl->nchunks = (ntg_all + ntg_max - 1) / ntg_max;
@@ -387,19 +422,31 @@ int mm_launch_zth_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, lon
     const long long nitems = ((plane + kPB - 1) / kPB) * pl.nchunks;
     MM_REQUIRE(nitems < (1LL << 31), "z operator: too many frequency groups");
     a.nitems = (int)nitems;
-    a.jin_hi = zpad;
-    a.jout_lo = Z - 1 - zpad;
+    // the column segments of one reflection class
+    a.nseg = 0;
+    for (int j = 0, prev = -1; j < Z; ++j) {
+        const bool vin = j >= 1 && j <= zpad, vout = j >= Z - 1 - zpad && j <= Z - 2;
+        const int cls = vin ? (vout ? 2 : 0) : (vout ? 1 : 3);
+        if (cls != prev) {
+            MM_REQUIRE(a.nseg < 6, "z operator: more than six column segments");
+            a.segj[a.nseg] = j;
+            a.segc[a.nseg] = cls;
+            ++a.nseg;
+            prev = cls;
+        }
+    }
     a.kA = (int)kA;
     a.xbytes = (unsigned)(kPB * Z * pl.ntc * sizeof(float2));
     a.wbytesA = (unsigned)(kPB * kA * sizeof(float2));
     a.wbytesB = (unsigned)(kPB * (kb + 1) * sizeof(float2));
     a.bufstride = (unsigned)zth_bufstride(Z, pl.ntg, &a.woff);
+    a.zoff = 2 * a.bufstride;
     MM_REQUIRE(a.bufstride % 128 == 0 && a.woff % 128 == 0 && a.wbytesA % 128 == 0,
                "TMA destinations of the z operator must be 128-byte aligned");
     MM_REQUIRE(a.xbytes <= a.woff, "z operator: the X box overruns its buffer");
     a.fresp = fresp;
     a.err = err;
-    const size_t sm = 2 * (size_t)a.bufstride;
+    const size_t sm = 2 * (size_t)a.bufstride + zth_zero_bytes(Z);
     const int threads = zth_threads(Z, a.ntg);
     const void *fn = pl.nchunks > 1 ? (const void *)k_zth_apply<0, true>
                      : Z == 50     ? (const void *)k_zth_apply<50, false>

@@ -268,15 +268,19 @@ def test_zpass_flop_model_follows_the_z_pass_form():
 
 
 def test_z_operator_register_rings_restate_the_matrix():
-    """The TMA z operator (csrc/zop_tma.cu) forms M[i][j] in registers from
-    three rings of five z-kernel values (the direct copy of plane j and its
-    reflections about zpad and zpad + Z - 1) and loads one value of each ring
-    per column.  Restated here with the kernel's slot arithmetic and staged
-    rows (k + kA for w[k mod Zp], kA = 2Z - 2 rounded up to a multiple of 4,
-    the rows past the padded depth zero as the TMA fills them), against M
-    built from the padding map; every read stays inside the staged rows."""
+    """The register z operator (csrc/zop_tma.cu) forms M[i][j] in registers from
+    two rings of five values: the direct copy w[i - j], and the reflected copy
+    of the column's class, read from the staged kernel rows (w[i + j] or
+    w[i + j - 2Z + 2]), from hB[i + j] = w[i + j] + w[i + j - 2Z + 2] where
+    both reflections copy plane j, or from zero rows where neither does.  The
+    columns come in segments of one class; a column that starts a segment
+    reloads the reflected ring.  Restated here with the kernel's slot
+    arithmetic, segment table and staged rows (k + kA for w[k mod Zp], kA =
+    2Z - 2 rounded up to a multiple of 4, the rows past the padded depth zero as
+    the TMA fills them; hB after them), against M built from the padding map;
+    every read stays inside the staged, hB or zero rows."""
     rng = np.random.default_rng(5)
-    for Z, zpad in [(50, 49), (50, 24), (30, 29), (40, 20), (10, 3), (15, 14), (20, 9)]:
+    for Z, zpad in [(50, 49), (50, 24), (30, 29), (40, 20), (10, 3), (15, 14), (20, 9), (80, 79), (80, 39)]:
         Zp = Z + 2 * zpad
         w = rng.standard_normal(Zp) + 1j * rng.standard_normal(Zp)
         M = np.zeros((Z, Z), complex)
@@ -288,35 +292,57 @@ def test_z_operator_register_rings_restate_the_matrix():
         kA = (2 * Z - 2 + 3) & ~3  # rows of box A: 2Z - 2 rounded up to a multiple of 4 (128-byte boxes)
         kb, ko = kA, kA - (2 * Z - 2)
         assert (kA * 4 * 8) % 128 == 0
-        staged = np.zeros(kA + 2 * Z - 1, complex)
+        wrows = kA + 2 * Z - 1
+        staged = np.zeros(wrows + 2 * Z - 1, complex)
         for row in range(kA):  # box A: kernel rows Zp - kA .. Zp - 1 (negative rows read as zero)
             src = Zp - kA + row
             staged[row] = w[src] if 0 <= src < Zp else 0
         for row in range(2 * Z - 1):  # box B: kernel rows 0 .. 2Z - 2 (rows >= Zp read as zero)
             staged[kA + row] = w[row] if row < Zp else 0
-        n_staged = len(staged)
+        for sr in range(2 * Z - 1):  # hB, written by the producer warp
+            staged[wrows + sr] = staged[sr + kb] + staged[sr + ko]
+        zeros = np.zeros(2 * Z + 3, complex)
+        zrow = 1000  # the zero rows, elsewhere in shared memory
+        # column segments of one reflection class (the host's table)
+        segj, segc = [], []
+        for j in range(Z):
+            vin, vout = 1 <= j <= zpad, Z - 1 - zpad <= j <= Z - 2
+            cls = (2 if vout else 0) if vin else (1 if vout else 3)
+            if not segc or segc[-1] != cls:
+                segj.append(j)
+                segc.append(cls)
+        assert len(segj) <= 6
 
         def at(i):
-            assert 0 <= i < n_staged, i  # every read stays inside the staged rows
+            if i >= zrow:
+                assert i - zrow < len(zeros), i
+                return zeros[i - zrow]
+            assert 0 <= i < len(staged), i  # every read stays inside the staged rows
             return staged[i]
+
+        def seg_row(k):
+            return {0: kb, 1: ko, 2: wrows, 3: zrow}[segc[k]]
 
         got = np.zeros((Z, Z), complex)
         for i0 in range(0, Z, 5):
-            rT, rI, rO = [0j] * 5, [0j] * 5, [0j] * 5
+            sk, hrow = 0, seg_row(0)
+            jnext = segj[1] if len(segj) > 1 else Z
+            rT, rH = [0j] * 5, [0j] * 5
             for q in range(1, 5):
                 rT[q] = at(i0 + q + kb)
             for q in range(4):
-                rI[q] = at(i0 + q + kb)
-                rO[q] = at(i0 + q + ko)
+                rH[q] = at(i0 + q + hrow)
             for j0 in range(0, Z, 5):
                 for u in range(5):
                     j = j0 + u
                     rT[(5 - u) % 5] = at(i0 - j + kb)
-                    rI[(u + 4) % 5] = at(i0 + j + 4 + kb)
-                    rO[(u + 4) % 5] = at(i0 + j + 4 + ko)
-                    vin = 1 <= j <= zpad
-                    vout = Z - 1 - zpad <= j <= Z - 2
+                    if j == jnext:
+                        sk += 1
+                        hrow = seg_row(sk)
+                        jnext = segj[sk + 1] if sk + 1 < len(segj) else Z
+                        for q in range(4):
+                            rH[(q + u) % 5] = at(i0 + j + q + hrow)
+                    rH[(u + 4) % 5] = at(i0 + j + 4 + hrow)
                     for q in range(5):
-                        m = rT[(q - u + 5) % 5] + (rI[(q + u) % 5] if vin else 0) + (rO[(q + u) % 5] if vout else 0)
-                        got[i0 + q, j] = m
+                        got[i0 + q, j] = rT[(q - u + 5) % 5] + rH[(q + u) % 5]
         np.testing.assert_allclose(got, M, rtol=0, atol=1e-12)
