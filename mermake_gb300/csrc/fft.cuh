@@ -643,6 +643,119 @@ __device__ __noinline__ void stage_rader(float2 *__restrict__ src, float2 *__res
     }
 }
 
+// 678 = 113 x 6 in two stages of one pass less: the Rader 113 stage (phases
+// 1 and 2 of stage_rader, NL lines, Ns = 1), then its phase 3 fused with the
+// radix-6 stage.  Sub-transform jb of a line (elements jb + 6 r) gives
+// Y_jb[k], k < 113, and the radix-6 butterfly of output k combines the six
+// Y_jb[k] (twiddled by w678^(k jb)) into X[k + 113 r'].  A pair of threads
+// owns (q1, line): thread c runs phase 3 for the sub-transforms jb = c, c + 2,
+// c + 4, which yields Y_jb[k] for the 7 outputs k = g^(q1 + 16 q2) (and k = 0
+// when q1 = 0), so that the even (c = 0) and odd (c = 1) halves of each
+// radix-6 butterfly (6 = 2 x 3, as dft6) are in the pair's registers: each
+// thread does its 3-point DFT, the pair swaps three values by shuffle, and
+// each writes three of the six outputs.  The result is left in A (the input,
+// consumed by phase 1); T (phases 1-2) lives in B.  Needs 32 NL threads per
+// work round (a pair per (q1, line), 16 values of q1) in whole warps.
+template <bool INV, int NL>
+__device__ __noinline__ void stage_rader113_x6(float2 *__restrict__ A, float2 *__restrict__ B,
+                                               const float2 *__restrict__ tw, const float2 *__restrict__ tb,
+                                               float4 *__restrict__ scr_all) {
+    constexpr int R = 113, N1 = 16, N2 = 7, M = R - 1, n = 678, m = 6, nb = m * NL;
+    constexpr int lnl = ilog2c(NL);
+    const float2 *Hh = tb + R + (INV ? M : 0);
+    const float2 *wM = tb + R + 2 * M;
+    const int2 *gq = reinterpret_cast<const int2 *>(tb + R + 3 * M);  // (g^-q, g^q)
+    float c2[1], s2[1];
+    float2 *x0s = reinterpret_cast<float2 *>(scr_all);
+    float2 *s0s = x0s + nb;
+    float2 *T = B;
+    for (int e = threadIdx.x; e < N1 * nb; e += blockDim.x) {
+        const int q1 = e / nb, b = e - q1 * nb;
+        const int l = b & (NL - 1), j = b >> lnl;
+        float2 v[N2];
+#pragma unroll
+        for (int q2 = 0; q2 < N2; ++q2) v[q2] = A[sidx(j + gq[q1 + N1 * q2].x * m, l, NL)];
+        if (q1 == 0) x0s[b] = A[sidx(j, l, NL)];
+        rader_dft<N2, false>(v, c2, s2);
+        T[(q1 * N2) * nb + b] = v[0];
+#pragma unroll
+        for (int k2 = 1; k2 < N2; ++k2) T[(q1 * N2 + k2) * nb + b] = cmul(v[k2], wM[q1 * k2]);
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < N2 * nb; e += blockDim.x) {
+        const int k2 = e / nb, b = e - k2 * nb;
+        float2 v[N1];
+#pragma unroll
+        for (int q1 = 0; q1 < N1; ++q1) v[q1] = T[(q1 * N2 + k2) * nb + b];
+        rader_dft<N1, false>(v, c2, s2);
+        if (k2 == 0) s0s[b] = v[0];
+#pragma unroll
+        for (int k1 = 0; k1 < N1; ++k1) v[k1] = cmul(v[k1], Hh[k2 + N2 * k1]);
+        rader_dft<N1, true>(v, c2, s2);
+        T[k2 * nb + b] = v[0];
+#pragma unroll
+        for (int q1 = 1; q1 < N1; ++q1) T[(q1 * N2 + k2) * nb + b] = cmulc(v[q1], wM[q1 * k2]);
+    }
+    __syncthreads();
+    const float h = 0.5f, rt = 0.86602540378443864676f;
+    const float2 w61 = make_float2(h, INV ? rt : -rt), w62 = make_float2(-h, INV ? rt : -rt);
+    for (int e = threadIdx.x; e < 2 * N1 * NL; e += blockDim.x) {
+        const int c = e & 1, l = (e >> 1) & (NL - 1), q1 = e >> (1 + lnl);
+        // phase 3 of sub-transforms jb = c + 2 i
+        float2 y[3][N2], x0[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const int b = (c + 2 * i) * NL + l;
+#pragma unroll
+            for (int k2 = 0; k2 < N2; ++k2) y[i][k2] = T[(q1 * N2 + k2) * nb + b];
+            rader_dft<N2, true>(y[i], c2, s2);
+            x0[i] = x0s[b];
+        }
+        // output k of the three sub-transforms, twiddled, 3-point DFT, swap
+        // with the pair, three outputs X[k + 113 r]
+        auto butterfly = [&](int k, float2 y0, float2 y1, float2 y2, unsigned mask) {
+            float2 z[3] = {y0, y1, y2};
+#pragma unroll
+            for (int i = 1; i < 3; ++i) {
+                const float2 w = tw[k * (c + 2 * i)];
+                z[i] = INV ? cmulc(z[i], w) : cmul(z[i], w);
+            }
+            if (c) {
+                const float2 w = tw[k];
+                z[0] = INV ? cmulc(z[0], w) : cmul(z[0], w);
+            }
+            dft_odd<3, INV>(z);
+            // c = 0 holds E (even jb), c = 1 the odd half O and sends w6^r O[r]
+            if (c) {
+                z[1] = cmul(z[1], w61);
+                z[2] = cmul(z[2], w62);
+            }
+            float2 g[3];
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+                g[r] = make_float2(__shfl_xor_sync(mask, z[r].x, 1), __shfl_xor_sync(mask, z[r].y, 1));
+#pragma unroll
+            for (int r = 0; r < 3; ++r)
+                A[sidx(k + R * (r + 3 * c), l, NL)] = c ? csub(g[r], z[r]) : cadd(z[r], g[r]);
+        };
+        // the lanes of a warp take the same rounds (32 NL work items in whole
+        // warps), so the shuffles run with full warps; the q1 = 0 pairs (the
+        // output k = 0 of the three sub-transforms) shuffle among themselves
+#pragma unroll
+        for (int q2 = 0; q2 < N2; ++q2)
+            butterfly(gq[q1 + N1 * q2].y, cadd(x0[0], y[0][q2]), cadd(x0[1], y[1][q2]), cadd(x0[2], y[2][q2]),
+                      0xffffffffu);
+        const unsigned m0 = __ballot_sync(0xffffffffu, q1 == 0);
+        if (q1 == 0) {
+            float2 s0[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) s0[i] = s0s[(c + 2 * i) * NL + l];
+            butterfly(0, cadd(x0[0], s0[0]), cadd(x0[1], s0[1]), cadd(x0[2], s0[2]), m0);
+        }
+    }
+    (void)n;
+}
+
 template <int R, bool INV, int NC = 0, int NLC = 0, int NSC = 0>
 __device__ __forceinline__ void stage_small(const float2 *__restrict__ src, float2 *__restrict__ dst,
                                             int n, int nl, int Ns, const float2 *tw) {
@@ -803,9 +916,9 @@ __device__ float2 *fft_lines_fixed(float2 *A, float2 *B, const FftPlan &P, const
                                    const float2 *tab_s, float4 *scr) {
     static_assert(N == 678 || N == 478, "specialised lengths: 678, 478");
     if constexpr (N == 678) {
-        stage_rader<113, 16, 7, INV, 678, NL, 1>(A, B, N, NL, 1, tw_s, tab_s + P.ptab[0], scr);
+        stage_rader113_x6<INV, NL>(A, B, tw_s, tab_s + P.ptab[0], scr);
         __syncthreads();
-        stage_small<6, INV, 678, NL, 113>(A, B, N, NL, 113, tw_s);
+        return A;
     } else {
         stage_rader<239, 14, 17, INV, 478, NL, 1>(A, B, N, NL, 1, tw_s, tab_s + P.ptab[0], scr);
         __syncthreads();
