@@ -78,6 +78,11 @@ WORKLOADS = {
                            delta_fit=3, sigmaZ=1, sigmaXY=1.5),
                   dapi_args=dict(tile_size=500, overlap=89, beta=0.01, threshold=3.0, blur_radius=50, delta=5,
                                  delta_fit=5, sigmaZ=1, sigmaXY=1.5)),
+    "dapi1k": dict(Z=50, X=1024, Y=1024, colours=0, puncta=0, flat=False, dapi=True, nuclei=75,
+                   hyb=dict(tile_size=500, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
+                            delta_fit=3, sigmaZ=1, sigmaXY=1.5),
+                   dapi_args=dict(tile_size=500, overlap=89, beta=0.01, threshold=3.0, blur_radius=50, delta=5,
+                                  delta_fit=5, sigmaZ=1, sigmaXY=1.5)),
     "quad": dict(Z=50, X=1000, Y=1000, colours=1, puncta=10000, flat=True, dapi=False, nuclei=0,
                  hyb=dict(tile_size=500, overlap=89, beta=1e-4, threshold=3600, blur_radius=30, delta=1,
                           delta_fit=3, sigmaZ=1, sigmaXY=1.5)),

@@ -276,6 +276,10 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
     const char4 *sph = g_sphere[delta];
     const unsigned lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+    // a raw value with |x| <= lo is below the threshold after x -> x / div
+    // (either sign): its quotient is not computed
+    const bool skip_small = t.div > 0.f && th > 0.f;
+    const float lo = skip_small ? th * t.div * (1.f - 0x1p-18f) : 0.f;
     unsigned *my_k = qk[warp];
     int *my_y = qy[warp];
     float *my_v = qv[warp];
@@ -293,14 +297,21 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
                 vals[k] = y < yhi ? rp[y] : 0.f;
             }
             // queue the voxels above the threshold (maxima.cu:19; a NaN
-            // threshold admits every voxel)
+            // threshold admits every voxel) whose y neighbours held by the
+            // adjacent lanes are not larger: a larger neighbour in the sphere
+            // fails the test anyway, so only the others need it
 #pragma unroll
             for (int k = 0; k < kMaxY; ++k) {
                 const int y = y0 + 32 * k + (int)lane;
-                const float v = xf(vals[k], t);
+                // a value below the threshold enters only as a y neighbour,
+                // which it cannot be above, so 0 stands for it there
+                const float v = skip_small && fabsf(vals[k]) <= lo ? 0.f : xf(vals[k], t);
+                const float vl = __shfl_up_sync(0xffffffffu, v, 1), vr = __shfl_down_sync(0xffffffffu, v, 1);
+                const bool hasl = delta > 0 && lane > 0 && y - 1 < yhi, hasr = delta > 0 && lane < 31 && y + 1 < yhi;
                 for (int sgn = 0; sgn < (both ? 2 : 1); ++sgn) {
                     const float sv = sgn ? -v : v;
-                    const bool up = y < yhi && !(sv <= th);
+                    const bool lower = (hasl && sv < (sgn ? -vl : vl)) || (hasr && sv < (sgn ? -vr : vr));
+                    const bool up = y < yhi && !(sv <= th) && !lower;
                     const unsigned m = __ballot_sync(0xffffffffu, up);
                     if (up) {
                         const int at = qn + __popc(m & ((1u << lane) - 1));
@@ -415,7 +426,10 @@ k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand
         if (table) {
             // at most 515 samples, so the reference's cap of 600 (maxima.cu:194)
             // never binds: kFitU rounds of loads in flight, then their sums in
-            // the same per-lane order as one round at a time
+            // the same per-lane order as one round at a time.  A spot
+            // delta_fit or more from every face samples without reflection.
+            const bool inner = z0 >= delta_fit && z0 < Z - delta_fit && x0 >= delta_fit && x0 < X - delta_fit &&
+                               y0 >= delta_fit && y0 < Y - delta_fit;
             for (int c0 = 0; c0 < nsamp; c0 += 32 * kFitU) {
                 float vv[kFitU], rr[kFitU], gg[kFitU];
                 char4 oo[kFitU];
@@ -428,8 +442,13 @@ k_fit(Vols V, const uint2 *__restrict__ cand, const unsigned *__restrict__ ncand
                     oo[u] = make_char4(0, 0, 0, 0);
                     if (ci < nsamp) {
                         const char4 o = otab[ci];
-                        const int zz = refl(z0 + o.x, Z), xx = refl(x0 + o.y, X), yy = refl(y0 + o.z, Y);
-                        if (zz >= 0 && zz < Z && xx >= 0 && xx < X && yy >= 0 && yy < Y) {
+                        int zz = z0 + o.x, xx = x0 + o.y, yy = y0 + o.z;
+                        if (!inner) {
+                            zz = refl(zz, Z);
+                            xx = refl(xx, X);
+                            yy = refl(yy, Y);
+                        }
+                        if (inner || (zz >= 0 && zz < Z && xx >= 0 && xx < X && yy >= 0 && yy < Y)) {
                             okk[u] = true;
                             oo[u] = o;
                             vv[u] = xf(img[zz * V.isz + xx * V.isx + yy], t);
@@ -577,12 +596,15 @@ static Vols make_vols(const MaximaArgs &a) {
 }
 
 static dim3 maxima_grid(const MaximaArgs &a) {
-    // a warp per (z, x) row, 8 rows per CTA
+    // a warp per (z, x) row, 8 rows per CTA, the CTAs of all volumes together
+    // about two rounds of the SMs' resident CTAs (four per SM), so that each
+    // warp's queue of candidates persists over many rows
     long long rows = (long long)a.Z * (a.tiles ? (long long)a.tiles->P : (long long)a.X);
-    int gx = (int)((rows + 7) / 8);
-    if (gx > 152 * 16) gx = 152 * 16;
+    long long gx = (rows + 7) / 8;
+    const long long cap = (long long)mm_sm_count() * 8 / (a.nvol > 0 ? a.nvol : 1);
+    if (gx > cap) gx = cap;
     if (gx < 1) gx = 1;
-    return dim3(gx, a.nvol);
+    return dim3((unsigned)gx, a.nvol);
 }
 
 // Launches maxima + fit.  cand/ncand: scratch list and its device counter;
@@ -597,7 +619,7 @@ int mm_launch_maxima_fit(const MaximaArgs &a, uint2 *cand, unsigned cand_cap, un
     k_maxima<false><<<maxima_grid(a), 32 * kMaxWarps, 0, st>>>(V, a.th, a.delta, t, cand, cand_cap, ncand, nullptr,
                                                                 nullptr);
     MM_CHECK_LAUNCH();
-    k_fit<<<152 * 8, 256, 0, st>>>(V, cand, ncand, cand_cap, a.delta_fit, a.sigmaZ, a.sigmaXY, t, out, out_cap,
+    k_fit<<<mm_sm_count() * 8, 256, 0, st>>>(V, cand, ncand, cand_cap, a.delta_fit, a.sigmaZ, a.sigmaXY, t, out, out_cap,
                                    out_count, a.keep_filter);
     MM_CHECK_LAUNCH();
     return MM_OK;
@@ -617,10 +639,10 @@ int mm_launch_maxima_fit_pm(const MaximaArgs &a, uint2 *cand, unsigned cap, unsi
     k_maxima<true><<<maxima_grid(a), 32 * kMaxWarps, 0, st>>>(V, a.th, a.delta, tp, cand, cap, ncand_plus, cand + cap,
                                                                ncand_minus);
     MM_CHECK_LAUNCH();
-    k_fit<<<152 * 8, 256, 0, st>>>(V, cand, ncand_plus, cap, a.delta_fit, a.sigmaZ, a.sigmaXY, tp, out_plus, cap_plus,
+    k_fit<<<mm_sm_count() * 8, 256, 0, st>>>(V, cand, ncand_plus, cap, a.delta_fit, a.sigmaZ, a.sigmaXY, tp, out_plus, cap_plus,
                                    nullptr, 0);
     MM_CHECK_LAUNCH();
-    k_fit<<<152 * 8, 256, 0, st>>>(V, cand + cap, ncand_minus, cap, a.delta_fit, a.sigmaZ, a.sigmaXY, tm, out_minus,
+    k_fit<<<mm_sm_count() * 8, 256, 0, st>>>(V, cand + cap, ncand_minus, cap, a.delta_fit, a.sigmaZ, a.sigmaXY, tm, out_minus,
                                    cap_minus, nullptr, 0);
     MM_CHECK_LAUNCH();
     return MM_OK;
