@@ -172,6 +172,7 @@ class FovRunner:
         self._slots = [dict(), dict()]
         self._next = 0
         self._buffer = None
+        self._out = {}
         self.h2d_bytes = 0
 
     def _dev(self, slot, key, host):
@@ -203,23 +204,90 @@ class FovRunner:
         return ticket
 
     def run(self, ticket, flats=None, dapi_flat=None):
+        """The FOV of ``ticket``: the DAPI block and every colour enqueued on the
+        current stream by the asynchronous drivers (their counts on the
+        device), then one read of all counts and the rows.  An output that did
+        not fit its rows (or candidate list) is run again by the synchronous
+        driver, which resizes; later FOVs get rows sized from its count."""
         cur = torch.cuda.current_stream()
         evs, devs = list(ticket["events"]), list(ticket["dev"])
+        n = len(devs) - (1 if ticket["has_dapi"] else 0)
+        flats = list(flats) if flats is not None else [None] * n
+        Z, X, Y = shape = tuple(int(v) for v in devs[0].shape)
+        dev = devs[0].device
+        L = _lib.lib()
+        ctx = _lib.ctx(dev.index)
+        sp = _lib.stream_ptr(cur)
+        counts = torch.zeros(3 + 2 * n, dtype=torch.int32, device=dev)
+        cbase = counts.data_ptr()
         out_plus = out_minus = None
+        dapi_img = dflat = None
         if ticket["has_dapi"]:
+            d, a = self.dec_dapi, _settings(self.dapi_args)
             cur.wait_event(evs.pop(0))
-            p, m, self._buffer, _ = dapi_spots(self.dec_dapi, devs.pop(0), dapi_flat, buffer=self._buffer,
-                                               batch=self.batch, **self.dapi_args)
-            out_plus, out_minus = p.cpu().numpy(), m.cpu().numpy()
-        flats = list(flats) if flats is not None else [None] * len(devs)
-        rows = []
-        for ev, d, f in zip(evs, devs, flats):
+            dapi_img = devs.pop(0)
+            dflat = _flat(dapi_flat, shape)
+            if self._buffer is None or tuple(self._buffer.shape) != shape:
+                self._buffer = torch.empty(shape, dtype=torch.float32, device=dev)
+            cap_p = _capacity(d, ("dapi+", Z, X, Y), 1 << 16)
+            cap_m = _capacity(d, ("dapi-", Z, X, Y), 1 << 16)
+            plus = self._rows("plus", cap_p, dev)
+            minus = self._rows("minus", cap_m, dev)
+            rms = self._rows("rms", 1, dev)
+            bd = tune.batch_for(d, shape, dapi=True) if self.batch == 0 else self.batch
+            _lib.check(L.mm_dapi_spots_async(
+                ctx, _lib.ptr(dapi_img), Z, X, Y, dapi_img.stride(0), dapi_img.stride(1), _lib.ptr(dflat),
+                dflat.stride(0) if dflat is not None else 0, _lib.ptr(d.psf_fft), d.psf_fft.shape[0],
+                _lib.ptr(d.z_operator), d.tile_size, d.zpad, d.overlap, a["br"], a["th"], a["delta"], a["dfit"],
+                a["sz"], a["sxy"], max(int(bd), 0), _lib.ptr(self._buffer), _lib.ptr(plus), cap_p, _lib.ptr(minus),
+                cap_m, _lib._vp(cbase), _lib.ptr(rms), sp))
+        d, a = self.dec_hyb, _settings(self.hyb_args)
+        cap = _capacity(d, ("hyb", Z, X, Y), 1 << 18)
+        bh = tune.batch_for(d, shape) if self.batch == 0 else self.batch
+        rows, fls = [], []
+        for c, (ev, img, f) in enumerate(zip(evs, devs, flats)):
             cur.wait_event(ev)
-            rows.append(hyb_spots(self.dec_hyb, d, f, batch=self.batch, **self.hyb_args).cpu().numpy())
+            fl = _flat(f, shape)
+            fls.append(fl)
+            r = self._rows(("hyb", c), cap, dev)
+            rows.append(r)
+            _lib.check(L.mm_hyb_spots_async(
+                ctx, _lib.ptr(img), Z, X, Y, img.stride(0), img.stride(1), _lib.ptr(fl),
+                fl.stride(0) if fl is not None else 0, _lib.ptr(d.psf_fft), d.psf_fft.shape[0],
+                _lib.ptr(d.z_operator), d.tile_size, d.zpad, d.overlap, a["br"], a["th"], a["delta"], a["dfit"],
+                a["sz"], a["sxy"], max(int(bh), 0), _lib.ptr(r), cap, _lib._vp(cbase + 4 * (3 + 2 * c)),
+                _lib._vp(cbase + 4 * (4 + 2 * c)), sp))
+        cnt = counts.cpu().tolist()  # the FOV's one synchronisation
+        if ticket["has_dapi"]:
+            dd = self.dec_dapi
+            _seen(dd, ("dapi+", Z, X, Y), cnt[0])
+            _seen(dd, ("dapi-", Z, X, Y), cnt[1])
+            if cnt[2] or cnt[0] > cap_p or cnt[1] > cap_m:
+                p, m, self._buffer, _ = dapi_spots(dd, dapi_img, dapi_flat, buffer=self._buffer, batch=self.batch,
+                                                   **self.dapi_args)
+            else:
+                p, m = plus[:cnt[0]], minus[:cnt[1]]
+            out_plus, out_minus = p.cpu().numpy(), m.cpu().numpy()
+        out = []
+        for c in range(n):
+            nc = cnt[3 + 2 * c]
+            _seen(d, ("hyb", Z, X, Y), nc)
+            if cnt[4 + 2 * c] or nc > cap:
+                out.append(hyb_spots(d, devs[c], fls[c], batch=self.batch, **self.hyb_args).cpu().numpy())
+            else:
+                out.append(rows[c][:nc].cpu().numpy())
         done = torch.cuda.Event()
         done.record(cur)
         self._slots[ticket["slot"]]["free"] = done
-        return out_plus, out_minus, rows
+        return out_plus, out_minus, out
+
+    def _rows(self, key, cap, dev):
+        """A persistent device buffer of at least ``cap`` rows of 8 floats."""
+        buf = self._out.get(key)
+        if buf is None or buf.shape[0] < cap or buf.device != dev:
+            buf = torch.empty((cap, 8), dtype=torch.float32, device=dev)
+            self._out[key] = buf
+        return buf
 
 
 def _settings(args):

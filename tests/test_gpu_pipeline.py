@@ -198,6 +198,28 @@ def test_fov_runner_matches_direct_calls(mm):
     assert runner.h2d_bytes == 3 * Z * X * Y * 2
 
 
+def test_fov_runner_reruns_outputs_that_overflow(mm, monkeypatch):
+    """FovRunner enqueues a FOV with the asynchronous drivers and reads all
+    counts once; an output whose rows did not fit (here every output, with
+    row buffers of 8) is run again by the synchronous driver, and the rows
+    are those of the direct calls."""
+    Z, X, Y = 12, 170, 150
+    dapi = mm["synth"].dapi_stack(Z, X, Y, 5, n_nuclei=12, radii=(3.0, 12.0, 12.0))
+    img, flat, psf = hyb_case(mm, seed=3, Z=Z, X=X, Y=Y)
+    flat_d = torch.from_numpy(flat).cuda()
+    dh = mm["dc"].Deconvolver(psf, (Z, X, Y), zpad=Z - 1, **HYB)
+    dd = mm["dc"].Deconvolver(psf, (Z, X, Y), zpad=(Z - 1) // 2, **DAPI)
+    want_p, want_m, _, _ = mm["pl"].dapi_spots(dd, dapi.cuda(), None, **DAPI)
+    want = mm["pl"].hyb_spots(dh, img.cuda(), flat_d, **HYB)
+    assert len(want) > 8 and len(want_p) > 8
+    monkeypatch.setattr(mm["pl"], "_capacity", lambda dec, key, default: 8)
+    runner = mm["pl"].FovRunner(dh, dd, HYB, DAPI)
+    p, m, rows = runner.run(runner.submit(dapi.cpu().pin_memory(), [img.cpu().pin_memory()]), [flat_d])
+    np.testing.assert_array_equal(ck.sort_rows(p), ck.sort_rows(want_p.cpu().numpy()))
+    np.testing.assert_array_equal(ck.sort_rows(m), ck.sort_rows(want_m.cpu().numpy()))
+    np.testing.assert_array_equal(ck.sort_rows(rows[0]), ck.sort_rows(want.cpu().numpy()))
+
+
 def test_autotune_picks_batch_and_z_form(mm):
     """tune.autotune times every candidate batch size with every z form the
     geometry qualifies for (25 tiles of one PSF, Z = 10: the matrix in
