@@ -299,12 +299,13 @@ def job_rate(world, units_per_rank, steps, total_ms):
     return world * units_per_rank * steps / (total_ms / 1e3)
 
 
-def zpass_flops(w, s):
+def zpass_flops(w, s, zform="auto"):
     """FP32 flops of one FOV's z passes, by the form each channel's batch runs
     (the library's choice in run_tiles): one Z x Z complex matrix per frequency
     and tile when one spectrum serves a batch of >= 10 tiles of height <= 64,
-    else the direct sum over the padded planes (outputs and planes in blocks of
-    8).  A complex FMA is 8 flops."""
+    or when each tile's matrix is formed from its own z kernel (Z a multiple
+    of 5 up to 80, 1 <= zpad <= Z - 1); else the direct sum over the padded
+    planes (outputs and planes in blocks of 8).  A complex FMA is 8 flops."""
     shape = (w["Z"], w["X"], w["Y"])
     out = 0.0
     for dec, n in ((s["dec_h"], w["colours"]), (s["dec_d"], 1 if s["dec_d"] is not None else 0)):
@@ -313,7 +314,9 @@ def zpass_flops(w, s):
         nt, Z, plane = dec.n_tiles(shape), dec.tile_height, dec.P * dec.H
         if dec.z_operator is None:
             continue
-        if dec.psf_fft.shape[0] == 1 and nt >= 10 and Z <= 64:
+        shared = dec.psf_fft.shape[0] == 1 and nt >= 10 and Z <= 64
+        per_tile = Z % 5 == 0 and Z <= 80 and 1 <= dec.zpad <= Z - 1
+        if zform != "direct" and (shared or per_tile):
             per = Z * Z
         else:
             per = -(-Z // 8) * 8 * (-(-dec.Zp // 8) * 8)
@@ -460,7 +463,7 @@ def gpu_arm(args, rank, world, local):
         props = torch.cuda.get_device_properties(dev)
         mhz = (line["clocks"] or {}).get("sm_max_mhz") or peaks.get("sm_max_mhz") or 2070.0
         fpeak = props.multi_processor_count * 128 * 2 * mhz * 1e6 / 1e12
-        fl = zpass_flops(w, s) * args.steps / dl
+        fl = zpass_flops(w, s, args.zform) * args.steps / dl
         fach = fl / ((dms / dl) / 1e3) / 1e12
         rf = line["roofline"]
         hbm = {k: rf[k] for k in ("achieved", "peak", "unit", "frac", "peak_source")}

@@ -226,15 +226,22 @@ int fill_geom(TileGeom &g, int Z, int X, int Y, long long isz, long long isx, lo
 // kept spots of a hyb tile have centroids inside it and read their maxima and
 // fit neighbourhoods, at most delta_fit + max(delta, delta_fit) closer to the
 // edge.
-// The z step of a batch: MM_ZFORM_REGISTERS (k_zth_apply), _SHARED
-// (k_zop_apply), _DIRECT (k_zconv) or _TRANSFORMS (k_zpass).  The context's
-// MM_OPT_ZFORM choice when the batch qualifies for it (a z kernel, one
-// spectrum for the two matrix forms, the forms' shape limits), else the first
-// of those four that qualifies, the matrix forms only for batches of at least
-// MM_ZOP_MIN_TILES tiles.  A register-form batch split into tile chunks
-// (deeper tiles: each chunk reloads the z kernel and rounds its tiles up to
-// whole thread groups) gives way to the shared-memory form where that form
-// takes the depth.
+// The z step of a batch: MM_ZFORM_REGISTERS (k_zth_apply over one shared
+// spectrum, else k_zpt_apply with a kernel per tile), _SHARED (k_zop_apply),
+// _DIRECT (k_zconv) or _TRANSFORMS (k_zpass).  The context's MM_OPT_ZFORM
+// choice when the batch qualifies for it (a z kernel, one spectrum for the
+// shared and tensor forms, the forms' shape limits), else the first of
+// registers, shared, direct and transforms that qualifies, the shared-spectrum
+// matrix forms only for batches of at least MM_ZOP_MIN_TILES tiles.  A
+// register-form batch split into tile chunks (deeper tiles: each chunk reloads
+// the z kernel and rounds its tiles up to whole thread groups) gives way to
+// the shared-memory form where that form takes the depth.
+bool zth_takes(const TileGeom &g, bool forced) {
+    if (g.npsf != 1 || g.nt < (forced ? 1 : MM_ZOP_MIN_TILES)) return false;
+    const int chunks = mm_zth_supported(g.Z, g.zpad, g.nt, (long long)g.P * g.H);
+    return chunks == 1 || (chunks > 1 && (forced || mm_zop_supported(g.Z, g.zpad) == 0));
+}
+
 int zform_of(const mm_ctx *c, const TileGeom &g, const float2 *zop) {
     const long long plane = (long long)g.P * g.H;
     // forced: the context's own choice, which takes any batch the form takes
@@ -242,9 +249,12 @@ int zform_of(const mm_ctx *c, const TileGeom &g, const float2 *zop) {
         const int min_tiles = forced ? 1 : MM_ZOP_MIN_TILES;
         switch (f) {
             case MM_ZFORM_REGISTERS: {
-                if (!zop || g.npsf != 1 || g.nt < min_tiles) return false;
-                const int chunks = mm_zth_supported(g.Z, g.zpad, g.nt, plane);
-                return chunks == 1 || (chunks > 1 && (forced || mm_zop_supported(g.Z, g.zpad) == 0));
+                if (!zop) return false;
+                // one spectrum and a batch the shared-spectrum forms take: the
+                // per-tile form only where k_zth_apply does not take it
+                if (g.npsf == 1 && g.nt >= min_tiles && mm_zop_supported(g.Z, g.zpad) != 0)
+                    return zth_takes(g, forced);
+                return zth_takes(g, forced) || mm_zpt_supported(g.Z, g.zpad, g.nt, plane) != 0;
             }
             case MM_ZFORM_SHARED:
                 return zop && g.npsf == 1 && g.nt >= min_tiles && mm_zop_supported(g.Z, g.zpad) != 0;
@@ -316,13 +326,21 @@ int run_tiles(mm_ctx *c, TileGeom g, const void *image, int dtype, const float *
         if ((rc = small_get(c, &sm, st))) return rc;
         StageTimer t(c, ST_ZPASS, 2 * spec_b + 8.0 * wstride, st);
         if ((rc = mm_launch_zmma_apply(S, zop, g.Z, g.zpad, g.Zp, plane_c, g.nt, fresp, &sm->err, st))) return rc;
-    } else if (zform == MM_ZFORM_REGISTERS) {
+    } else if (zform == MM_ZFORM_REGISTERS && zth_takes(g, c->zform == MM_ZFORM_REGISTERS)) {
         // the matrix formed in registers, operands staged by TMA; the z kernel
         // is read once per batch
         Small *sm;
         if ((rc = small_get(c, &sm, st))) return rc;
         StageTimer t(c, ST_ZPASS, 2 * spec_b + 8.0 * wstride, st);
         if ((rc = mm_launch_zth_apply(S, zop, g.Z, g.zpad, g.Zp, plane_c, g.nt, fresp, &sm->err, st))) return rc;
+    } else if (zform == MM_ZFORM_REGISTERS) {
+        // the same with each tile's own z kernel, read once per tile
+        Small *sm;
+        if ((rc = small_get(c, &sm, st))) return rc;
+        StageTimer t(c, ST_ZPASS, 2 * spec_b + (g.npsf == 1 ? 8.0 * wstride : w_b), st);
+        if ((rc = mm_launch_zpt_apply(S, zop, wstride, g.Z, g.zpad, g.Zp, plane_c, g.t0, g.nt, g.npsf, fresp,
+                                      &sm->err, st)))
+            return rc;
     } else if (zform == MM_ZFORM_SHARED) {
         // the z kernel (Zp per frequency, the size of W) is read once per batch
         StageTimer t(c, ST_ZPASS, 2 * spec_b + 8.0 * wstride, st);

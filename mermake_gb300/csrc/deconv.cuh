@@ -156,6 +156,13 @@ int mm_launch_zmma_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, lo
                          const float *fresp, unsigned *err, cudaStream_t st);
 int mm_launch_zth_apply(float2 *S, const float2 *w, int Z, int zpad, int Zp, long long plane, int nt,
                         const float *fresp, unsigned *err, cudaStream_t st);
+// The register form with a z kernel per tile (zop_pt.cu): tile t of the
+// launch, spectrum index t0 + t, takes the kernel w + (t0 + t) * wstride when
+// npsf > 1, else w.  Z a multiple of 5 up to 80, 1 <= zpad <= Z - 1, an even
+// plane.  A CTA that gives up waiting for its copies sets *err.
+int mm_zpt_supported(int Z, int zpad, int nt, long long plane);
+int mm_launch_zpt_apply(float2 *S, const float2 *w, long long wstride, int Z, int zpad, int Zp, long long plane,
+                        int t0, int nt, int npsf, const float *fresp, unsigned *err, cudaStream_t st);
 // 1 - D(kx) D(ky) per half-spectrum frequency of a P x P plane, D the
 // frequency response of the box mean of width 2 delta + 1 (zop.cu)
 int mm_blur_response_get(int P, int delta, const float **out);

@@ -11,8 +11,9 @@ time).  ``default_batch`` therefore takes all tiles, up to a scratch budget
 (``SCRATCH_BYTES``), and the library picks the z form (``MM_ZFORM_AUTO``).
 
 ``autotune`` times, on a real channel, every candidate batch size with every
-z form the geometry qualifies for (the matrix in registers, the matrix in
-shared memory, the direct sum per tile, the transforms over the padded depth;
+z form the geometry qualifies for (the matrix in registers, over one shared
+spectrum or per tile, the matrix on the tensor cores or in shared memory, the
+direct sum per tile, the transforms over the padded depth;
 ``mm_ctx_set_option(MM_OPT_ZFORM)``) and keeps the fastest pair on the
 Deconvolver, where the drivers find it (``settings_for``).
 
@@ -66,9 +67,9 @@ def zforms(dec):
     from . import _lib
     forms = [_lib.MM_ZFORM_TRANSFORMS]
     if dec.z_operator is not None:
-        forms = [_lib.MM_ZFORM_DIRECT] + forms
+        forms = [_lib.MM_ZFORM_REGISTERS, _lib.MM_ZFORM_DIRECT] + forms
         if dec.psf_fft.shape[0] == 1:
-            forms = [_lib.MM_ZFORM_REGISTERS, _lib.MM_ZFORM_TENSOR, _lib.MM_ZFORM_SHARED] + forms
+            forms = forms[:1] + [_lib.MM_ZFORM_TENSOR, _lib.MM_ZFORM_SHARED] + forms[1:]
     return forms
 
 

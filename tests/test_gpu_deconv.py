@@ -227,9 +227,11 @@ def test_z_operator_matches_padded_transforms(dc, Z, zpad, ts, ov):
                                                   (50, 24, 30, 9, 25, 5)])
 def test_z_convolution_matches_padded_transforms(dc, Z, zpad, ts, ov, npsf, nx):
     """The direct z convolution (each tile's own z kernel, summed over the
-    padded planes) against the FFT z pass over the padded depth: one PSF in
-    batches below the matrix form's 10 tiles, a PSF per tile, Z = 80 and 128
-    (past the matrix form's 64), zpad > Z, and 25 tiles of 25 PSFs."""
+    padded planes; MM_ZFORM_DIRECT) against the FFT z pass over the padded
+    depth: one PSF in batches below the matrix form's 10 tiles, a PSF per
+    tile, Z = 80 and 128 (past the matrix form's 64), zpad > Z, and 25 tiles
+    of 25 PSFs."""
+    from mermake_gb300 import _lib
     rng = np.random.default_rng(Z + npsf)
     X = Y = nx * ts
     img = rng.integers(100, 5000, (Z, X, Y)).astype(np.uint16)
@@ -248,8 +250,53 @@ def test_z_convolution_matches_padded_transforms(dc, Z, zpad, ts, ov, npsf, nx):
     assert npsf > 1 or nt < 10
     ra = torch.empty((nt, Z, a.P, a.P), device="cuda")
     rb = torch.empty_like(ra)
-    a._call(u16(img), dc.MM_DTYPE_U16, None, 0, nt, 6, res_out=ra)
+    with _lib.zform(_lib.MM_ZFORM_DIRECT):
+        a._call(u16(img), dc.MM_DTYPE_U16, None, 0, nt, 6, res_out=ra)
     b._call(u16(img), dc.MM_DTYPE_U16, None, 0, nt, 6, res_out=rb)
+    err = float((ra - rb).abs().max() / rb.abs().max())
+    assert err < 2e-5, err
+
+
+@pytest.mark.parametrize("Z,zpad,ts,ov,npsf,nx,batch", [(40, 39, 12, 4, 4, 2, 6), (40, 39, 10, 3, 9, 3, 6),
+                                                        (50, 24, 30, 9, 25, 5, 25), (5, 1, 10, 3, 6, 3, 4),
+                                                        (45, 10, 12, 4, 4, 2, 4), (80, 79, 8, 3, 1, 3, 9),
+                                                        (60, 29, 11, 4, 16, 4, 16), (10, 9, 21, 5, 1, 2, 3),
+                                                        (50, 49, 10, 3, 4, 2, 4), (20, 19, 10, 3, 9, 3, 9)])
+def test_per_tile_register_z_operator_matches_padded_transforms(dc, Z, zpad, ts, ov, npsf, nx, batch):
+    """The z operator with each tile's matrix formed in registers from its own
+    z kernel (csrc/zop_pt.cu; the register form of a batch of several PSFs,
+    or of one PSF in batches below the shared-spectrum forms' 10 tiles)
+    against the FFT z pass over the padded depth: items of 16 frequencies
+    (Z <= 55) and of 8 (Z = 60, 80), chunks of several tiles (Z = 5, 10, 20)
+    with a last chunk of fewer, batches that start past tile 0 (the kernel
+    index t0 + t), zpad 1 to Z - 1 (the column classes at compile time for
+    zpad = Z - 1), and planes whose last group of frequencies lies partly
+    outside them (P = 19, 20, 31)."""
+    from mermake_gb300 import _lib
+    rng = np.random.default_rng(200 + Z + npsf)
+    X = Y = nx * ts
+    img = rng.integers(100, 5000, (Z, X, Y)).astype(np.uint16)
+    psfs = {}
+    for k in range(npsf):
+        p = np.zeros((5, 5, 5), np.float32)
+        p[2, 2, 2] = 1.0
+        p[1:4, 1:4, 1:4] += 0.1 * rng.random((3, 3, 3)).astype(np.float32)
+        psfs[k] = p
+    psf = psfs if npsf > 1 else psfs[0]
+    args = dict(tile_size=ts, zpad=zpad, overlap=ov, beta=0.01)
+    a = dc.Deconvolver(psf, img.shape, z_operator=True, **args)
+    b = dc.Deconvolver(psf, img.shape, z_operator=False, **args)
+    nt = a.n_tiles(img.shape)
+    assert nt == (nx * nx if npsf == 1 else min(nx * nx, npsf))  # zip() drops the tiles past the PSFs
+    ra = torch.full((nt, Z, a.P, a.P), float("nan"), device="cuda")
+    rb = torch.empty_like(ra)
+    with _lib.zform(_lib.MM_ZFORM_REGISTERS if npsf > 1 else _lib.MM_ZFORM_AUTO):
+        for t0 in range(0, nt, batch):
+            n = min(batch, nt - t0)
+            a._call(u16(img), dc.MM_DTYPE_U16, None, t0, n, 6, res_out=ra[t0:t0 + n])
+    b._call(u16(img), dc.MM_DTYPE_U16, None, 0, nt, 6, res_out=rb)
+    torch.cuda.synchronize()
+    assert bool(torch.isfinite(ra).all())
     err = float((ra - rb).abs().max() / rb.abs().max())
     assert err < 2e-5, err
 

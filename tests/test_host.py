@@ -248,23 +248,29 @@ def test_fov_graph_settings_follow_the_driver_defaults():
 
 def test_zpass_flop_model_follows_the_z_pass_form():
     """bench.zpass_flops: the matrix form (Z x Z complex FMAs per frequency and
-    tile) for one spectrum and >= 10 tiles of height <= 64, else the direct sum
-    (outputs and padded planes in blocks of 8); 8 flops a complex FMA."""
+    tile) for one spectrum and >= 10 tiles of height <= 64, or per tile for Z
+    a multiple of 5 up to 80 with 1 <= zpad <= Z - 1, else (or with the direct
+    form forced) the direct sum (outputs and padded planes in blocks of 8);
+    8 flops a complex FMA."""
     import sys
     import types
     sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
     import bench
 
     def dec(Z, zpad, P, npsf, nt):
-        return types.SimpleNamespace(tile_height=Z, Zp=Z + 2 * zpad, P=P, H=P // 2 + 1, z_operator=object(),
-                                     psf_fft=np.zeros((npsf, 1)), n_tiles=lambda shape: nt)
+        return types.SimpleNamespace(tile_height=Z, zpad=zpad, Zp=Z + 2 * zpad, P=P, H=P // 2 + 1,
+                                     z_operator=object(), psf_fft=np.zeros((npsf, 1)), n_tiles=lambda shape: nt)
 
     w = dict(Z=50, X=2048, Y=2048, colours=3)
     s = dict(dec_h=dec(50, 49, 678, 1, 25), dec_d=dec(50, 24, 678, 1, 25))
     assert bench.zpass_flops(w, s) == 4 * 25 * 678 * 340 * 2500 * 8.0
     w = dict(Z=40, X=3000, Y=3000, colours=1)
     s = dict(dec_h=dec(40, 39, 478, 100, 100), dec_d=None)
-    assert bench.zpass_flops(w, s) == 100 * 478 * 240 * 40 * 120 * 8.0
+    assert bench.zpass_flops(w, s) == 100 * 478 * 240 * 1600 * 8.0
+    assert bench.zpass_flops(w, s, "direct") == 100 * 478 * 240 * 40 * 120 * 8.0
+    w = dict(Z=42, X=3000, Y=3000, colours=1)
+    s = dict(dec_h=dec(42, 41, 478, 100, 100), dec_d=None)
+    assert bench.zpass_flops(w, s) == 100 * 478 * 240 * 48 * 128 * 8.0
 
 
 def test_z_operator_register_rings_restate_the_matrix():
@@ -312,6 +318,10 @@ def test_z_operator_register_rings_restate_the_matrix():
                 segj.append(j)
                 segc.append(cls)
         assert len(segj) <= 6
+        if zpad == Z - 1 and Z >= 2:
+            # the fixed classes the per-tile kernel (csrc/zop_pt.cu) compiles
+            # in for zpad = Z - 1: column 0, columns 1 .. Z - 2, column Z - 1
+            assert (segj, segc) == (([0, 1, Z - 1], [1, 2, 0]) if Z > 2 else ([0, 1], [1, 0]))
 
         def at(i):
             if i >= zrow:
