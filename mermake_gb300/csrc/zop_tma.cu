@@ -36,6 +36,7 @@
 namespace {
 
 constexpr int kPB = 4;      // frequencies per group (32 bytes of a plane row)
+constexpr int kLPR = kPB / 2;  // 16-byte pieces of a row (copying lanes per row)
 constexpr int kTI = 5;      // rows of a thread, and the unroll of the column loop
 constexpr int kTT = 5;      // tiles of a thread
 constexpr int kThreadsMax = 256;
@@ -192,10 +193,15 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA, c
             zth_item(a, item, grp, own0, box0);
             if (lane == 0) item_of[buf] = make_int3(grp, own0, box0);  // published by the arrives below
             const int p0 = grp * kPB;
-            const int nchunk = 2 * Z * a.ntc;  // 16-byte halves of the box's rows
-            for (int k = lane; k < nchunk; k += 32) {
-                const int row = k >> 1;  // (tile - box0) * Z + plane
-                cp_async16(b + (size_t)k * 16, S + ((long long)box0 * Z + row) * a.plane + p0 + 2 * (k & 1));
+            const int nchunk = kLPR * Z * a.ntc;  // 16-byte pieces of the box's rows
+            // a piece past the plane (the last group of a plane of 2 mod 4
+            // frequencies) is not copied: its results are not stored
+            const long long pc = p0 + 2 * (lane % kLPR);
+            if (pc < a.plane) {
+                for (int k = lane; k < nchunk; k += 32) {
+                    const int row = k / kLPR;  // (tile - box0) * Z + plane
+                    cp_async16(b + (size_t)k * 16, S + ((long long)box0 * Z + row) * a.plane + pc);
+                }
             }
             cp_async_arrive(&full[buf]);
             if (lane == 0) {

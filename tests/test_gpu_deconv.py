@@ -190,7 +190,7 @@ def test_apply_stitch_order_matches_reference(dc, npsf):
 
 @pytest.mark.parametrize("Z,zpad,ts,ov", [(13, 12, 10, 3), (64, 63, 10, 3), (50, 24, 30, 9), (7, 2, 15, 3),
                                           (5, 9, 10, 3), (50, 49, 10, 3), (30, 14, 12, 4), (80, 79, 10, 3),
-                                          (60, 29, 10, 3), (100, 99, 8, 2)])
+                                          (60, 29, 10, 3), (100, 99, 8, 2), (50, 49, 11, 4)])
 def test_z_operator_matches_padded_transforms(dc, Z, zpad, ts, ov):
     """The z operator (one Z x Z matrix per frequency, from the z kernel)
     against the FFT z pass over the padded depth, on whole batches: Z not a
@@ -202,7 +202,8 @@ def test_z_operator_matches_padded_transforms(dc, Z, zpad, ts, ov):
     in registers and TMA-staged operands (csrc/zop_tma.cu), whose 25 tiles
     are split into two chunks of 13 at Z = 80 and 100 (the second chunk's box
     reaching back one tile into the first; at Z = 60 the shared-memory form
-    takes the batch instead)."""
+    takes the batch instead), also on a plane of 190 frequencies (P = 19: the
+    last group of four half outside the plane)."""
     rng = np.random.default_rng(Z)
     X = Y = 5 * ts
     img = rng.integers(100, 5000, (Z, X, Y)).astype(np.uint16)
