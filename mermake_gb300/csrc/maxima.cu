@@ -279,6 +279,8 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
     // a raw value with |x| <= lo is below the threshold after x -> x / div
     // (either sign): its quotient is not computed
     const bool skip_small = t.div > 0.f && th > 0.f;
+    // the two-sign pass with th >= 0 (not NaN): one queue round per voxel
+    const bool excl = both && th >= 0.f;
     const float lo = skip_small ? th * t.div * (1.f - 0x1p-18f) : 0.f;
     unsigned *my_k = qk[warp];
     int *my_y = qy[warp];
@@ -308,6 +310,28 @@ k_maxima(Vols V, float th, int delta, Xform t, uint2 *__restrict__ cand, unsigne
                 const float v = skip_small && fabsf(vals[k]) <= lo ? 0.f : xf(vals[k], t);
                 const float vl = __shfl_up_sync(0xffffffffu, v, 1), vr = __shfl_down_sync(0xffffffffu, v, 1);
                 const bool hasl = delta > 0 && lane > 0 && y - 1 < yhi, hasr = delta > 0 && lane < 31 && y + 1 < yhi;
+                if (excl) {
+                    // both signs in one queue round: with th >= 0 a voxel
+                    // other than NaN is above the threshold in one sign at
+                    // most (a round with a lane above it in both takes the
+                    // two-round path below)
+                    const bool lo0 = (hasl && v < vl) || (hasr && v < vr);
+                    const bool lo1 = (hasl && -v < -vl) || (hasr && -v < -vr);
+                    const bool up0 = y < yhi && !(v <= th) && !lo0;
+                    const bool up1 = y < yhi && !(-v <= th) && !lo1;
+                    if (!__any_sync(0xffffffffu, up0 && up1)) {
+                        const bool up = up0 || up1;
+                        const unsigned m = __ballot_sync(0xffffffffu, up);
+                        if (up) {
+                            const int at = qn + __popc(m & ((1u << lane) - 1));
+                            my_k[at] = key;
+                            my_y[at] = y | ((int)up1 << 30);
+                            my_v[at] = vals[k];
+                        }
+                        qn += __popc(m);
+                        continue;
+                    }
+                }
                 for (int sgn = 0; sgn < (both ? 2 : 1); ++sgn) {
                     const float sv = sgn ? -v : v;
                     const bool lower = (hasl && sv < (sgn ? -vl : vl)) || (hasr && sv < (sgn ? -vr : vr));
