@@ -82,10 +82,12 @@ enum { MM_BLUR_AUTO = 0, MM_BLUR_EXACT = 1, MM_BLUR_SPECTRAL = 2 };
 /* MM_OPT_ZFORM selects how the z step of tile_wise (padding by reflection,
  * transforms over Zp, times W, crop; mermake/deconvolver.py:139-157) runs:
  *   MM_ZFORM_AUTO (default): the first form below that the batch qualifies for
- *     (the two matrix forms from batches of 10 tiles);
+ *     (over one shared spectrum, the matrix forms from batches of 10 tiles);
  *   MM_ZFORM_REGISTERS: one Z x Z matrix per frequency, formed in registers
- *     from the z kernel (one spectrum, Z a multiple of 5, 1 <= zpad <= Z - 1,
- *     up to 30 tiles), operands staged by TMA;
+ *     from the z kernel (Z a multiple of 5, 1 <= zpad <= Z - 1): over one
+ *     spectrum shared by the batch, operands staged by TMA; or, with a
+ *     spectrum per tile or a batch below 10 tiles, each tile's matrix from its
+ *     own z kernel (Z <= 80);
  *   MM_ZFORM_SHARED: the same matrix summed into shared memory (one spectrum,
  *     Z <= 64, at most four copies of a plane);
  *   MM_ZFORM_DIRECT: the direct sum over the padded planes per tile;
