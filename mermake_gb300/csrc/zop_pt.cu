@@ -36,6 +36,7 @@ constexpr int kTI = 5;     // rows of a thread, the unroll of the column loop
 constexpr int kTiles = 5;  // tiles per item at most
 constexpr int kMaxBuf = 4;
 constexpr size_t kSmemMax = 112 * 1024;
+constexpr int kFullTiles = 1;  // tiles per item of the zpad = Z - 1 variant
 constexpr unsigned kWaitPolls = 1u << 24;
 
 __device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
@@ -129,6 +130,23 @@ __device__ __forceinline__ void reload(Rings &R, const float2 *W, int i0, int j,
     for (int q = 0; q < kTI - 1; ++q) R.rH[(q + U) % kTI] = W[(i0 + j + q + hrow) * PB];
 }
 
+// a column of the class with both reflections, its reflected value summed
+// from the two kernel rows (kb: w[0], ko: w[-(2Z-2)])
+template <int PB, int U>
+__device__ __forceinline__ void col2(Rings &R, const float2 *W, const float2 *xr, int i0, int j, int kb, int ko) {
+    R.rT[(kTI - U) % kTI] = W[(i0 - j + kb) * PB];
+    const int h = i0 + j + kTI - 1;
+    R.rH[(U + kTI - 1) % kTI] = cadd(W[(h + kb) * PB], W[(h + ko) * PB]);
+    const float2 x = xr[(size_t)j * PB];
+#pragma unroll
+    for (int q = 0; q < kTI; ++q) R.acc[q] = cfma(cadd(R.rT[(q - U + kTI) % kTI], R.rH[(q + U) % kTI]), x, R.acc[q]);
+}
+template <int PB, int U>
+__device__ __forceinline__ void reload2(Rings &R, const float2 *W, int i0, int j, int kb, int ko) {
+#pragma unroll
+    for (int q = 0; q < kTI - 1; ++q) R.rH[(q + U) % kTI] = cadd(W[(i0 + j + q + kb) * PB], W[(i0 + j + q + ko) * PB]);
+}
+
 template <int ZC, bool FULL, int PB>
 __global__ void __launch_bounds__(kMaxCompute + 32 * kProd, 2)
 k_zpt_apply(float2 *__restrict__ S, const float2 *__restrict__ w, const ZptArgs a) {
@@ -155,8 +173,10 @@ k_zpt_apply(float2 *__restrict__ S, const float2 *__restrict__ w, const ZptArgs 
         // the zero rows, and the staged kernel rows that lie outside the
         // padded depth (as a TMA box of the (Zp, plane) kernel would fill
         // them): the same rows of every item, written once
-        float2 *zr = reinterpret_cast<float2 *>(smem + a.zoff);
-        for (int e = tid; e < (2 * Z + 3) * kPB; e += blockDim.x) zr[e] = make_float2(0.f, 0.f);
+        if (!FULL) {
+            float2 *zr = reinterpret_cast<float2 *>(smem + a.zoff);
+            for (int e = tid; e < (2 * Z + 3) * kPB; e += blockDim.x) zr[e] = make_float2(0.f, 0.f);
+        }
         for (int e = tid; e < a.nbuf * a.ntpi * a.wrows * kPB; e += blockDim.x) {
             const int r = (e / kPB) % a.wrows, s = r - kb;
             if (s < -a.Zp || s >= a.Zp) {
@@ -233,7 +253,7 @@ k_zpt_apply(float2 *__restrict__ S, const float2 *__restrict__ w, const ZptArgs 
         // it & 1.  Every warp has left item it - 2 (the region's last user)
         // once all have met on hdone for item it - 1.
         float2 *hb = reinterpret_cast<float2 *>(smem + a.hoff + (it & 1) * a.hbytes);
-        {
+        if (!FULL) {
             const float2 *wb = reinterpret_cast<const float2 *>(b + a.xbytes);
             for (int t2 = 0; t2 < ntl; ++t2) {
                 const float2 *wt = wb + (size_t)t2 * a.wrows * kPB;
@@ -266,26 +286,27 @@ k_zpt_apply(float2 *__restrict__ S, const float2 *__restrict__ w, const ZptArgs 
             const float2 *Wp = W + p;
             if (FULL) {
                 // zpad = Z - 1: column 0 takes w[i + j - 2Z + 2], columns
-                // 1 .. Z - 2 hB[i + j], column Z - 1 w[i + j]
+                // 1 .. Z - 2 the sum w[i + j] + w[i + j - 2Z + 2] (two loads
+                // and an add per column), column Z - 1 w[i + j]
                 ring_start<PB>(R, Wp, i0, kb, ko);
                 col<PB, 0>(R, Wp, xr, i0, 0, kb, ko);
-                reload<PB, 1>(R, Wp, i0, 1, hrowB);
-                col<PB, 1>(R, Wp, xr, i0, 1, kb, hrowB);
-                col<PB, 2>(R, Wp, xr, i0, 2, kb, hrowB);
-                col<PB, 3>(R, Wp, xr, i0, 3, kb, hrowB);
-                col<PB, 4>(R, Wp, xr, i0, 4, kb, hrowB);
+                reload2<PB, 1>(R, Wp, i0, 1, kb, ko);
+                col2<PB, 1>(R, Wp, xr, i0, 1, kb, ko);
+                col2<PB, 2>(R, Wp, xr, i0, 2, kb, ko);
+                col2<PB, 3>(R, Wp, xr, i0, 3, kb, ko);
+                col2<PB, 4>(R, Wp, xr, i0, 4, kb, ko);
                 for (int j0 = kTI; j0 < Z - kTI; j0 += kTI) {
-                    col<PB, 0>(R, Wp, xr, i0, j0, kb, hrowB);
-                    col<PB, 1>(R, Wp, xr, i0, j0 + 1, kb, hrowB);
-                    col<PB, 2>(R, Wp, xr, i0, j0 + 2, kb, hrowB);
-                    col<PB, 3>(R, Wp, xr, i0, j0 + 3, kb, hrowB);
-                    col<PB, 4>(R, Wp, xr, i0, j0 + 4, kb, hrowB);
+                    col2<PB, 0>(R, Wp, xr, i0, j0, kb, ko);
+                    col2<PB, 1>(R, Wp, xr, i0, j0 + 1, kb, ko);
+                    col2<PB, 2>(R, Wp, xr, i0, j0 + 2, kb, ko);
+                    col2<PB, 3>(R, Wp, xr, i0, j0 + 3, kb, ko);
+                    col2<PB, 4>(R, Wp, xr, i0, j0 + 4, kb, ko);
                 }
                 const int j0 = Z - kTI;
-                col<PB, 0>(R, Wp, xr, i0, j0, kb, hrowB);
-                col<PB, 1>(R, Wp, xr, i0, j0 + 1, kb, hrowB);
-                col<PB, 2>(R, Wp, xr, i0, j0 + 2, kb, hrowB);
-                col<PB, 3>(R, Wp, xr, i0, j0 + 3, kb, hrowB);
+                col2<PB, 0>(R, Wp, xr, i0, j0, kb, ko);
+                col2<PB, 1>(R, Wp, xr, i0, j0 + 1, kb, ko);
+                col2<PB, 2>(R, Wp, xr, i0, j0 + 2, kb, ko);
+                col2<PB, 3>(R, Wp, xr, i0, j0 + 3, kb, ko);
                 reload<PB, 4>(R, Wp, i0, j0 + 4, kb);
                 col<PB, 4>(R, Wp, xr, i0, j0 + 4, kb, kb);
             } else {
@@ -338,25 +359,43 @@ size_t zpt_bufstride(int Z, int ntpi, int pb, unsigned *xbytes) {
 size_t zpt_hbytes(int Z, int ntpi, int pb) {
     return ((size_t)ntpi * (2 * Z - 1) * pb * sizeof(float2) + 127) & ~(size_t)127;
 }
-size_t zpt_smem(int Z, int ntpi, int nbuf, int pb) {
-    return nbuf * zpt_bufstride(Z, ntpi, pb, nullptr) + 2 * zpt_hbytes(Z, ntpi, pb) + zpt_zero_bytes(Z, pb);
+// shared memory of a CTA: the buffers, and for the generic variant the two hB
+// regions and the zero rows (the variant for zpad = Z - 1 sums the two
+// reflections as it reads them and has no column without one)
+size_t zpt_smem(int Z, int ntpi, int nbuf, int pb, bool full) {
+    const size_t bufs = nbuf * zpt_bufstride(Z, ntpi, pb, nullptr);
+    return full ? bufs : bufs + 2 * zpt_hbytes(Z, ntpi, pb) + zpt_zero_bytes(Z, pb);
 }
-// Frequencies per item (pb), tiles per item and buffers: the widest rows of
-// which one tile fits two buffers of two CTAs per SM, with as many tiles as
-// fit (0: none).  The operands are rows of pb x 8 bytes at the spectrum's
-// plane stride, and wider rows read DRAM faster: on 100 tiles of Z = 40,
-// P = 478 (a PSF per tile) the z step took 8.0 ms with rows of 32 bytes (five
-// tiles per item), 7.1 ms with 64 (three) and 6.65 ms with 128 (one); the
-// copies alone took 6.2 ms at 32 bytes.  Three or four buffers, or three CTAs
-// per SM, changed nothing.
-int zpt_config(int Z, int *nbuf, int *pb) {
-    *nbuf = 2;
-    for (int w = 16; w >= 8; w /= 2)
+// zpad = Z - 1 (Z >= 10): the column classes at compile time
+bool zpt_full(int Z, int zpad) { return zpad == Z - 1 && Z >= 2 * kTI; }
+// Frequencies per item (pb), tiles per item and buffers, for two CTAs per SM
+// (0 tiles: none fit).  The operands are rows of pb x 8 bytes at the
+// spectrum's plane stride, and wider rows read DRAM faster: on 100 tiles of
+// Z = 40, P = 478 (a PSF per tile) the z step took 8.0 ms with rows of 32
+// bytes (five tiles per item), 7.1 ms with 64 (three) and 6.68 ms with 128
+// (one); the copies alone took 6.2 ms at 32 bytes.  So pb is 16 where one
+// tile fits two buffers, else 8.  The variant for zpad = Z - 1 then takes one
+// tile per item and two buffers: small CTAs, four per SM at Z = 40, 5.39 ms
+// on that workload, against 5.81 ms with four buffers (two CTAs per SM) and
+// 6.68 ms for the generic variant's hB rows and per-item barrier.  The
+// generic variant takes two buffers of as many tiles as fit.
+int zpt_config(int Z, bool full, int *nbuf, int *pb) {
+    for (int w = 16; w >= 8; w /= 2) {
+        if (full) {
+            if (zpt_smem(Z, kFullTiles, 2, w, true) <= kSmemMax && w * (Z / kTI) * kFullTiles <= kMaxCompute) {
+                *nbuf = 2;
+                *pb = w;
+                return kFullTiles;
+            }
+            continue;
+        }
         for (int n = kTiles; n >= 1; --n)
-            if (zpt_smem(Z, n, 2, w) <= kSmemMax && w * (Z / kTI) * n <= kMaxCompute) {
+            if (zpt_smem(Z, n, 2, w, false) <= kSmemMax && w * (Z / kTI) * n <= kMaxCompute) {
+                *nbuf = 2;
                 *pb = w;
                 return n;
             }
+    }
     return 0;
 }
 
@@ -365,7 +404,7 @@ int zpt_config(int Z, int *nbuf, int *pb) {
 int mm_zpt_supported(int Z, int zpad, int nt, long long plane) {
     if (Z < kTI || Z % kTI != 0 || Z > kMaxZ || zpad < 1 || zpad > Z - 1 || nt < 1 || plane % 2 != 0) return 0;
     int nb, pb;
-    return zpt_config(Z, &nb, &pb) > 0;
+    return zpt_config(Z, zpt_full(Z, zpad), &nb, &pb) > 0;
 }
 
 int mm_launch_zpt_apply(float2 *S, const float2 *w, long long wstride, int Z, int zpad, int Zp, long long plane,
@@ -381,8 +420,9 @@ int mm_launch_zpt_apply(float2 *S, const float2 *w, long long wstride, int Z, in
     a.npsf = npsf;
     a.plane = plane;
     a.wstride = wstride;
+    const bool full = zpt_full(Z, zpad);
     int pb = 0;
-    a.ntpi = zpt_config(Z, &a.nbuf, &pb);
+    a.ntpi = zpt_config(Z, full, &a.nbuf, &pb);
     a.ngroups = (int)((plane + pb - 1) / pb);
     const long long nitems = (long long)a.ngroups * ((nt + a.ntpi - 1) / a.ntpi);
     MM_REQUIRE(nitems < (1LL << 31), "z operator: too many items");
@@ -407,10 +447,8 @@ int mm_launch_zpt_apply(float2 *S, const float2 *w, long long wstride, int Z, in
     }
     a.fresp = fresp;
     a.err = err;
-    const size_t sm = zpt_smem(Z, a.ntpi, a.nbuf, pb);
+    const size_t sm = zpt_smem(Z, a.ntpi, a.nbuf, pb, full);
     const int threads = zpt_block(Z, a.ntpi, pb);
-    // zpad = Z - 1 (Z >= 10): the column classes at compile time
-    const bool full = zpad == Z - 1 && Z >= 2 * kTI;
     const void *fn;
     if (pb == 16)
         fn = !full     ? (const void *)k_zpt_apply<0, false, 16>
