@@ -21,10 +21,11 @@
 // both boxes land on 128-byte boundaries as tiled TMA requires), double
 // buffered.  The persistent CTAs take groups of kPB consecutive frequencies.
 // A producer warp issues each group's copies once the buffer is free; the
-// compute warps wait only for their buffer to fill (its "full" mbarrier
-// completes with the copies: 32 cp.async arrivals and the TMA bytes) and
-// release it with one arrive per warp on its "empty" mbarrier, so no CTA
-// barrier separates the groups.  Every wait is bounded: a thread that gives up
+// compute warps take the group's work in warp-sized units from a shared
+// counter, wait only for their buffer to fill (its "full" mbarrier completes
+// with the copies: 32 cp.async arrivals and the TMA bytes) and release it with
+// one arrive per unit on its "empty" mbarrier, so no CTA barrier separates the
+// groups.  Every wait is bounded: a thread that gives up
 // records the failure in *err and returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
@@ -138,13 +139,10 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA, c
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ __align__(8) uint64_t full[2], empty[2], wfull[2];
     __shared__ int3 item_of[2];  // (group, first owned tile, box start) of each buffer's item
+    __shared__ unsigned unit_next;  // the next (item, warp unit) a compute warp takes
     const int Z = ZC > 0 ? ZC : a.Z;
     const int nig = Z / kTI;
     const int tid = threadIdx.x;
-    const int p = tid % kPB;
-    const int r = tid / kPB;
-    const int ig = r % nig, tg = r / nig;
-    const int i0 = ig * kTI, tl0 = tg * kTT;  // first row, first tile of the chunk's box
     const int kb = a.kA;              // row of w[0] in the staged kernel rows
     const int ko = kb - (2 * Z - 2);  // row of w[-(2Z-2)], the lowest index the rings read
 
@@ -165,6 +163,7 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA, c
             mbar_init(&empty[b], ncw);
             mbar_init(&wfull[b], 1);
         }
+        unit_next = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     {
@@ -229,12 +228,33 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA, c
         return;
     }
 
-    for (int item = blockIdx.x, it = 0; item < a.nitems; item += gridDim.x, ++it) {
+    // An item's threads (kPB x Z/kTI x ntg) come in ncw warp units: unit u
+    // is threads 32u .. 32u + 31 of the item.  The compute warps take the
+    // units in order from a shared counter, so a warp on a less loaded SM
+    // sub-partition takes more of them (ncw warps of two CTAs do not divide
+    // evenly over four sub-partitions).  A warp takes a unit of item it only
+    // after units of items it - 1 and before (all taken, each warp holding one
+    // at a time), so buffer it & 1's previous item (it - 2) is at most being
+    // released: waiting for that release first makes the "full" parity below
+    // this item's.
+    for (;;) {
+        unsigned sq = 0;
+        if (lane == 0) sq = atomicAdd(&unit_next, 1u);
+        sq = __shfl_sync(0xffffffffu, sq, 0);
+        const int it = (int)(sq / (unsigned)ncw), unit = (int)(sq - (unsigned)it * (unsigned)ncw);
+        const long long item_ll = blockIdx.x + (long long)it * gridDim.x;
+        if (item_ll >= a.nitems) break;
+        const int item = (int)item_ll;
         const int buf = it & 1;
-        if (!mbar_wait(&full[buf], (it >> 1) & 1)) {
+        if ((it >= 2 && !mbar_wait(&empty[buf], ((it - 2) >> 1) & 1)) || !mbar_wait(&full[buf], (it >> 1) & 1)) {
             atomicOr(a.err, 1u);
             return;
         }
+        const int vt = unit * 32 + lane;
+        const int p = vt % kPB;
+        const int r = vt / kPB;
+        const int ig = r % nig, tg = r / nig;
+        const int i0 = ig * kTI, tl0 = tg * kTT;  // first row, first tile of the chunk's box
         const float2 *X = reinterpret_cast<const float2 *>(smem + (size_t)buf * a.bufstride);
         const float2 *W = reinterpret_cast<const float2 *>(smem + (size_t)buf * a.bufstride + a.woff);
         if (tg < a.ntg) {
