@@ -479,18 +479,24 @@ def gpu_arm(args, rank, world, local):
         io = {"h2d": 0, "d2h": 0}
         if args.form == "batched":
             # the public FovRunner: FOV k+1's channels are copied from pinned host
-            # memory on a side stream while FOV k computes; every step copies one
-            # FOV and computes one FOV, and the timed region ends after the last
-            # copy it issued
+            # memory on a side stream while FOV k computes, and FOV k is launched
+            # before FOV k - 1's rows are collected, so the GPU has work queued
+            # while the host reads results.  Every step copies one FOV, launches
+            # one and reads one back; the timed region ends after the last FOV
+            # it launched and the last copy it issued.
             runner = pipeline.FovRunner(s["dec_h"], s["dec_d"], w["hyb"], w.get("dapi_args"), batch=args.batch)
             state = {}
 
             def e2e_step():
-                t = state.pop("ticket", None) or runner.submit(host_dapi, host_ch)
-                state["ticket"] = runner.submit(host_dapi, host_ch)
-                p, m, rows = runner.run(t, s["flats"])
+                t = state.pop("next", None) or runner.submit(host_dapi, host_ch)
+                pend = runner.launch(t, s["flats"])
+                prev = state.pop("pending", None)
+                if prev is not None:
+                    p, m, rows = runner.collect(prev)
+                    io["d2h"] = sum(a.nbytes for a in [p, m] + rows if a is not None)
+                state["pending"] = pend
+                state["next"] = runner.submit(host_dapi, host_ch)
                 io["h2d"] = runner.h2d_bytes
-                io["d2h"] = sum(a.nbytes for a in [p, m] + rows if a is not None)
 
             for _ in range(max(args.warmup, 1)):
                 e2e_step()
@@ -506,6 +512,7 @@ def gpu_arm(args, rank, world, local):
             torch.cuda.synchronize()
             barrier()
             e_ms = e0.elapsed_time(e1)
+            runner.collect(state.pop("pending"))
         else:
             if args.form == "graph":  # the graph reads the channels it was captured on
                 dev_ch, dev_dapi = s["chans"], s["dapi"]

@@ -161,6 +161,12 @@ class FovRunner:
     a ticket; ``run(ticket, flats)`` waits for that FOV's copies channel by
     channel and returns ``(Xh_plus, Xh_minus, [Xh per colour])`` as host
     arrays.  Submit FOV k+1 before running FOV k to overlap them.
+
+    ``run`` is ``collect(launch(ticket, flats))``: ``launch`` enqueues the FOV
+    without waiting for anything, ``collect`` makes its one synchronisation
+    and reads the rows back.  Launching FOV k before collecting FOV k - 1
+    keeps the GPU busy while the host reads results; a slot is free for the
+    next ``submit`` once its FOV has been collected.
     """
 
     def __init__(self, dec_hyb, dec_dapi=None, hyb_args=None, dapi_args=None, batch=0):
@@ -169,6 +175,7 @@ class FovRunner:
         self.dapi_args = dict(dapi_args or {})
         self.batch = batch
         self.copy_stream = torch.cuda.Stream()
+        self.read_stream = torch.cuda.Stream()  # collect's reads, behind only the FOV read
         self._slots = [dict(), dict()]
         self._next = 0
         self._buffer = None
@@ -209,7 +216,13 @@ class FovRunner:
         device), then one read of all counts and the rows.  An output that did
         not fit its rows (or candidate list) is run again by the synchronous
         driver, which resizes; later FOVs get rows sized from its count."""
+        return self.collect(self.launch(ticket, flats, dapi_flat))
+
+    def launch(self, ticket, flats=None, dapi_flat=None):
+        """Enqueues the FOV of ``ticket`` on the current stream (no host
+        synchronisation) and returns the handle ``collect`` takes."""
         cur = torch.cuda.current_stream()
+        slot = ticket["slot"]
         evs, devs = list(ticket["events"]), list(ticket["dev"])
         n = len(devs) - (1 if ticket["has_dapi"] else 0)
         flats = list(flats) if flats is not None else [None] * n
@@ -220,7 +233,6 @@ class FovRunner:
         sp = _lib.stream_ptr(cur)
         counts = torch.zeros(3 + 2 * n, dtype=torch.int32, device=dev)
         cbase = counts.data_ptr()
-        out_plus = out_minus = None
         dapi_img = dflat = None
         if ticket["has_dapi"]:
             d, a = self.dec_dapi, _settings(self.dapi_args)
@@ -231,9 +243,9 @@ class FovRunner:
                 self._buffer = torch.empty(shape, dtype=torch.float32, device=dev)
             cap_p = _capacity(d, ("dapi+", Z, X, Y), 1 << 16)
             cap_m = _capacity(d, ("dapi-", Z, X, Y), 1 << 16)
-            plus = self._rows("plus", cap_p, dev)
-            minus = self._rows("minus", cap_m, dev)
-            rms = self._rows("rms", 1, dev)
+            plus = self._rows(("plus", slot), cap_p, dev)
+            minus = self._rows(("minus", slot), cap_m, dev)
+            rms = self._rows(("rms", slot), 1, dev)
             bd = tune.batch_for(d, shape, dapi=True) if self.batch == 0 else self.batch
             _lib.check(L.mm_dapi_spots_async(
                 ctx, _lib.ptr(dapi_img), Z, X, Y, dapi_img.stride(0), dapi_img.stride(1), _lib.ptr(dflat),
@@ -249,7 +261,7 @@ class FovRunner:
             cur.wait_event(ev)
             fl = _flat(f, shape)
             fls.append(fl)
-            r = self._rows(("hyb", c), cap, dev)
+            r = self._rows(("hyb", c, slot), cap, dev)
             rows.append(r)
             _lib.check(L.mm_hyb_spots_async(
                 ctx, _lib.ptr(img), Z, X, Y, img.stride(0), img.stride(1), _lib.ptr(fl),
@@ -257,28 +269,56 @@ class FovRunner:
                 _lib.ptr(d.z_operator), d.tile_size, d.zpad, d.overlap, a["br"], a["th"], a["delta"], a["dfit"],
                 a["sz"], a["sxy"], max(int(bh), 0), _lib.ptr(r), cap, _lib._vp(cbase + 4 * (3 + 2 * c)),
                 _lib._vp(cbase + 4 * (4 + 2 * c)), sp))
-        cnt = counts.cpu().tolist()  # the FOV's one synchronisation
+        # the slot's images are free for the next submit once these kernels
+        # have run (collect moves the mark past any rerun that reads them)
+        used = torch.cuda.Event()
+        used.record(cur)
+        self._slots[slot]["free"] = used
+        return dict(ticket=ticket, counts=counts, shape=shape, n=n, devs=devs, fls=fls, rows=rows, used=used,
+                    dapi=(dapi_img, dapi_flat, plus, minus, cap_p, cap_m) if ticket["has_dapi"] else None, cap=cap)
+
+    def collect(self, h):
+        """The rows of a launched FOV as host arrays, after its one
+        synchronisation (and the reruns of outputs that did not fit)."""
+        cur = torch.cuda.current_stream()
+        ticket, n, devs, fls, rows, cap = h["ticket"], h["n"], h["devs"], h["fls"], h["rows"], h["cap"]
+        Z, X, Y = h["shape"]
+        d = self.dec_hyb
+        out_plus = out_minus = None
+        reran = False
+        # the reads go on a stream of their own, behind this FOV's kernels only,
+        # so a FOV launched after it keeps the GPU busy meanwhile
+        rs = self.read_stream
+        rs.wait_event(h["used"])
+        with torch.cuda.stream(rs):
+            cnt = h["counts"].cpu().tolist()  # the FOV's one synchronisation
         if ticket["has_dapi"]:
+            dapi_img, dapi_flat, plus, minus, cap_p, cap_m = h["dapi"]
             dd = self.dec_dapi
             _seen(dd, ("dapi+", Z, X, Y), cnt[0])
             _seen(dd, ("dapi-", Z, X, Y), cnt[1])
             if cnt[2] or cnt[0] > cap_p or cnt[1] > cap_m:
+                reran = True
                 p, m, self._buffer, _ = dapi_spots(dd, dapi_img, dapi_flat, buffer=self._buffer, batch=self.batch,
                                                    **self.dapi_args)
+                out_plus, out_minus = p.cpu().numpy(), m.cpu().numpy()
             else:
-                p, m = plus[:cnt[0]], minus[:cnt[1]]
-            out_plus, out_minus = p.cpu().numpy(), m.cpu().numpy()
+                with torch.cuda.stream(rs):
+                    out_plus, out_minus = plus[:cnt[0]].cpu().numpy(), minus[:cnt[1]].cpu().numpy()
         out = []
         for c in range(n):
             nc = cnt[3 + 2 * c]
             _seen(d, ("hyb", Z, X, Y), nc)
             if cnt[4 + 2 * c] or nc > cap:
+                reran = True
                 out.append(hyb_spots(d, devs[c], fls[c], batch=self.batch, **self.hyb_args).cpu().numpy())
             else:
-                out.append(rows[c][:nc].cpu().numpy())
-        done = torch.cuda.Event()
-        done.record(cur)
-        self._slots[ticket["slot"]]["free"] = done
+                with torch.cuda.stream(rs):
+                    out.append(rows[c][:nc].cpu().numpy())
+        if reran:
+            done = torch.cuda.Event()
+            done.record(cur)
+            self._slots[ticket["slot"]]["free"] = done
         return out_plus, out_minus, out
 
     def _rows(self, key, cap, dev):

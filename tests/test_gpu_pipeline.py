@@ -198,6 +198,51 @@ def test_fov_runner_matches_direct_calls(mm):
     assert runner.h2d_bytes == 3 * Z * X * Y * 2
 
 
+@pytest.mark.parametrize("small_rows", [False, True])
+def test_fov_runner_launch_before_collect(mm, monkeypatch, small_rows):
+    """FovRunner pipelined: FOV k is launched before FOV k - 1 is collected
+    and FOV k + 1 submitted after it, the order the bench's e2e loop uses.
+    Two different FOVs alternate over the two slots, so rows or images taken
+    from the wrong slot would show; with row buffers of 8 every output is
+    rerun by the synchronous driver while the next FOV is already queued."""
+    Z, X, Y = 12, 170, 150
+    fovs, want = [], []
+    imgs = [hyb_case(mm, seed=s, Z=Z, X=X, Y=Y) for s in (4, 5)]
+    psf = imgs[0][2]
+    dh = mm["dc"].Deconvolver(psf, (Z, X, Y), zpad=Z - 1, **HYB)
+    dd = mm["dc"].Deconvolver(psf, (Z, X, Y), zpad=(Z - 1) // 2, **DAPI)
+    flats = [torch.from_numpy(f).cuda() for _, f, _ in imgs]
+    for k in range(2):
+        dapi = mm["synth"].dapi_stack(Z, X, Y, 6 + k, n_nuclei=10 + 3 * k, radii=(3.0, 12.0, 12.0))
+        cols = [imgs[k][0], imgs[1 - k][0]]
+        fl = [flats[k], flats[1 - k]]
+        p, m, _, _ = mm["pl"].dapi_spots(dd, dapi.cuda(), None, **DAPI)
+        rows = [mm["pl"].hyb_spots(dh, c.cuda(), f, **HYB) for c, f in zip(cols, fl)]
+        want.append((p.cpu().numpy(), m.cpu().numpy(), [r.cpu().numpy() for r in rows]))
+        fovs.append((dapi.cpu().pin_memory(), [c.cpu().pin_memory() for c in cols], fl))
+    if small_rows:
+        assert min(len(w[0]) for w in want) > 8 and min(len(r) for w in want for r in w[2]) > 8
+        monkeypatch.setattr(mm["pl"], "_capacity", lambda dec, key, default: 8)
+    runner = mm["pl"].FovRunner(dh, dd, HYB, DAPI)
+    seq = [0, 1, 0, 1, 1, 0]
+    nxt, pending, got = runner.submit(fovs[seq[0]][0], fovs[seq[0]][1]), None, []
+    for k, f in enumerate(seq):
+        h = (runner.launch(nxt, fovs[f][2]), f)
+        if pending is not None:
+            got.append((runner.collect(pending[0]), pending[1]))
+        pending = h
+        if k + 1 < len(seq):
+            nxt = runner.submit(fovs[seq[k + 1]][0], fovs[seq[k + 1]][1])
+    got.append((runner.collect(pending[0]), pending[1]))
+    assert [f for _, f in got] == seq
+    for (p, m, rows), f in got:
+        wp, wm, wr = want[f]
+        np.testing.assert_array_equal(ck.sort_rows(p), ck.sort_rows(wp))
+        np.testing.assert_array_equal(ck.sort_rows(m), ck.sort_rows(wm))
+        for g, w in zip(rows, wr):
+            np.testing.assert_array_equal(ck.sort_rows(g), ck.sort_rows(w))
+
+
 def test_fov_runner_reruns_outputs_that_overflow(mm, monkeypatch):
     """FovRunner enqueues a FOV with the asynchronous drivers and reads all
     counts once; an output whose rows did not fit (here every output, with
