@@ -356,3 +356,70 @@ def test_z_operator_register_rings_restate_the_matrix():
                     for q in range(5):
                         got[i0 + q, j] = rT[(q - u + 5) % 5] + rH[(q + u) % 5]
         np.testing.assert_allclose(got, M, rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("Z", [10, 15, 40, 50, 80])
+def test_per_tile_z_operator_full_variant_restates_the_matrix(Z):
+    """The per-tile z operator's variant for zpad = Z - 1 (csrc/zop_pt.cu,
+    k_zpt_apply<., true, .>): its producer stages the tile's kernel rows
+    w[-kA .. 2Z - 2] by copying, in two linear runs, the rows
+    [max(kA - Zp, 0), kA) from w[r - kA + Zp] and [kA, min(kA + Zp, wrows))
+    from w[r - kA] (the rest are zero rows written once); column 0 takes the
+    reflection w[i + j - 2Z + 2], columns 1 .. Z - 2 the sum
+    w[i + j] + w[i + j - 2Z + 2] formed as the reflected ring is loaded (two
+    staged rows per value), column Z - 1 the reflection w[i + j], the class
+    changes at compile-time columns.  Restated with the kernel's ring slots
+    and staged rows against M built from the padding map; every read stays
+    inside the staged rows."""
+    zpad = Z - 1
+    Zp = Z + 2 * zpad
+    rng = np.random.default_rng(Z)
+    w = rng.standard_normal(Zp) + 1j * rng.standard_normal(Zp)
+    M = np.zeros((Z, Z), complex)
+    for z in range(Zp):
+        j = int(_map_z(z, Z, zpad, Zp))
+        if j >= 0:
+            for i in range(Z):
+                M[i, j] += w[(zpad + i - z) % Zp]
+    kA = (2 * Z - 2 + 3) & ~3
+    kb, ko = kA, kA - (2 * Z - 2)
+    wrows = kA + 2 * Z - 1
+    rlo, rhi = max(kb - Zp, 0), min(wrows, kb + Zp)
+    staged = np.full(wrows, np.nan, complex)
+    staged[:rlo] = 0
+    staged[rhi:] = 0
+    for r in range(rlo, kb):  # first run
+        staged[r] = w[r - kb + Zp]
+    for r in range(kb, rhi):  # second run
+        staged[r] = w[r - kb]
+    assert not np.isnan(staged).any()
+
+    def at(i):
+        assert 0 <= i < wrows, i
+        return staged[i]
+
+    got = np.zeros((Z, Z), complex)
+    for i0 in range(0, Z, 5):
+        rT, rH = [0j] * 5, [0j] * 5
+        for q in range(1, 5):  # ring_start, column 0's class (hrow = ko)
+            rT[q] = at(i0 + q + kb)
+        for q in range(4):
+            rH[q] = at(i0 + q + ko)
+
+        def col(j, u, rh):
+            rT[(5 - u) % 5] = at(i0 - j + kb)
+            rH[(u + 4) % 5] = rh(i0 + j + 4)
+            for q in range(5):
+                got[i0 + q, j] = rT[(q - u + 5) % 5] + rH[(q + u) % 5]
+
+        one = lambda h: at(h + ko)  # noqa: E731
+        two = lambda h: at(h + kb) + at(h + ko)  # noqa: E731
+        col(0, 0, one)
+        for q in range(4):  # reload2<1>
+            rH[(q + 1) % 5] = two(i0 + 1 + q)
+        for j in range(1, Z - 1):
+            col(j, j % 5, two)
+        for q in range(4):  # reload<4> from w[i + j]
+            rH[(q + 4) % 5] = at(i0 + Z - 1 + q + kb)
+        col(Z - 1, (Z - 1) % 5, lambda h: at(h + kb))
+    np.testing.assert_allclose(got, M, rtol=0, atol=1e-12)
