@@ -232,11 +232,12 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA, c
     // is threads 32u .. 32u + 31 of the item.  The compute warps take the
     // units in order from a shared counter, so a warp on a less loaded SM
     // sub-partition takes more of them (ncw warps of two CTAs do not divide
-    // evenly over four sub-partitions).  A warp takes a unit of item it only
-    // after units of items it - 1 and before (all taken, each warp holding one
-    // at a time), so buffer it & 1's previous item (it - 2) is at most being
-    // released: waiting for that release first makes the "full" parity below
-    // this item's.
+    // evenly over four sub-partitions).  The parity wait below passes on this
+    // item's own phase: to pass on item it - 2's, a warp would have to take a
+    // unit of item it while that item's buffer is unfilled.  The producer
+    // fills in order, so no unit of items it - 2 and it - 1 could have
+    // finished, and their 2 ncw units would occupy more warps than the CTA's
+    // ncw.
     for (;;) {
         unsigned sq = 0;
         if (lane == 0) sq = atomicAdd(&unit_next, 1u);
@@ -246,7 +247,7 @@ k_zth_apply(float2 *__restrict__ S, const __grid_constant__ CUtensorMap wmapA, c
         if (item_ll >= a.nitems) break;
         const int item = (int)item_ll;
         const int buf = it & 1;
-        if ((it >= 2 && !mbar_wait(&empty[buf], ((it - 2) >> 1) & 1)) || !mbar_wait(&full[buf], (it >> 1) & 1)) {
+        if (!mbar_wait(&full[buf], (it >> 1) & 1)) {
             atomicOr(a.err, 1u);
             return;
         }

@@ -423,3 +423,86 @@ def test_per_tile_z_operator_full_variant_restates_the_matrix(Z):
             rH[(q + 4) % 5] = at(i0 + Z - 1 + q + kb)
         col(Z - 1, (Z - 1) % 5, lambda h: at(h + kb))
     np.testing.assert_allclose(got, M, rtol=0, atol=1e-12)
+
+
+def _unit_protocol_run(rng, nwarps, nunits, nitems):
+    """One simulated run of the register z operator's warp-unit protocol
+    (csrc/zop_tma.cu): nwarps compute warps take units in order from a shared
+    counter (unit u of item it = sequence number it * nunits + u) and wait for
+    their buffer (it & 1) with an mbarrier parity wait, (it >> 1) & 1; the
+    producer fills item it once all units of item it - 2 have arrived on the
+    buffer's "empty" barrier.  A parity wait passes once the number of
+    completed phases P has P % 2 != parity.  Returns [] after a run whose
+    every wait passed on its own item's phase, else [(item, completed
+    phases)] of the first wait that did not."""
+    import heapq
+    full_done, empty_done, empty_cnt = [0, 0], [0, 0], [0, 0]
+    counter, t_now, ev = 0, 0.0, []
+    prod = {"it": 0, "busy": False}
+    done = set()
+    warps = ["grab"] * nwarps
+    for _ in range(200000):
+        if not prod["busy"] and prod["it"] < nitems:
+            it = prod["it"]
+            if it < 2 or empty_done[it & 1] % 2 != ((it - 2) >> 1) & 1:
+                prod["busy"] = True
+                heapq.heappush(ev, (t_now + float(rng.uniform(0.1, 3.0)), 0, it))
+        progress = False
+        for k in range(nwarps):
+            if warps[k] == "grab":
+                it, u = divmod(counter, nunits)
+                counter += 1
+                warps[k] = "done" if it >= nitems else ("wait", it, u)
+                progress = True
+            st = warps[k]
+            if isinstance(st, tuple) and st[0] == "wait":
+                _, it, u = st
+                b = it & 1
+                if full_done[b] % 2 != (it >> 1) & 1:
+                    if full_done[b] != (it >> 1) + 1:
+                        return [(it, full_done[b])]  # what follows runs on the wrong data
+                    assert (it, u) not in done
+                    warps[k] = ("run", it, u)
+                    heapq.heappush(ev, (t_now + float(rng.uniform(0.5, 2.0)), 1, k))
+                    progress = True
+        if all(w == "done" for w in warps) and prod["it"] >= nitems and not ev:
+            assert len(done) == nitems * nunits
+            return []
+        if not progress:
+            assert ev, "deadlock"
+            t_now, kind, pay = heapq.heappop(ev)
+            if kind == 0:
+                full_done[pay & 1] += 1
+                prod["busy"] = False
+                prod["it"] += 1
+            else:
+                _, it, u = warps[pay]
+                done.add((it, u))
+                empty_cnt[it & 1] += 1
+                if empty_cnt[it & 1] == nunits:
+                    empty_cnt[it & 1] = 0
+                    empty_done[it & 1] += 1
+                warps[pay] = "grab"
+    raise AssertionError("no end")
+
+
+def test_register_z_operator_warp_unit_protocol():
+    """The register z operator's compute warps take an item's warp units from
+    a shared counter and wait for their buffer with a parity wait only.  With
+    as many units per item as compute warps (the kernel: ncw of each), every
+    wait passes on its own item's phase, every unit runs once and nothing
+    deadlocks (random unit times and copy latencies).  A warp could pass on
+    an earlier phase only by reaching item it while item it - 2's buffer is
+    unfilled; the producer fills in order, so then no unit of items it - 2 and
+    it - 1 can have finished, and holding them takes 2 x units warps besides
+    the taker: with 2 x units + 1 warps the simulation finds such a pass,
+    with the kernel's units = warps it cannot happen."""
+    rng = np.random.default_rng(11)
+    for _ in range(300):
+        n = int(rng.integers(1, 9))
+        assert _unit_protocol_run(rng, n, n, int(rng.integers(1, 25))) == []
+    found = 0
+    for _ in range(100):
+        u = int(rng.integers(1, 4))
+        found += len(_unit_protocol_run(rng, 2 * u + 1, u, int(rng.integers(3, 25)))) > 0
+    assert found > 0
