@@ -14,18 +14,24 @@
 // between tiles, so a thread owns five rows of one tile and forms them from
 // two register rings of five along j (zop_tma.cu has the scheme): the direct
 // value w[i - j] and the reflected value of the column's class (w[i + j],
-// w[i + j - 2Z + 2], hB[i + j] = their sum, or zero), one load each per
-// column, one complex add per entry.
+// w[i + j - 2Z + 2], their sum, or zero), one complex add per entry.
 //
 // A persistent CTA takes items of pb frequencies (pb = 16 or 8: rows of 128
-// or 64 bytes) x a chunk of tiles (as many as two CTAs per SM hold
-// double buffered), the items of a chunk in frequency order (neighbouring
-// CTAs read neighbouring pieces of the same rows).  Two producer warps copy,
-// with cp.async from all lanes, the chunk's X rows and each tile's kernel rows
-// w[-kA .. 2Z-2] (rows outside the padded depth are zero rows written once),
-// the buffer's "full" mbarrier completing as they land; the compute warps
-// write each tile's hB, meet on a second mbarrier, and release the buffer on
-// its "empty" mbarrier.  Double buffered; every wait bounded.
+// or 64 bytes) x a chunk of tiles, the items of a chunk in frequency order
+// (neighbouring CTAs read neighbouring pieces of the same rows).  Two
+// producer warps copy, with cp.async from all lanes, the chunk's X rows and
+// each tile's kernel rows w[-kA .. 2Z-2] (rows outside the padded depth are
+// zero rows written once) into one of two buffers, whose "full" mbarrier
+// completes as they land; the compute warps release it on its "empty"
+// mbarrier.  Every wait is bounded.
+//
+// Two variants.  For zpad = Z - 1 (FULL) the column classes are fixed
+// (column 0, columns 1 .. Z - 2, column Z - 1) and the middle columns' sum
+// is formed as the ring is loaded (two rows per value): no hB rows, no zero
+// rows and no barrier between the compute warps, one tile per item, so a
+// CTA is small (51 KB at Z = 40) and four share an SM.  The generic variant
+// checks the class per column and reads the sum from hB rows that its compute
+// warps write per item into one of two regions, meeting on an mbarrier.
 #include <cuda.h>
 
 #include "deconv.cuh"
@@ -34,7 +40,7 @@ namespace {
 
 constexpr int kTI = 5;     // rows of a thread, the unroll of the column loop
 constexpr int kTiles = 5;  // tiles per item at most
-constexpr int kMaxBuf = 4;
+constexpr int kBufs = 2;   // operand buffers (double buffered)
 constexpr size_t kSmemMax = 112 * 1024;
 constexpr int kFullTiles = 1;  // tiles per item of the zpad = Z - 1 variant
 constexpr unsigned kWaitPolls = 1u << 24;
@@ -76,7 +82,6 @@ struct ZptArgs {
     long long plane, wstride;
     int ntpi;              // tiles per item (chunk), at most kTiles
     int ngroups, nitems;   // frequency groups of pb; items = tile chunks x groups, chunk-major
-    int nbuf;              // operand buffers (stages of the copy pipeline), at most kMaxBuf
     int kA;                // staged row of w[0]: 2Z - 2 rounded up to a multiple of 4
     int wrows;             // kernel rows per tile: kA + 2Z - 1
     unsigned xbytes;       // X bytes of a buffer (ntpi x Z x pb float2); the tiles' kernel rows follow
@@ -155,14 +160,14 @@ k_zpt_apply(float2 *__restrict__ S, const float2 *__restrict__ w, const ZptArgs 
     constexpr int kLPR = kPB / 2;    // copying lanes per row (16 bytes each)
     constexpr int kRPS = 32 / kLPR;  // rows a warp's copy instruction covers
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ __align__(8) uint64_t full[kMaxBuf], empty[kMaxBuf], hdone[2];
+    __shared__ __align__(8) uint64_t full[kBufs], empty[kBufs], hdone[2];
     const int Z = ZC > 0 ? ZC : a.Z;
     const int nig = Z / kTI;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int ncw = (kPB * nig * a.ntpi + 31) / 32;  // compute warps; the warps after them copy
     const int kb = a.kA, ko = kb - (2 * Z - 2);
     if (tid == 0) {
-        for (int b = 0; b < a.nbuf; ++b) {
+        for (int b = 0; b < kBufs; ++b) {
             mbar_init(&full[b], 32 * kProd);
             mbar_init(&empty[b], ncw);
         }
@@ -177,7 +182,7 @@ k_zpt_apply(float2 *__restrict__ S, const float2 *__restrict__ w, const ZptArgs 
             float2 *zr = reinterpret_cast<float2 *>(smem + a.zoff);
             for (int e = tid; e < (2 * Z + 3) * kPB; e += blockDim.x) zr[e] = make_float2(0.f, 0.f);
         }
-        for (int e = tid; e < a.nbuf * a.ntpi * a.wrows * kPB; e += blockDim.x) {
+        for (int e = tid; e < kBufs * a.ntpi * a.wrows * kPB; e += blockDim.x) {
             const int r = (e / kPB) % a.wrows, s = r - kb;
             if (s < -a.Zp || s >= a.Zp) {
                 const int tb = e / (kPB * a.wrows);  // buffer * ntpi + tile
@@ -197,7 +202,7 @@ k_zpt_apply(float2 *__restrict__ S, const float2 *__restrict__ w, const ZptArgs 
         const int rlo = max(kb - a.Zp, 0), rhi = min(a.wrows, kb + a.Zp);  // staged rows inside the padded depth
         int buf = 0, ph = 0;
         for (int item = blockIdx.x, it = 0; item < a.nitems; item += gridDim.x, ++it) {
-            const bool ok = it < a.nbuf || mbar_wait(&empty[buf], ph ^ 1);
+            const bool ok = it < kBufs || mbar_wait(&empty[buf], ph ^ 1);
             if (!__all_sync(0xffffffffu, ok)) {
                 if (lane == 0) atomicOr(a.err, 4u);
                 break;
@@ -230,7 +235,7 @@ k_zpt_apply(float2 *__restrict__ S, const float2 *__restrict__ w, const ZptArgs 
                 }
             }
             asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(&full[buf])) : "memory");
-            if (++buf == a.nbuf) buf = 0, ph ^= 1;
+            if (++buf == kBufs) buf = 0, ph ^= 1;
         }
         // no copy may still be landing when the CTA exits
         asm volatile("cp.async.wait_all;" ::: "memory");
@@ -344,7 +349,7 @@ k_zpt_apply(float2 *__restrict__ S, const float2 *__restrict__ w, const ZptArgs 
 #pragma unroll
             for (int q = 0; q < kTI; ++q) S[(t * Z + i0 + q) * a.plane + pg] = cscale(acc[q], f);
         }
-        if (++buf == a.nbuf) buf = 0, ph ^= 1;
+        if (++buf == kBufs) buf = 0, ph ^= 1;
     }
 }
 
@@ -362,8 +367,8 @@ size_t zpt_hbytes(int Z, int ntpi, int pb) {
 // shared memory of a CTA: the buffers, and for the generic variant the two hB
 // regions and the zero rows (the variant for zpad = Z - 1 sums the two
 // reflections as it reads them and has no column without one)
-size_t zpt_smem(int Z, int ntpi, int nbuf, int pb, bool full) {
-    const size_t bufs = nbuf * zpt_bufstride(Z, ntpi, pb, nullptr);
+size_t zpt_smem(int Z, int ntpi, int pb, bool full) {
+    const size_t bufs = kBufs * zpt_bufstride(Z, ntpi, pb, nullptr);
     return full ? bufs : bufs + 2 * zpt_hbytes(Z, ntpi, pb) + zpt_zero_bytes(Z, pb);
 }
 // zpad = Z - 1 (Z >= 10): the column classes at compile time
@@ -379,19 +384,17 @@ bool zpt_full(int Z, int zpad) { return zpad == Z - 1 && Z >= 2 * kTI; }
 // on that workload, against 5.81 ms with four buffers (two CTAs per SM) and
 // 6.68 ms for the generic variant's hB rows and per-item barrier.  The
 // generic variant takes two buffers of as many tiles as fit.
-int zpt_config(int Z, bool full, int *nbuf, int *pb) {
+int zpt_config(int Z, bool full, int *pb) {
     for (int w = 16; w >= 8; w /= 2) {
         if (full) {
-            if (zpt_smem(Z, kFullTiles, 2, w, true) <= kSmemMax && w * (Z / kTI) * kFullTiles <= kMaxCompute) {
-                *nbuf = 2;
+            if (zpt_smem(Z, kFullTiles, w, true) <= kSmemMax && w * (Z / kTI) * kFullTiles <= kMaxCompute) {
                 *pb = w;
                 return kFullTiles;
             }
             continue;
         }
         for (int n = kTiles; n >= 1; --n)
-            if (zpt_smem(Z, n, 2, w, false) <= kSmemMax && w * (Z / kTI) * n <= kMaxCompute) {
-                *nbuf = 2;
+            if (zpt_smem(Z, n, w, false) <= kSmemMax && w * (Z / kTI) * n <= kMaxCompute) {
                 *pb = w;
                 return n;
             }
@@ -403,8 +406,8 @@ int zpt_config(int Z, bool full, int *nbuf, int *pb) {
 
 int mm_zpt_supported(int Z, int zpad, int nt, long long plane) {
     if (Z < kTI || Z % kTI != 0 || Z > kMaxZ || zpad < 1 || zpad > Z - 1 || nt < 1 || plane % 2 != 0) return 0;
-    int nb, pb;
-    return zpt_config(Z, zpt_full(Z, zpad), &nb, &pb) > 0;
+    int pb;
+    return zpt_config(Z, zpt_full(Z, zpad), &pb) > 0;
 }
 
 int mm_launch_zpt_apply(float2 *S, const float2 *w, long long wstride, int Z, int zpad, int Zp, long long plane,
@@ -422,7 +425,7 @@ int mm_launch_zpt_apply(float2 *S, const float2 *w, long long wstride, int Z, in
     a.wstride = wstride;
     const bool full = zpt_full(Z, zpad);
     int pb = 0;
-    a.ntpi = zpt_config(Z, full, &a.nbuf, &pb);
+    a.ntpi = zpt_config(Z, full, &pb);
     a.ngroups = (int)((plane + pb - 1) / pb);
     const long long nitems = (long long)a.ngroups * ((nt + a.ntpi - 1) / a.ntpi);
     MM_REQUIRE(nitems < (1LL << 31), "z operator: too many items");
@@ -430,7 +433,7 @@ int mm_launch_zpt_apply(float2 *S, const float2 *w, long long wstride, int Z, in
     a.kA = zpt_ka(Z);
     a.wrows = a.kA + 2 * Z - 1;
     a.bufstride = (unsigned)zpt_bufstride(Z, a.ntpi, pb, &a.xbytes);
-    a.hoff = a.nbuf * a.bufstride;
+    a.hoff = kBufs * a.bufstride;
     a.hbytes = (unsigned)zpt_hbytes(Z, a.ntpi, pb);
     a.zoff = a.hoff + 2 * a.hbytes;
     a.nseg = 0;
@@ -447,7 +450,7 @@ int mm_launch_zpt_apply(float2 *S, const float2 *w, long long wstride, int Z, in
     }
     a.fresp = fresp;
     a.err = err;
-    const size_t sm = zpt_smem(Z, a.ntpi, a.nbuf, pb, full);
+    const size_t sm = zpt_smem(Z, a.ntpi, pb, full);
     const int threads = zpt_block(Z, a.ntpi, pb);
     const void *fn;
     if (pb == 16)
