@@ -129,6 +129,23 @@ def test_default_batch_takes_all_tiles_within_the_scratch_budget(monkeypatch):
     assert tune.zform_for(d, (40, 3000, 3000), dapi=True) == 0  # MM_ZFORM_AUTO
 
 
+def test_tuner_z_forms_per_deconvolver():
+    """tune.zforms: with one PSF, the register, tensor, shared-memory, direct
+    and transform forms; with a PSF per tile, the register form (each tile's
+    matrix from its own z kernel), the direct sum and the transforms; without
+    z kernels, the transforms only."""
+    import types
+    from mermake_gb300 import tune
+    L = _lib
+    one = types.SimpleNamespace(z_operator=object(), psf_fft=np.zeros((1, 2)))
+    grid = types.SimpleNamespace(z_operator=object(), psf_fft=np.zeros((100, 2)))
+    none = types.SimpleNamespace(z_operator=None, psf_fft=np.zeros((1, 2)))
+    assert tune.zforms(one) == [L.MM_ZFORM_REGISTERS, L.MM_ZFORM_TENSOR, L.MM_ZFORM_SHARED, L.MM_ZFORM_DIRECT,
+                                L.MM_ZFORM_TRANSFORMS]
+    assert tune.zforms(grid) == [L.MM_ZFORM_REGISTERS, L.MM_ZFORM_DIRECT, L.MM_ZFORM_TRANSFORMS]
+    assert tune.zforms(none) == [L.MM_ZFORM_TRANSFORMS]
+
+
 def test_spot_capacity_grows_from_counts_seen():
     """The drivers size the output rows from the largest count a Deconvolver
     has returned for the shape (plus a quarter), so a FOV with more spots than
